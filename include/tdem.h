@@ -1,0 +1,164 @@
+/*
+ * tdem.h - C ABI of the GB300 (sm_103a) 2-D DEM step library, libtdem_sm103.so.
+ *
+ * Plain C: opaque handles, plain pointers and sizes. Device pointers are CUDA
+ * device addresses (for example torch.Tensor.data_ptr() of a contiguous CUDA
+ * tensor); host pointers are ordinary (ideally pinned) host memory. A
+ * `void* stream` is a cudaStream_t (NULL = the legacy default stream).
+ *
+ * Every function returns an int status: TDEM_OK (0) or one of the TDEM_ERR_*
+ * codes below; the text of the last error of a handle is available from
+ * tdem_last_error(). Handles are not re-entrant: one handle per stream.
+ *
+ * Two engines sit behind this ABI:
+ *
+ *  1. "icedem": the reference mode. It reproduces, in FP64, the step of the
+ *     reference's `IceDEM` (src/tensordem/dem.py:75-624): central-force bonds
+ *     on the square+diagonal lattice, tensile and objective-shear breakage,
+ *     linear penalty contacts with a no-tension clamp, a circular indenter or
+ *     a polyline hull, linear drag, semi-implicit Euler and the accounting
+ *     ledger. The state arrays are owned by the caller (the Python drop-in
+ *     keeps them as torch tensors) and passed on every call.
+ *
+ *  2. "hm": the spec mode, a 2-D Hertz-Mindlin disc engine: cell-list
+ *     contact detection with a Verlet skin, Hertz normal + Tsuji dashpot,
+ *     Mindlin tangential spring with Coulomb cap and per-contact history,
+ *     bonded-particle normal/shear springs with irreversible tensile and
+ *     objective-shear breakage, planar walls, a circular indenter, gravity and
+ *     velocity-Verlet. FP32 per-contact arithmetic on FP32 offsets from an
+ *     integer cell origin; compensated (float-float) per-particle sums; FP64
+ *     ledger. Its state lives in the handle, in HBM.
+ */
+#ifndef TDEM_H_
+#define TDEM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  TDEM_OK = 0,
+  TDEM_ERR_BADARG = 1,    /* invalid argument: maps to ValueError */
+  TDEM_ERR_CUDA = 2,      /* a CUDA runtime call failed: RuntimeError */
+  TDEM_ERR_NONFINITE = 3, /* non-finite state after a step: FloatingPointError */
+  TDEM_ERR_CAPACITY = 4,  /* a fixed-capacity buffer overflowed: RuntimeError */
+  TDEM_ERR_STATE = 5      /* call out of order (e.g. no state uploaded) */
+};
+
+/* Library version, for a loader's sanity check. */
+int tdem_version(void);
+
+/* ========================================================================
+ * 1. Reference mode ("icedem")
+ * ====================================================================== */
+
+typedef struct tdem_icedem tdem_icedem;
+
+/* Constant configuration of one IceDEM instance. Field meaning follows the
+ * reference's DEMConfig (src/tensordem/dem.py:17-72); `mass` is the disc mass
+ * rho*pi*r^2*t and `dt` the resolved step (config.dt or recommended_dt). */
+typedef struct {
+  int32_t n;                /* number of discs, 2 <= n <= tdem_icedem_max_discs() */
+  double radius;
+  double mass;
+  double bond_stiffness;
+  double contact_stiffness;
+  double breaking_strain;
+  double shear_breaking_strain;
+  double contact_damping;
+  double drag;
+  double tool_radius;
+  double dt;
+  double tool_start[2];     /* dem.py:146-150 */
+  double tool_velocity[2];  /* dem.py:151-153 */
+  int32_t hull_vertices;    /* 0: circular tool; >= 2: polyline hull (dem.py:154-169) */
+  const double* hull_profile_host; /* (hull_vertices, 2) host, local hull vertices */
+  double hull_start[2];
+  double hull_velocity[2];
+} tdem_icedem_config;
+
+/* Caller-owned state, device pointers, passed on every call. Pair-indexed
+ * arrays use the reference's all-pairs order: pair p = (i, j), i < j, in the
+ * row-major order of triu_indices(n, n, 1) (dem.py:116-118). */
+typedef struct {
+  double* positions;             /* (n, 2) m */
+  double* velocities;            /* (n, 2) m/s */
+  const double* initial_positions; /* (n, 2) m */
+  const uint8_t* fixed;          /* (n,) bool */
+  uint8_t* alive;                /* (P,) bool, P = n(n-1)/2 */
+  uint8_t* failure_mode;         /* (P,) 0 intact, 1 tensile, 2 shear, 3 both */
+  double* failure_time_s;        /* (P,) */
+  double* failure_extension_m;   /* (P,) */
+  double* failure_energy_J;      /* (P,) */
+} tdem_icedem_state;
+
+/* Ledger slots of tdem_icedem_read_ledger / tdem_icedem_write_ledger. The
+ * first 13 are the reference's `accounting` dict (dem.py:139-144) in this
+ * order; the rest mirror `last_step` (dem.py:372-376) and diagnostics. */
+enum {
+  TDEM_L_EXTERNAL_WORK = 0, TDEM_L_FRACTURE_RELEASE, TDEM_L_CONTACT_ACQUIRED,
+  TDEM_L_TOOL_WORK, TDEM_L_DAMPING_DISSIPATION,
+  TDEM_L_EXTERNAL_IMPULSE_X, TDEM_L_EXTERNAL_IMPULSE_Y,
+  TDEM_L_SUPPORT_IMPULSE_X, TDEM_L_SUPPORT_IMPULSE_Y,
+  TDEM_L_DRAG_IMPULSE_X, TDEM_L_DRAG_IMPULSE_Y,
+  TDEM_L_TOOL_IMPULSE_X, TDEM_L_TOOL_IMPULSE_Y,
+  TDEM_L_LAST_SUPPORT_X = 13, TDEM_L_LAST_SUPPORT_Y,
+  TDEM_L_LAST_REACTION_X, TDEM_L_LAST_REACTION_Y,
+  TDEM_L_LAST_EXTERNAL_X, TDEM_L_LAST_EXTERNAL_Y,
+  TDEM_L_LAST_EXTERNAL_WORK, TDEM_L_LAST_EXTERNAL_MOMENT,
+  TDEM_L_LAST_TIME_START, TDEM_L_LAST_TIME_END,
+  TDEM_L_DAMPING_POWER, TDEM_L_TOOL_POWER,
+  TDEM_L_MIN_BREAK_MARGIN, /* min over steps/alive bonds of the relative distance to a threshold */
+  TDEM_L_COUNT = 32
+};
+
+/* Largest disc count of one reference-mode instance (one CTA holds it). */
+int tdem_icedem_max_discs(void);
+
+/* Build the instance: bond topology from `initial_positions_host` ((n,2),
+ * bonds where |x_j - x_i| <= 2 r sqrt(2) (1 + 1e-10), dem.py:119-124), the
+ * per-disc bond lists in the reference's accumulation order, and the constant
+ * pseudo-inverse of each disc's bond covariance (dem.py:194-202).
+ * Replaces IceDEM.__init__ (dem.py:86-169). */
+int tdem_icedem_create(const tdem_icedem_config* cfg, const double* initial_positions_host,
+                       tdem_icedem** out);
+void tdem_icedem_destroy(tdem_icedem* h);
+
+/* Number of bonds found at create time and their pair indices (host out, int64). */
+int tdem_icedem_num_bonds(const tdem_icedem* h);
+int tdem_icedem_bond_pairs(const tdem_icedem* h, int64_t* out_pair_index_host);
+
+/* One force evaluation at `time`: commits breaks and their ledger entries and
+ * writes the total force (n,2) and the ice-on-tool reaction (2) to device
+ * buffers. `loads` is an optional (n,2) device array of external nodal
+ * forces (NULL = none). Replaces IceDEM.forces (dem.py:226-345). */
+int tdem_icedem_forces(tdem_icedem* h, const tdem_icedem_state* st, const double* loads,
+                       double time, double* out_force, double* out_reaction, void* stream);
+
+/* `n_steps` semi-implicit Euler steps from `time` in one launch (loads, if
+ * given, are held over all of them). Replaces IceDEM.step (dem.py:347-382).
+ * Returns TDEM_ERR_NONFINITE (after finishing the offending step, as the
+ * reference does) when the state stops being finite; the call synchronizes
+ * `stream` to read that status. */
+int tdem_icedem_step(tdem_icedem* h, const tdem_icedem_state* st, const double* loads,
+                     int n_steps, double time, void* stream);
+
+/* Steps completed by the last tdem_icedem_step call (less than requested only
+ * when it stopped on a non-finite state). */
+int tdem_icedem_steps_done(const tdem_icedem* h);
+
+/* Ledger transfer (host doubles, up to TDEM_L_COUNT). Synchronizes `stream`. */
+int tdem_icedem_read_ledger(tdem_icedem* h, double* out_host, int count, void* stream);
+int tdem_icedem_write_ledger(tdem_icedem* h, const double* in_host, int count, void* stream);
+
+/* Text of the last error of `h` (or of the last failed create when h is NULL). */
+int tdem_icedem_last_error(const tdem_icedem* h, char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDEM_H_ */

@@ -1,0 +1,124 @@
+"""ctypes binding of libtdem_sm103.so (the C ABI declared in include/tdem.h).
+
+There is no fallback: if the library is missing or fails to load, every call
+raises. The library is built in-tree by ``tensordem_gb300.build``.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from .build import LIB
+
+TDEM_OK = 0
+TDEM_ERR_BADARG = 1
+TDEM_ERR_CUDA = 2
+TDEM_ERR_NONFINITE = 3
+TDEM_ERR_CAPACITY = 4
+TDEM_ERR_STATE = 5
+
+# Ledger slots (include/tdem.h, TDEM_L_*)
+L_EXTERNAL_WORK = 0
+L_FRACTURE_RELEASE = 1
+L_CONTACT_ACQUIRED = 2
+L_TOOL_WORK = 3
+L_DAMPING_DISSIPATION = 4
+L_IMPULSES = 5  # 8 values: external, support, drag, tool (x, y each)
+L_LAST_SUPPORT = 13
+L_LAST_REACTION = 15
+L_LAST_EXTERNAL = 17
+L_LAST_EXTERNAL_WORK = 19
+L_LAST_EXTERNAL_MOMENT = 20
+L_LAST_TIME_START = 21
+L_LAST_TIME_END = 22
+L_DAMPING_POWER = 23
+L_TOOL_POWER = 24
+L_MIN_BREAK_MARGIN = 25
+L_COUNT = 32
+
+
+class IceDEMConfigC(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("radius", C.c_double), ("mass", C.c_double),
+        ("bond_stiffness", C.c_double), ("contact_stiffness", C.c_double),
+        ("breaking_strain", C.c_double), ("shear_breaking_strain", C.c_double),
+        ("contact_damping", C.c_double), ("drag", C.c_double),
+        ("tool_radius", C.c_double), ("dt", C.c_double),
+        ("tool_start", C.c_double * 2), ("tool_velocity", C.c_double * 2),
+        ("hull_vertices", C.c_int32),
+        ("hull_profile_host", C.POINTER(C.c_double)),
+        ("hull_start", C.c_double * 2), ("hull_velocity", C.c_double * 2),
+    ]
+
+
+class IceDEMStateC(C.Structure):
+    _fields_ = [
+        ("positions", C.c_void_p), ("velocities", C.c_void_p),
+        ("initial_positions", C.c_void_p), ("fixed", C.c_void_p),
+        ("alive", C.c_void_p), ("failure_mode", C.c_void_p),
+        ("failure_time_s", C.c_void_p), ("failure_extension_m", C.c_void_p),
+        ("failure_energy_J", C.c_void_p),
+    ]
+
+
+_lock = threading.Lock()
+_lib: C.CDLL | None = None
+
+
+def _declare(lib: C.CDLL) -> None:
+    vp, i32, dbl = C.c_void_p, C.c_int, C.c_double
+    sig = {
+        "tdem_version": (i32, []),
+        "tdem_icedem_max_discs": (i32, []),
+        "tdem_icedem_create": (i32, [C.POINTER(IceDEMConfigC), C.POINTER(C.c_double), C.POINTER(vp)]),
+        "tdem_icedem_destroy": (None, [vp]),
+        "tdem_icedem_num_bonds": (i32, [vp]),
+        "tdem_icedem_bond_pairs": (i32, [vp, C.POINTER(C.c_int64)]),
+        "tdem_icedem_forces": (i32, [vp, C.POINTER(IceDEMStateC), vp, dbl, vp, vp, vp]),
+        "tdem_icedem_step": (i32, [vp, C.POINTER(IceDEMStateC), vp, i32, dbl, vp]),
+        "tdem_icedem_steps_done": (i32, [vp]),
+        "tdem_icedem_read_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
+        "tdem_icedem_write_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
+        "tdem_icedem_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib() -> C.CDLL:
+    """Load (once) and return the native library; raise if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = Path(LIB)
+            if not path.exists():
+                raise RuntimeError(
+                    f"{path} is missing: build it with `python -m tensordem_gb300.build` "
+                    "(CUDA toolkit with sm_103a support required); there is no CPU fallback")
+            handle = C.CDLL(str(path), mode=C.RTLD_GLOBAL)
+            _declare(handle)
+            _lib = handle
+    return _lib
+
+
+def last_error(fn_name: str, handle) -> str:
+    buf = C.create_string_buffer(1024)
+    lib().tdem_icedem_last_error(handle, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, handle, what: str) -> None:
+    """Map a TDEM status to the reference's exception types."""
+    if rc == TDEM_OK:
+        return
+    msg = last_error(what, handle) or what
+    if rc == TDEM_ERR_BADARG:
+        raise ValueError(msg)
+    if rc == TDEM_ERR_NONFINITE:
+        raise FloatingPointError(msg)
+    raise RuntimeError(f"{what}: {msg} (status {rc})")

@@ -1,0 +1,83 @@
+"""Pin the numpy IceDEM oracle to golden vectors produced by the reference.
+
+The fixtures in ``tests/golden`` come from the reference ``IceDEM``
+(``src/tensordem/dem.py``) run by ``tests/golden/make_golden.py``. These tests
+run on CPU and need no GPU.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle.icedem import IceDEMOracle, OracleConfig
+from tests import _icedem_parity as P
+
+
+def _oracle_from(g, **extra):
+    cfg = P.config_dict(g)
+    return IceDEMOracle(OracleConfig(**cfg), **extra)
+
+
+@pytest.mark.parametrize("name", ["demo_b0.01_s0.02", "demo_b0.015_s0.03"])
+def test_demo_break_sequence_and_frames(name):
+    g = P.load(name)
+    sim = _oracle_from(g)
+    worst = P.replay(g, sim, to_np=np.asarray)
+    assert sim.broken_bonds == int((g["failure_mode"] > 0).sum())
+    assert worst["force"] < P.RTOL
+
+
+def test_demo_break_counts_match_reference_runs():
+    # 2000 steps then a final forces() evaluation at t = 2000 dt.
+    assert int((P.load("demo_b0.01_s0.02")["failure_mode"] > 0).sum()) == 252
+    assert int((P.load("demo_b0.015_s0.03")["failure_mode"] > 0).sum()) == 230
+    assert str(P.load("demo_b0.015_s0.03")["break_digest"]) == "111527dd778f1d6f"
+
+
+def test_reproducibility_case():
+    g = P.load("repro_7x3")
+    P.replay(g, _oracle_from(g), to_np=np.asarray)
+
+
+def test_hull_case():
+    g = P.load("hull_9x3")
+    sim = _oracle_from(g, hull_profile=g["hull_profile"], hull_start=tuple(g["hull_start"]),
+                       hull_velocity=tuple(g["hull_velocity"]))
+    P.replay(g, sim, to_np=np.asarray)
+
+
+def test_external_loads_case():
+    g = P.load("loads_5x3")
+    sim = _oracle_from(g)
+    P.replay(g, sim, to_np=np.asarray, loads_fn=lambda s: g["loads"][s])
+
+
+@pytest.mark.parametrize("case", ["shear", "rotation", "tension", "compress", "contact",
+                                  "coincident", "tool"])
+def test_unit_force_cases(case):
+    g = P.load("unit_cases")
+    if case == "tool":
+        sim = IceDEMOracle(OracleConfig(nx=5, ny=3))
+        sim.time = 0.02
+    elif case in ("shear",):
+        sim = IceDEMOracle(OracleConfig(nx=3, ny=2, drag=0, fix_edges=False,
+                                        shear_breaking_strain=0.02, breaking_strain=0.5))
+    else:
+        sim = IceDEMOracle(OracleConfig(nx=3, ny=2, drag=0, fix_edges=False))
+    sim.positions = g[f"{case}_pos"].copy()
+    sim.velocities = g[f"{case}_vel"].copy()
+    if case == "compress":
+        sim.alive[sim.bonded] = False
+    else:
+        sim.alive[sim.bonded] = g[f"{case}_alive_in"]
+    f, r = sim.forces()
+    assert P.normwise(f, g[f"{case}_force"], floor=1e-300) <= P.RTOL or \
+        np.abs(f - g[f"{case}_force"]).max() <= 1e-12
+    assert np.array_equal(sim.alive[sim.bonded], g[f"{case}_alive"])
+
+
+def test_recommended_dt_matches_reference_value():
+    g = P.load("demo_b0.01_s0.02")
+    assert OracleConfig().recommended_dt == float(g["dt"])
+    assert math.isclose(float(g["dt"]), 6.8788e-05, rel_tol=1e-4)
