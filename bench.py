@@ -1,0 +1,304 @@
+"""Benchmark of the 2-D Hertz-Mindlin DEM step on GB300 (one JSON line on rank 0).
+
+Workload: the seeded 1,048,576-disc polydisperse settling case (radii
+U[0.8, 1.2] mm, rho 2500, E 70 GPa, nu 0.25, mu 0.5, e 0.8, jittered grid at
+area fraction 0.55, four walls, gravity, dt = 0.2 Rayleigh time), FP32
+contacts with compensated sums and an FP64 ledger. A bench step is one
+velocity-Verlet DEM step of all discs; the run's state is device-resident and
+L2 is flushed (a buffer larger than L2 written, then read) before every timed
+step, outside its CUDA-event bracket.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: the path does not shard in this build ("replicas only"): under
+torchrun every rank runs its own replica (seeded by rank) and the line reports
+the aggregate particle-steps/s over the slowest rank's time (weak scaling).
+``--impl reference`` times the CPU oracle (the FP64 restatement of the
+reference's algorithm, oracle/hm2d.py) on a bounded sample of the same
+workload on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s @1M discs"
+UNIT = "particle-steps/s"
+N_SIDE = 1024
+L2_FLUSH_BYTES = 256 << 20
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _args():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10000, help="timed DEM steps (the full 10,000-step run)")
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--cpu-sample-steps", type=int, default=100)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload_config(seed: int = 0) -> dict:
+    return {"workload": "2-D polydisperse Hertz-Mindlin disc settling, 1,048,576 discs "
+                        "(1024x1024 jittered grid, area fraction 0.55, 4 walls, gravity), "
+                        "radii U[0.8,1.2] mm, E 70 GPa, nu 0.25, mu 0.5, e 0.8, dt 0.2 Rayleigh",
+            "discs": N_SIDE * N_SIDE, "seed": seed, "precision": "fp32 contacts, compensated sums, fp64 ledger",
+            "l2": "flushed before every timed step (256 MiB written, another 256 MiB read)",
+            "parallelism": "replicas"}
+
+
+# ----------------------------------------------------------------- CPU side
+def cpu_oracle_rate(steps: int) -> dict:
+    """Time the numpy FP64 oracle on the same workload (bounded sample)."""
+    from oracle.hm2d import HM2DOracle, HMParams
+    from tensordem_gb300.hm2d import granular_gas_case
+    cfg, st = granular_gas_case(N_SIDE, seed=0)
+    p = HMParams(young=cfg.young, poisson=cfg.poisson, restitution=cfg.restitution, mu=cfg.mu,
+                 mu_wall=cfg.mu_wall, dt=cfg.dt, gravity=cfg.gravity, box=cfg.box, skin=cfg.skin)
+    o = HM2DOracle(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"], p)
+    o.prime()
+    o.step(2)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    return {"value": cfg.n * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} velocity-Verlet steps of the full 1,048,576-disc case after a 3-step "
+                      f"warm-up, numpy FP64 oracle (oracle/hm2d.py), one host thread, {dt:.1f} s"}
+
+
+def run_reference(a) -> None:
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    steps = max(1, min(a.steps, a.cpu_sample_steps))
+    cb = cpu_oracle_rate(steps)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * (N_SIDE * N_SIDE) / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(),
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU side
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic() -> float | None:
+    """DRAM bytes per step-kernel launch from the committed ncu summary (1M discs)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "hm_step_1M_traffic.json")) as f:
+            return float(json.load(f)["dram_bytes_per_launch"])
+    except Exception:
+        return None
+
+
+def algorithmic_bytes(n: int, head_bytes: int, contact_sides: int) -> int:
+    """Bytes one step must move: state read + write (pos, vel: 2 x 2 x 16 B per
+    disc), the list head (16 B per disc) and the tangential history of every
+    touching contact side (8 B read + 8 B write)."""
+    return n * (64 + head_bytes) + 16 * contact_sides
+
+
+def run_ours(a) -> None:
+    import torch
+
+    from tensordem_gb300.hm2d import HM2D, granular_gas_case
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg, st = granular_gas_case(N_SIDE, seed=rank)
+    eng = HM2D(cfg, device=dev)
+    eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
+    tuning = eng.autotune(steps=10)
+    eng.step(max(3, a.warmup))
+    # L2 flush: write one buffer larger than L2, then read another, so the
+    # cache is left holding clean, unrelated lines (no write-backs in the step)
+    flush_w = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    flush_r = torch.ones(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def flush_l2():
+        flush_w.fill_(1.0)
+        flush_r.sum()
+
+    stream = torch.cuda.current_stream(dev)
+    led0 = eng.ledger()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for e0, e1 in evs:
+            flush_l2()
+            e0.record(stream)
+            eng.step(1, check=False)
+            e1.record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+    eng.check()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        torch.distributed.barrier()
+    led1 = eng.ledger()
+    rebuilds = led1["rebuilds"] - led0["rebuilds"]
+    clk = clocks.summary()
+    n = cfg.n
+    value = world * n * a.steps / (total_ms / 1e3)
+
+    # contacts touching at the end of the run (for the algorithmic byte count)
+    hist = eng.history()
+    contact_sides = 2 * len(hist)
+    alg = algorithmic_bytes(n, 16, contact_sides)
+    peak, peak_kind = measured_peak()
+    achieved = alg / (total_ms / a.steps / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profiled_traffic(), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_step": alg}
+
+    # end to end through the C ABI with host buffers (rank-local)
+    import numpy as np
+    e2e_eng = HM2D(cfg, device=dev)
+    e2e_eng.variant = eng.variant
+    host = {k: np.ascontiguousarray(v) for k, v in st.items()}
+    out_pos = np.empty((n, 2))
+    out_vel = np.empty((n, 2))
+    out_om = np.empty(n)
+    flush_l2()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    e2e_eng.set_state(host["pos"], host["vel"], host["omega"], host["radius"], host["mass"], host["inertia"])
+    e2e_eng.step(a.steps, check=False)
+    e2e_eng.read_state_host(out_pos, out_vel, out_om)
+    e2e_s = time.perf_counter() - t0
+    e2e_eng.check()
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = 8 * n * (2 + 2 + 1 + 1 + 1 + 1)
+    d2h = 8 * n * (2 + 2 + 1)
+    e2e = {"value": world * n * a.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
+           "note": "one solve through tdem_hm_set_state/step/read_state with host arrays: upload, "
+                   f"{a.steps} steps, download; L2 flushed before it"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        cpu = cpu_oracle_rate(max(1, a.cpu_sample_steps))
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": workload_config(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": a.steps * 2 + 11 * rebuilds,
+                "clocks": clk,
+                "extra": {"variant": eng.variant, "autotune_ms_per_10_steps": tuning,
+                          "rebuilds_in_timed_region": rebuilds, "wall_s_timed_loop": wall,
+                          "max_neighbors_seen": led1["max_neighbors"],
+                          "touching_contacts_end": len(hist)}}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

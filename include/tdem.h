@@ -157,6 +157,113 @@ int tdem_icedem_write_ledger(tdem_icedem* h, const double* in_host, int count, v
 /* Text of the last error of `h` (or of the last failed create when h is NULL). */
 int tdem_icedem_last_error(const tdem_icedem* h, char* buf, size_t len);
 
+/* ========================================================================
+ * 2. North-star mode ("hm"): 2-D Hertz-Mindlin discs
+ * ====================================================================== */
+
+typedef struct tdem_hm tdem_hm;
+
+/* Configuration. The box is [0, ncx*cell] x [0, ncy*cell]; walls sit on its
+ * edges (bit 0 left x=0, bit 1 right, bit 2 bottom y=0, bit 3 top). `cell`
+ * must be >= 2 r_max + skin. Material: E, nu, restitution (Tsuji damping),
+ * particle and wall friction. Contact law as the reference's Hertz-Mindlin
+ * pieces: src/tensordem/scale_ceiling/kernel.py:277-401,
+ * src/tensordem/hertz_mindlin.py:94-176, src/tensordem/granular2d/engine.py:458-503. */
+typedef struct {
+  int32_t n;              /* particles */
+  int32_t precision;      /* 32: FP32 contacts, compensated sums; 64: plain FP64 */
+  int32_t max_neighbors;  /* candidate slots per particle, 1..24 */
+  int32_t walls;          /* wall bit mask */
+  int32_t ncx, ncy;       /* cell grid */
+  double cell;            /* cell edge (m) */
+  double skin;            /* Verlet skin (m) */
+  double dt;              /* time step (s) */
+  double young, poisson, restitution, mu, mu_wall;
+  double gravity[2];      /* m/s^2 */
+  double inertia_factor;  /* I = inertia_factor * m * r^2 (0.5 for uniform discs) */
+} tdem_hm_config;
+
+/* Ledger slots of tdem_hm_read_ledger (J unless noted). */
+enum {
+  TDEM_HM_L_KINETIC = 0,     /* translational + rotational */
+  TDEM_HM_L_POTENTIAL = 1,   /* gravitational, -sum m g.x */
+  TDEM_HM_L_HERTZ = 2,       /* normal elastic 0.4 F_el delta */
+  TDEM_HM_L_TANGENTIAL = 3,  /* tangential spring 0.5 S_t |xi|^2 */
+  TDEM_HM_L_TOTAL = 4,       /* sum of the above + dissipated */
+  TDEM_HM_L_DISSIPATED = 5,  /* cumulative dashpot + Coulomb slip loss */
+  TDEM_HM_L_EVALS = 6,       /* committed force evaluations */
+  TDEM_HM_L_REBUILDS = 7,    /* neighbour-list rebuilds */
+  TDEM_HM_L_MAX_NEIGHBORS = 8, /* largest candidate count at the last rebuild */
+  TDEM_HM_L_STATUS = 9,      /* device status bits */
+  TDEM_HM_L_COUNT = 16
+};
+
+/* Allocate the engine (all device buffers sized for n). Replaces the
+ * reference engines' constructors: FloeBed.__init__
+ * (src/tensordem/scale_ceiling/kernel.py:147-197) and DiskSystem.__init__
+ * (src/tensordem/granular2d/engine.py:147-211). */
+int tdem_hm_create(const tdem_hm_config* cfg, tdem_hm** out);
+void tdem_hm_destroy(tdem_hm* h);
+
+/* Upload a state in original particle order (FP64: positions (n,2),
+ * velocities (n,2), omega (n), radius (n), mass (n), moment of inertia (n));
+ * host=1: host pointers (staged through pinned memory), host=0: device
+ * pointers. Builds the first neighbour list (cell list, kernel.py:230-266,
+ * src/tensordem/scale_ceiling/search.py:60-162). */
+int tdem_hm_set_state(tdem_hm* h, const double* pos, const double* vel, const double* omega,
+                      const double* radius, const double* mass, const double* inertia, int host,
+                      void* stream);
+
+/* Advance n velocity-Verlet steps (FloeBed.step, kernel.py:410-419), list
+ * rebuilds and history remap included (kernel.py:230-274). Asynchronous:
+ * check tdem_hm_status afterwards. */
+int tdem_hm_step(tdem_hm* h, int64_t n_steps, void* stream);
+
+/* Integer-time state in original order: positions, velocities, omega, total
+ * force (incl. gravity), torque; any output may be NULL. host=1: host
+ * pointers (synchronizes), host=0: device pointers. */
+int tdem_hm_read_state(tdem_hm* h, double* pos, double* vel, double* omega, double* force,
+                       double* torque, int host, void* stream);
+
+/* Energy ledger and counters (TDEM_HM_L_*) into host doubles; synchronizes.
+ * Mirrors FloeBed.energy_ledger (kernel.py:483-487) plus the dissipation
+ * ledger of DiskSystem (granular2d/engine.py:576-588). */
+int tdem_hm_read_ledger(tdem_hm* h, double* out_host, int count, void* stream);
+
+/* Synchronize and map the device status: TDEM_ERR_NONFINITE, TDEM_ERR_CAPACITY. */
+int tdem_hm_status(tdem_hm* h, void* stream);
+
+/* Current candidate pairs as original ids (i < j), for verification against a
+ * brute-force search (tests/test_scale_ceiling_dem.py:41-50). Writes up to
+ * `capacity` pairs to out_host ((capacity, 2) int32) and the total to *count. */
+int tdem_hm_read_pairs(tdem_hm* h, int32_t* out_host, int64_t capacity, int64_t* count, void* stream);
+
+/* Rebuild the neighbour list now (sort by cell, candidates, history remap),
+ * as FloeBed.build_neighbours(keep_state=True) does
+ * (src/tensordem/scale_ceiling/kernel.py:230-266). */
+int tdem_hm_rebuild(tdem_hm* h, void* stream);
+
+/* Stored tangential history of every pair with a non-zero value: original ids
+ * (lo, hi) into pairs ((capacity, 2) int32, host) and the displacement of lo
+ * relative to hi into xi ((capacity, 2) double, host). The reference keeps the
+ * same state keyed by i*N+j (src/tensordem/granular2d/engine.py:388-396). */
+int tdem_hm_read_history(tdem_hm* h, int32_t* pairs, double* xi, int64_t capacity, int64_t* count,
+                         void* stream);
+
+/* Step-kernel variants (launch shapes) and the autotuner that picks one by
+ * timing `steps` steps of each on the live state (the simulation advances by
+ * tdem_hm_num_variants() * (steps + 2) steps). ms_out (optional, host) gets
+ * one time per variant. All variants compute bit-identical particle states. */
+int tdem_hm_num_variants(void);
+int tdem_hm_set_variant(tdem_hm* h, int variant);
+int tdem_hm_get_variant(const tdem_hm* h);
+int tdem_hm_autotune(tdem_hm* h, int steps, float* ms_out, void* stream);
+
+/* 1 (default): steps run as one conditional CUDA graph launch; 0: plain launches. */
+int tdem_hm_use_graph(tdem_hm* h, int on);
+
+int tdem_hm_last_error(const tdem_hm* h, char* buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,9 @@ All compute runs in hand-written CUDA kernels of ``libtdem_sm103.so`` (built by
 ``python -m tensordem_gb300.build``); there is no CPU fallback.
 """
 
+from . import hm2d
 from .dem import ADDITIVE_ACCOUNTING_KEYS, DEMConfig, IceDEM
+from .hm2d import HM2D, HM2DConfig, granular_gas_case
 
-__all__ = ["ADDITIVE_ACCOUNTING_KEYS", "DEMConfig", "IceDEM"]
+__all__ = ["ADDITIVE_ACCOUNTING_KEYS", "DEMConfig", "IceDEM", "HM2D", "HM2DConfig",
+           "granular_gas_case", "hm2d"]

@@ -64,6 +64,22 @@ class IceDEMStateC(C.Structure):
     ]
 
 
+class HMConfigC(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32), ("precision", C.c_int32), ("max_neighbors", C.c_int32),
+        ("walls", C.c_int32), ("ncx", C.c_int32), ("ncy", C.c_int32),
+        ("cell", C.c_double), ("skin", C.c_double), ("dt", C.c_double),
+        ("young", C.c_double), ("poisson", C.c_double), ("restitution", C.c_double),
+        ("mu", C.c_double), ("mu_wall", C.c_double), ("gravity", C.c_double * 2),
+        ("inertia_factor", C.c_double),
+    ]
+
+
+# Hertz-Mindlin ledger slots (TDEM_HM_L_*)
+HM_KINETIC, HM_POTENTIAL, HM_HERTZ, HM_TANGENTIAL, HM_TOTAL, HM_DISSIPATED = range(6)
+HM_EVALS, HM_REBUILDS, HM_MAX_NEIGHBORS, HM_STATUS = 6, 7, 8, 9
+HM_COUNT = 16
+
 _lock = threading.Lock()
 _lib: C.CDLL | None = None
 
@@ -83,6 +99,22 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_icedem_read_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
         "tdem_icedem_write_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
         "tdem_icedem_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "tdem_hm_create": (i32, [C.POINTER(HMConfigC), C.POINTER(vp)]),
+        "tdem_hm_destroy": (None, [vp]),
+        "tdem_hm_set_state": (i32, [vp, vp, vp, vp, vp, vp, vp, i32, vp]),
+        "tdem_hm_step": (i32, [vp, C.c_int64, vp]),
+        "tdem_hm_read_state": (i32, [vp, vp, vp, vp, vp, vp, i32, vp]),
+        "tdem_hm_read_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
+        "tdem_hm_status": (i32, [vp, vp]),
+        "tdem_hm_read_pairs": (i32, [vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
+        "tdem_hm_use_graph": (i32, [vp, i32]),
+        "tdem_hm_num_variants": (i32, []),
+        "tdem_hm_set_variant": (i32, [vp, i32]),
+        "tdem_hm_get_variant": (i32, [vp]),
+        "tdem_hm_autotune": (i32, [vp, i32, C.POINTER(C.c_float), vp]),
+        "tdem_hm_rebuild": (i32, [vp, vp]),
+        "tdem_hm_read_history": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
+        "tdem_hm_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -108,7 +140,10 @@ def lib() -> C.CDLL:
 
 def last_error(fn_name: str, handle) -> str:
     buf = C.create_string_buffer(1024)
-    lib().tdem_icedem_last_error(handle, buf, len(buf))
+    if fn_name.startswith("tdem_hm"):
+        lib().tdem_hm_last_error(handle, buf, len(buf))
+    else:
+        lib().tdem_icedem_last_error(handle, buf, len(buf))
     return buf.value.decode(errors="replace")
 
 

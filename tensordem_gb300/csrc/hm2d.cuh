@@ -1,0 +1,171 @@
+// Device-side data model of the Hertz-Mindlin 2-D disc engine.
+//
+// HBM layout (all per-particle arrays in the current sorted order; sorted by
+// a tiled Morton key of the cell so that neighbours in space are neighbours
+// in memory):
+//   pos[2][N]   V4 (x offset, y offset, radius, cell)     ping-pong per step
+//               cell = cx | cy << 16, the particle's integer cell origin,
+//               bit-cast into the last lane (exact in both precisions)
+//   vel[2][N]   V4 (vx, vy, omega, 1/m)                   ping-pong per step
+//   head[2][N]  uint4 {word, partner of slot 0, slot 1, slot 2}: one 16-byte
+//               load gives the count, the history mask and the first three
+//               partners, so all their position gathers issue together;
+//               word = candidate count (bits 0..7) | mask of slots whose
+//               stored tangential history is non-zero (bits 8..31)
+//   nbr[2][(W-3)*N] uint32 slot-major partners of slots 3 .. W-1
+//   hist[2][W*N] V2 tangential history of (particle, slot partner), one copy
+//               per side, both in the orientation of the pair's lower sorted
+//               index; both partners update their copy in place with the same
+//               arithmetic on the same operands, so the copies stay identical
+//   orig[2][N]  int original particle id
+//   whist[2][4N] V2 wall tangential history (4 walls)
+// head / nbr / hist / orig / whist swap at a rebuild. Position =
+// (cx * cell + x offset, cy * cell + y offset): FP32 offsets from an integer
+// cell origin keep contact geometry exact to ~ulp(cell) anywhere in a large
+// box. The moment of inertia is kappa m r^2 with one kappa per engine.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace tdem {
+namespace hm {
+
+constexpr int kMaxSlots = 24;
+constexpr int kThreads = 256;
+
+enum Status : int {
+  kStatusCapacity = 1,   // a particle had more candidates than slots
+  kStatusNonfinite = 2,  // non-finite position or velocity
+  kStatusEscaped = 4,    // a particle left the cell grid by more than a cell
+  kStatusInertia = 8,    // an uploaded moment of inertia was not kappa m r^2
+};
+
+template <class T>
+struct alignas(4 * sizeof(T)) V4 {
+  T x, y, z, w;
+};
+template <class T>
+struct alignas(2 * sizeof(T)) V2 {
+  T x, y;
+};
+
+template <class T>
+struct Params {
+  int n;          // particles
+  int W;          // slots per particle (ELL width)
+  int ncx, ncy;   // cell grid; walls sit at 0, ncx*cell and 0, ncy*cell
+  int tiles_x;    // 32x32-cell tiles along x (key = tile-major, Morton inside a tile)
+  int nkeys;      // size of the key space
+  int walls;      // bit 0 left, 1 right, 2 bottom, 3 top
+  T cell, inv_cell, skin, dt, half_dt;
+  T estar2;       // 2 E*
+  T gstar8;       // 8 G*
+  T damp;         // 2 sqrt(5/6) beta (Tsuji)
+  T mu, mu_wall;
+  T gx, gy;       // gravity (acceleration)
+  T kinv;         // 1 / kappa, with I = kappa m r^2
+  float rebuild_disp;  // rebuild once the displacement bound exceeds this
+};
+
+// Device control block: buffer parities, the rebuild trigger and status.
+struct Ctl {
+  int sp;                  // current pos/vel/hist buffer
+  int lp;                  // current list / cell / orig / wall-history buffer
+  unsigned ticket;         // completed blocks of the running step kernel
+  unsigned vmax2_bits;     // max |v|^2 of the running step (float bits)
+  float disp;              // displacement bound since the last rebuild
+  int rebuild_pending;     // a rebuild must run before the next evaluation
+  int status;              // Status bits
+  int rebuilds;
+  int max_cnt;             // largest candidate count of the last rebuild
+  int pad;
+  long long evals;         // force evaluations committed (prime + steps)
+  long long target;        // stop the step loop at this many evaluations
+};
+
+template <class T>
+struct Bufs {
+  V4<T>* pos[2];
+  V4<T>* vel[2];
+  uint4* head[2];
+  unsigned* nbr[2];
+  V2<T>* hist[2];
+  int* orig[2];
+  V2<T>* whist[2];
+  // rebuild scratch
+  int* cell_count;
+  int* cell_start;
+  int* cell_fill;
+  int* perm;
+  int* block_sums;
+  int* tmp_cell;
+  V2<T>* tmp_off;
+  // ledger and read-back
+  double* diss_part;   // per step-kernel warp: committed dissipation (J)
+  double* peek_part;   // per block x 8: kinetic, potential, Hertz, tangential, dissipation
+  V4<T>* peek_vel;     // integer-time velocity (vx, vy, omega, -)
+  V4<T>* peek_force;   // integer-time force (fx, fy, torque, -)
+  Ctl* ctl;
+};
+
+// The cell id rides in the last lane of the position vector: bit-cast for
+// FP32, an exactly representable integer for FP64.
+__device__ __forceinline__ float cell_to_lane(int c, float) { return __int_as_float(c); }
+__device__ __forceinline__ double cell_to_lane(int c, double) { return (double)c; }
+__device__ __forceinline__ int lane_to_cell(float x) { return __float_as_int(x); }
+__device__ __forceinline__ int lane_to_cell(double x) { return (int)x; }
+
+constexpr int kHeadSlots = 3;
+
+// Partner of slot s of particle i.
+__device__ __forceinline__ int slot_partner(const uint4& h, const unsigned* tail, size_t n, int i, int s) {
+  return s == 0 ? (int)h.y : s == 1 ? (int)h.z : s == 2 ? (int)h.w : (int)tail[(size_t)(s - kHeadSlots) * n + i];
+}
+
+// Compensated (float-float) accumulator: the sum of FP32 terms kept to about
+// 48 bits, in a fixed order. Plain double for the FP64 engine.
+template <class T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double get() const { return s; }
+};
+template <>
+struct Acc<float> {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += err;
+  }
+  __device__ __forceinline__ float get() const { return hi + lo; }
+};
+
+__device__ __forceinline__ unsigned spread5(unsigned v) {
+  v &= 31u;
+  v = (v | (v << 8)) & 0x00FF00FFu;
+  v = (v | (v << 4)) & 0x0F0F0F0Fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+
+// Tile-major key, Morton order inside each 32x32-cell tile.
+__host__ __device__ __forceinline__ int tile_key(int cx, int cy, int tiles_x) {
+#ifdef __CUDA_ARCH__
+  const unsigned m = spread5((unsigned)cx) | (spread5((unsigned)cy) << 1);
+#else
+  unsigned m = 0;
+  for (int b = 0; b < 5; ++b) m |= (((unsigned)cx >> b) & 1u) << (2 * b) | (((unsigned)cy >> b) & 1u) << (2 * b + 1);
+#endif
+  return (((cy >> 5) * tiles_x + (cx >> 5)) << 10) | (int)m;
+}
+
+}  // namespace hm
+}  // namespace tdem

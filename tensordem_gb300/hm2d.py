@@ -1,0 +1,289 @@
+"""Hertz-Mindlin 2-D disc engine (spec mode) on the GB300 CUDA path.
+
+:class:`HM2D` owns one engine of ``libtdem_sm103.so`` (include/tdem.h,
+``tdem_hm_*``): device-resident particle state sorted by cell, a Verlet
+neighbour list rebuilt on the device when the accumulated displacement bound
+reaches half the skin, and one fused force + velocity-Verlet kernel per step,
+all driven by a conditional CUDA graph. ``precision=32`` is the production
+form (FP32 contacts on FP32 offsets from an integer cell origin, compensated
+per-particle sums, FP64 ledger); ``precision=64`` is the plain FP64 kernel.
+
+:func:`granular_gas_case` builds the seeded 1,048,576-disc settling case:
+radii U[0.8, 1.2] mm, density 2500 kg/m^3, E = 70 GPa, nu = 0.25, mu = 0.5,
+restitution 0.8, a jittered square grid at area fraction 0.55 in a box with
+four rigid walls, Gaussian velocities (sigma 0.1 m/s), gravity -9.81 m/s^2,
+dt = 0.2 Rayleigh time of the smallest disc.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+
+WALL_LEFT, WALL_RIGHT, WALL_BOTTOM, WALL_TOP = 1, 2, 4, 8
+ALL_WALLS = 15
+
+
+@dataclass(frozen=True)
+class HM2DConfig:
+    """Engine configuration. The box is [0, ncx*cell] x [0, ncy*cell]."""
+
+    n: int
+    ncx: int
+    ncy: int
+    cell: float
+    skin: float
+    dt: float
+    young: float
+    poisson: float
+    restitution: float
+    mu: float
+    mu_wall: float
+    gravity: tuple[float, float] = (0.0, -9.81)
+    walls: int = ALL_WALLS
+    precision: int = 32
+    max_neighbors: int = 16
+    inertia_factor: float = 0.5
+
+    @property
+    def box(self) -> tuple[float, float]:
+        c = float(np.float32(self.cell)) if self.precision == 32 else float(self.cell)
+        return (self.ncx * c, self.ncy * c)
+
+    def to_c(self) -> _lib.HMConfigC:
+        c = _lib.HMConfigC()
+        c.n, c.precision, c.max_neighbors, c.walls = self.n, self.precision, self.max_neighbors, self.walls
+        c.ncx, c.ncy = self.ncx, self.ncy
+        c.cell, c.skin, c.dt = self.cell, self.skin, self.dt
+        c.young, c.poisson, c.restitution = self.young, self.poisson, self.restitution
+        c.mu, c.mu_wall = self.mu, self.mu_wall
+        c.gravity[0], c.gravity[1] = self.gravity
+        c.inertia_factor = self.inertia_factor
+        return c
+
+
+def grid_for_box(box: float, r_max: float, skin: float) -> tuple[int, float]:
+    """Largest cell count whose cells still hold the reach 2 r_max + skin."""
+    ncell = max(1, int(math.floor(box / (2.0 * r_max + skin))))
+    return ncell, box / ncell
+
+
+def rayleigh_dt(radius: float, density: float, young: float, poisson: float) -> float:
+    """pi r sqrt(rho/G) / (0.1631 nu + 0.8766) (xval/oss_rolling.py:183-200 of the reference)."""
+    g = young / (2.0 * (1.0 + poisson))
+    return math.pi * radius * math.sqrt(density / g) / (0.1631 * poisson + 0.8766)
+
+
+def granular_gas_case(n_side: int = 1024, *, seed: int = 0, r_min: float = 0.8e-3,
+                      r_max: float = 1.2e-3, density: float = 2500.0, young: float = 70e9,
+                      poisson: float = 0.25, mu: float = 0.5, restitution: float = 0.8,
+                      area_fraction: float = 0.55, sigma_v: float = 0.1, skin: float = 0.1e-3,
+                      precision: int = 32, max_neighbors: int = 16) -> tuple[HM2DConfig, dict]:
+    """Seeded polydisperse disc gas in a walled square box (numpy PCG64 ``seed``).
+
+    Discs sit on an n_side x n_side grid of spacing ``a`` chosen so that the
+    expected disc area fills ``area_fraction`` of the box; each centre is
+    jittered inside its grid square without touching its borders, so no two
+    discs overlap at t = 0. Disc thickness is 2 r (mass 2 pi rho r^3,
+    I = m r^2 / 2).
+    """
+    rng = np.random.default_rng(seed)
+    n = n_side * n_side
+    radius = rng.uniform(r_min, r_max, n)
+    mean_r2 = (r_max**3 - r_min**3) / (3.0 * (r_max - r_min))
+    a = math.sqrt(math.pi * mean_r2 / area_fraction)
+    if a < 2.0 * r_max:
+        raise ValueError("area fraction too high for a non-overlapping jittered grid")
+    box_req = n_side * a
+    ncell, cell = grid_for_box(box_req, r_max, skin)
+    c32 = float(np.float32(cell)) if precision == 32 else cell
+    box = ncell * c32
+    a = box / n_side  # spread the grid over the exact wall-to-wall box
+    jj, ii = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij")
+    centre = np.stack(((ii.ravel() + 0.5) * a, (jj.ravel() + 0.5) * a), axis=1)
+    room = np.maximum(0.5 * a - radius, 0.0)[:, None]
+    pos = centre + rng.uniform(-1.0, 1.0, (n, 2)) * room * 0.999
+    vel = rng.normal(0.0, sigma_v, (n, 2))
+    omega = np.zeros(n)
+    thickness = 2.0 * radius
+    mass = density * math.pi * radius**2 * thickness
+    inertia = 0.5 * mass * radius**2
+    dt = 0.2 * rayleigh_dt(float(radius.min()), density, young, poisson)
+    cfg = HM2DConfig(n=n, ncx=ncell, ncy=ncell, cell=cell, skin=skin, dt=dt, young=young,
+                     poisson=poisson, restitution=restitution, mu=mu, mu_wall=mu,
+                     gravity=(0.0, -9.81), walls=ALL_WALLS, precision=precision,
+                     max_neighbors=max_neighbors)
+    state = dict(pos=pos, vel=vel, omega=omega, radius=radius, mass=mass, inertia=inertia)
+    return cfg, state
+
+
+def _as_f64(x, device) -> tuple[object, int, object]:
+    """(pointer, host flag, keep-alive) for an FP64 array on the host or the GPU."""
+    if isinstance(x, torch.Tensor):
+        t = x.detach().to(dtype=torch.float64).contiguous()
+        if t.is_cuda:
+            return t.data_ptr(), 0, t
+        return t.data_ptr(), 1, t
+    a = np.ascontiguousarray(x, dtype=np.float64)
+    return a.ctypes.data, 1, a
+
+
+class HM2D:
+    """One Hertz-Mindlin engine instance on the current CUDA device."""
+
+    def __init__(self, config: HM2DConfig, device: str | torch.device = "cuda"):
+        self.config = config
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("HM2D runs on CUDA devices only")
+        if not torch.cuda.is_available():
+            raise ValueError("CUDA requested but unavailable")
+        self._lib = _lib.lib()
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_create(C.byref(config.to_c()), C.byref(h))
+        _lib.check(rc, None, "tdem_hm_create")
+        self._h = h
+        self.steps = 0
+        # TDEM_GRAPH=0 runs steps as plain launches (profilers cannot see
+        # kernels inside conditional CUDA graphs); results are identical.
+        if os.environ.get("TDEM_GRAPH", "1") == "0":
+            self.use_graph(False)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.tdem_hm_destroy(h)
+            self._h = None
+
+    def _stream(self) -> int:
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def use_graph(self, on: bool) -> None:
+        self._lib.tdem_hm_use_graph(self._h, 1 if on else 0)
+
+    def set_state(self, pos, vel, omega, radius, mass, inertia) -> None:
+        """Upload a state given in original particle order (host or device arrays)."""
+        n = self.config.n
+        args = [_as_f64(x, self.device) for x in (pos, vel, omega, radius, mass, inertia)]
+        for (_, _, a), shape in zip(args, [(n, 2), (n, 2), (n,), (n,), (n,), (n,)]):
+            if tuple(a.shape) != shape:
+                raise ValueError(f"state array of shape {tuple(a.shape)}, expected {shape}")
+        hosts = {h for _, h, _ in args}
+        if len(hosts) != 1:
+            raise ValueError("state arrays must all be on the host or all on the GPU")
+        self._keep = args
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_set_state(self._h, *[p for p, _, _ in args], hosts.pop(), self._stream())
+        _lib.check(rc, self._h, "tdem_hm_set_state")
+        self.check()
+        self.steps = 0
+
+    def step(self, n_steps: int = 1, *, check: bool = True) -> None:
+        """Advance n velocity-Verlet steps (one graph launch)."""
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_step(self._h, int(n_steps), self._stream())
+            _lib.check(rc, self._h, "tdem_hm_step")
+            self.steps += int(n_steps)
+            if check:
+                self.check()
+
+    def check(self) -> None:
+        rc = self._lib.tdem_hm_status(self._h, self._stream())
+        _lib.check(rc, self._h, "tdem_hm_status")
+
+    def state(self) -> dict[str, torch.Tensor]:
+        """Integer-time state in original order as FP64 CUDA tensors."""
+        n = self.config.n
+        out = dict(pos=torch.empty((n, 2), dtype=torch.float64, device=self.device),
+                   vel=torch.empty((n, 2), dtype=torch.float64, device=self.device),
+                   omega=torch.empty(n, dtype=torch.float64, device=self.device),
+                   force=torch.empty((n, 2), dtype=torch.float64, device=self.device),
+                   torque=torch.empty(n, dtype=torch.float64, device=self.device))
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_read_state(self._h, out["pos"].data_ptr(), out["vel"].data_ptr(),
+                                              out["omega"].data_ptr(), out["force"].data_ptr(),
+                                              out["torque"].data_ptr(), 0, self._stream())
+        _lib.check(rc, self._h, "tdem_hm_read_state")
+        return out
+
+    def read_state_host(self, pos: np.ndarray, vel: np.ndarray, omega: np.ndarray) -> None:
+        """Copy positions, velocities and omega into host arrays (synchronizes)."""
+        for a in (pos, vel, omega):
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("host outputs must be C-contiguous float64")
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_read_state(self._h, pos.ctypes.data, vel.ctypes.data,
+                                              omega.ctypes.data, None, None, 1, self._stream())
+        _lib.check(rc, self._h, "tdem_hm_read_state")
+
+    def ledger(self) -> dict[str, float]:
+        buf = (C.c_double * _lib.HM_COUNT)()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_read_ledger(self._h, buf, _lib.HM_COUNT, self._stream())
+        _lib.check(rc, self._h, "tdem_hm_read_ledger")
+        v = list(buf)
+        return dict(kinetic=v[0], potential=v[1], elastic_normal=v[2], elastic_tangential=v[3],
+                    total=v[4], dissipated=v[5], evals=int(v[6]), rebuilds=int(v[7]),
+                    max_neighbors=int(v[8]), status=int(v[9]))
+
+    def pairs(self) -> np.ndarray:
+        """Current candidate pairs (original ids, i < j), sorted, as an (M, 2) array."""
+        cap = self.config.n * self.config.max_neighbors
+        out = np.empty((cap, 2), dtype=np.int32)
+        count = C.c_int64()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_read_pairs(self._h, out.ctypes.data, cap, C.byref(count), self._stream())
+        _lib.check(rc, self._h, "tdem_hm_read_pairs")
+        m = min(int(count.value), cap)
+        pairs = out[:m].astype(np.int64)
+        order = np.lexsort((pairs[:, 1], pairs[:, 0]))
+        return pairs[order]
+
+    def rebuild(self) -> None:
+        """Rebuild the neighbour list now (history carried over by pair key)."""
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_rebuild(self._h, self._stream())
+        _lib.check(rc, self._h, "tdem_hm_rebuild")
+
+    def history(self) -> dict[tuple[int, int], tuple[float, float]]:
+        """Non-zero tangential history per original-id pair (lo, hi): xi of lo relative to hi."""
+        cap = self.config.n * self.config.max_neighbors
+        pairs = np.empty((cap, 2), dtype=np.int32)
+        xi = np.empty((cap, 2), dtype=np.float64)
+        count = C.c_int64()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_read_history(self._h, pairs.ctypes.data, xi.ctypes.data, cap,
+                                                C.byref(count), self._stream())
+        _lib.check(rc, self._h, "tdem_hm_read_history")
+        m = min(int(count.value), cap)
+        return {(int(a), int(b)): (float(x), float(y)) for (a, b), (x, y) in zip(pairs[:m], xi[:m])}
+
+    @property
+    def variant(self) -> int:
+        return int(self._lib.tdem_hm_get_variant(self._h))
+
+    @variant.setter
+    def variant(self, v: int) -> None:
+        _lib.check(self._lib.tdem_hm_set_variant(self._h, int(v)), self._h, "tdem_hm_set_variant")
+
+    def autotune(self, steps: int = 20) -> dict[int, float]:
+        """Time every step-kernel variant on the live state and keep the fastest.
+
+        The simulation advances while tuning (variants compute bit-identical
+        states). Returns milliseconds per variant for ``steps`` steps.
+        """
+        nv = int(self._lib.tdem_hm_num_variants())
+        ms = (C.c_float * nv)()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_autotune(self._h, int(steps), ms, self._stream())
+        _lib.check(rc, self._h, "tdem_hm_autotune")
+        self.steps += nv * (int(steps) + 2)
+        return {v: float(ms[v]) for v in range(nv)}
