@@ -195,6 +195,8 @@ enum {
   TDEM_HM_L_REBUILDS = 7,    /* neighbour-list rebuilds */
   TDEM_HM_L_MAX_NEIGHBORS = 8, /* largest candidate count at the last rebuild */
   TDEM_HM_L_STATUS = 9,      /* device status bits */
+  TDEM_HM_L_GRAPH = 10,      /* 1 when steps run as conditional CUDA graphs */
+  TDEM_HM_L_VARIANT = 11,    /* step-kernel variant in use */
   TDEM_HM_L_COUNT = 16
 };
 
@@ -249,6 +251,15 @@ int tdem_hm_rebuild(tdem_hm* h, void* stream);
  * same state keyed by i*N+j (src/tensordem/granular2d/engine.py:388-396). */
 int tdem_hm_read_history(tdem_hm* h, int32_t* pairs, double* xi, int64_t capacity, int64_t* count,
                          void* stream);
+
+/* One step as a single plain launch of the step kernel, with no rebuild:
+ * for callers that time the kernel alone (a list rebuild must follow when
+ * tdem_hm_rebuild_pending says so, before the next step). */
+int tdem_hm_step_kernel(tdem_hm* h, void* stream);
+
+/* Synchronize `stream`; 1 if the neighbour list must be rebuilt before the
+ * next step (then call tdem_hm_rebuild), 0 if not, negative on error. */
+int tdem_hm_rebuild_pending(tdem_hm* h, void* stream);
 
 /* Step-kernel variants (launch shapes) and the autotuner that picks one by
  * timing `steps` steps of each on the live state (the simulation advances by

@@ -109,6 +109,8 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_hm_read_pairs": (i32, [vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_hm_use_graph": (i32, [vp, i32]),
         "tdem_hm_num_variants": (i32, []),
+        "tdem_hm_step_kernel": (i32, [vp, vp]),
+        "tdem_hm_rebuild_pending": (i32, [vp, vp]),
         "tdem_hm_set_variant": (i32, [vp, i32]),
         "tdem_hm_get_variant": (i32, [vp]),
         "tdem_hm_autotune": (i32, [vp, i32, C.POINTER(C.c_float), vp]),

@@ -26,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "bulk.cuh"
 #include "common.h"
 #include "hm2d.cuh"
 
@@ -393,10 +394,10 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
   const int rebuild = (disp > P.rebuild_disp) ? 1 : 0;
   ctl->rebuild_pending = rebuild;
   const int keep_going = (ctl->evals < ctl->target) && !(ctl->status & kStatusNonfinite);
-  if (use_cond) {
-    cudaGraphSetConditional(h_rebuild, (unsigned)rebuild);
-    cudaGraphSetConditional(h_loop, (unsigned)keep_going);
-  }
+  // use_cond bit 0: this launch sits in a graph with a rebuild IF node;
+  // bit 1: it also sits in the step loop's WHILE body
+  if (use_cond & 1) cudaGraphSetConditional(h_rebuild, (unsigned)rebuild);
+  if (use_cond & 2) cudaGraphSetConditional(h_loop, (unsigned)keep_going);
 }
 
 // One thread per particle (variant 0) and the read-back kernel.
@@ -467,6 +468,67 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
     p = pn;
     v = vn;
     hd = hn;
+  }
+  commit_epilogue<T>(P, B, sp, L, h_rebuild, h_loop, use_cond);
+}
+
+// Bulk-copy variant: each block streams its tiles of own-particle state
+// (position, velocity, list head: 48 B per particle in FP32) from HBM into
+// shared memory with cp.async.bulk, double-buffered on two mbarriers, so the
+// next tile is in flight while the current one is computed. Partner state is
+// gathered from global memory (mostly L2 hits thanks to the cell sort).
+constexpr long long kWaitBudget = 2000000000LL;  // ~1 s of SM clock per wait
+
+template <class T, int MODE, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bufs<T> B,
+                                                                 cudaGraphConditionalHandle h_rebuild,
+                                                                 cudaGraphConditionalHandle h_loop, int use_cond,
+                                                                 int primed) {
+  static_assert(MODE != kPeek, "read-back uses force_kernel");
+  __shared__ alignas(128) V4<T> s_pos[2][BLOCK];
+  __shared__ alignas(128) V4<T> s_vel[2][BLOCK];
+  __shared__ alignas(128) uint4 s_head[2][BLOCK];
+  __shared__ alignas(8) uint64_t s_bar[2];
+  const int sp = B.ctl->sp, lp = B.ctl->lp;
+  const int n = P.n;
+  const int ntiles = (n + BLOCK - 1) / BLOCK;
+  ThreadLedger<T> L;
+  if (threadIdx.x == 0) {
+    bulk::mbar_init(&s_bar[0], 1);
+    bulk::mbar_init(&s_bar[1], 1);
+    bulk::fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int tile, int buf) {
+    const int start = tile * BLOCK;
+    const int cnt = min(BLOCK, n - start);
+    const uint32_t vb = (uint32_t)(cnt * sizeof(V4<T>));
+    const uint32_t hb = (uint32_t)(cnt * sizeof(uint4));
+    bulk::mbar_arrive_expect_tx(&s_bar[buf], 2 * vb + hb);
+    bulk::copy_g2s(&s_pos[buf][0], B.pos[sp] + start, vb, &s_bar[buf]);
+    bulk::copy_g2s(&s_vel[buf][0], B.vel[sp] + start, vb, &s_bar[buf]);
+    bulk::copy_g2s(&s_head[buf][0], B.head[lp] + start, hb, &s_bar[buf]);
+  };
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < ntiles) issue(tile, 0);
+  for (int k = 0; tile < ntiles; tile += gridDim.x, ++k) {
+    const int buf = k & 1;
+    const int next = tile + gridDim.x;
+    // buf ^ 1 was released by the barrier that ended the previous iteration
+    if (threadIdx.x == 0 && next < ntiles) issue(next, buf ^ 1);
+    const bool ok = bulk::mbar_wait_bounded(&s_bar[buf], (uint32_t)((k >> 1) & 1), kWaitBudget);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(&B.ctl->status, (int)kStatusTimeout);
+      break;
+    }
+    const int i = tile * BLOCK + threadIdx.x;
+    if (i < n) {
+      const V4<T> p = s_pos[buf][threadIdx.x];
+      const V4<T> v = s_vel[buf][threadIdx.x];
+      const uint4 hd = s_head[buf][threadIdx.x];
+      process_particle<T, MODE>(P, B, sp, lp, i, p, v, hd, primed, L);
+    }
+    __syncthreads();
   }
   commit_epilogue<T>(P, B, sp, L, h_rebuild, h_loop, use_cond);
 }
@@ -879,6 +941,8 @@ struct EngineBase {
   virtual int read_pairs(int* out, long long capacity, long long* count, cudaStream_t s) = 0;
   virtual int use_graph(int on) = 0;
   virtual int set_variant(int v) = 0;
+  virtual int step_kernel(cudaStream_t s) = 0;
+  virtual int rebuild_pending(cudaStream_t s) = 0;
   virtual int get_variant() const = 0;
   virtual int autotune(int steps, cudaStream_t s, float* ms_out) = 0;
   virtual int rebuild(cudaStream_t s) = 0;
@@ -889,7 +953,7 @@ struct EngineBase {
 // Step-kernel variants the autotuner chooses from: 0 = one thread per
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
 // block shapes.
-constexpr int kVariants = 4;
+constexpr int kVariants = 6;
 
 template <class T>
 struct StepKernel {
@@ -908,6 +972,8 @@ StepFn<T> step_fn(int variant, int mode) {
       case 1: return &force_kernel_pf<T, kPrime, 256, 3>;
       case 2: return &force_kernel_pf<T, kPrime, 128, 6>;
       case 3: return &force_kernel_pf<T, kPrime, 256, 2>;
+      case 4: return &force_kernel_bulk<T, kPrime, 256, 3>;
+      case 5: return &force_kernel_bulk<T, kPrime, 128, 6>;
       default: return &force_kernel<T, kPrime>;
     }
   }
@@ -915,11 +981,13 @@ StepFn<T> step_fn(int variant, int mode) {
     case 1: return &force_kernel_pf<T, kStep, 256, 3>;
     case 2: return &force_kernel_pf<T, kStep, 128, 6>;
     case 3: return &force_kernel_pf<T, kStep, 256, 2>;
+    case 4: return &force_kernel_bulk<T, kStep, 256, 3>;
+    case 5: return &force_kernel_bulk<T, kStep, 128, 6>;
     default: return &force_kernel<T, kStep>;
   }
 }
 
-inline int variant_block(int variant) { return variant == 2 ? 128 : 256; }
+inline int variant_block(int variant) { return (variant == 2 || variant == 5) ? 128 : 256; }
 
 template <class T>
 struct Engine final : EngineBase {
@@ -929,14 +997,20 @@ struct Engine final : EngineBase {
   int nblocks = 0;
   int scan_blocks = 0;
   int variant = 0;
-  int vgrid[kVariants] = {0, 0, 0, 0};
+  int vgrid[kVariants] = {};
   int nwarp_slots = 0;
   bool primed = false;
   bool has_state = false;
   bool graph_on = true;
   bool graph_failed = false;
-  cudaGraph_t graph = nullptr;
+  std::string graph_error;
+  cudaGraph_t graph = nullptr;       // n steps: WHILE loop
   cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph1 = nullptr;      // one step
+  cudaGraphExec_t exec1 = nullptr;
+  cudaGraphNode_t target_node = nullptr;
+  long long exec_target = 0;
+  cudaGraphConditionalHandle h_reb1 = 0;
   cudaStream_t cap_stream = nullptr;
   cudaGraphConditionalHandle h_loop = 0, h_reb = 0;
   double* stage = nullptr;        // device staging for host FP64 arrays
@@ -947,14 +1021,22 @@ struct Engine final : EngineBase {
   double* host_diss = nullptr;    // pinned committed partials
 
   ~Engine() override {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
+    destroy_graphs();
     if (cap_stream) cudaStreamDestroy(cap_stream);
     for (void* p : allocs) cudaFree(p);
     cudaFreeHost(host_stage);
     cudaFreeHost(host_ctl);
     cudaFreeHost(host_part);
     cudaFreeHost(host_diss);
+  }
+
+  void destroy_graphs() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (exec1) cudaGraphExecDestroy(exec1);
+    if (graph1) cudaGraphDestroy(graph1);
+    exec = exec1 = nullptr;
+    graph = graph1 = nullptr;
   }
 
   template <class U>
@@ -1095,21 +1177,11 @@ struct Engine final : EngineBase {
     return TDEM_OK;
   }
 
-  int build_graph() {
-    TDEM_CUDA_TRY(&err, cudaGraphCreate(&graph, 0));
-    TDEM_CUDA_TRY(&err, cudaGraphConditionalHandleCreate(&h_loop, graph, 1, cudaGraphCondAssignDefault));
-    cudaGraphNodeParams wp = {};
-    wp.type = cudaGraphNodeTypeConditional;
-    wp.conditional.handle = h_loop;
-    wp.conditional.type = cudaGraphCondTypeWhile;
-    wp.conditional.size = 1;
-    cudaGraphNode_t wnode;
-    TDEM_CUDA_TRY(&err, cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &wp));
-    cudaGraph_t body = wp.conditional.phGraph_out[0];
-    TDEM_CUDA_TRY(&err, cudaGraphConditionalHandleCreate(&h_reb, body, 0, cudaGraphCondAssignDefault));
-    // step kernel node
-    int use_cond = 1, prim = 1;
-    void* args[] = {&P, &B, &h_reb, &h_loop, &use_cond, &prim};
+  // Adds `kernel -> IF(h) { rebuild pipeline }` to graph g.
+  int add_step_and_rebuild(cudaGraph_t g, const cudaGraphNode_t* dep, size_t ndep,
+                           cudaGraphConditionalHandle h, cudaGraphConditionalHandle hl, int cond_bits) {
+    int prim = 1;
+    void* args[] = {&P, &B, &h, &hl, &cond_bits, &prim};
     cudaKernelNodeParams kp = {};
     kp.func = reinterpret_cast<void*>(step_fn<T>(variant, kStep));
     kp.gridDim = dim3((unsigned)vgrid[variant]);
@@ -1117,21 +1189,69 @@ struct Engine final : EngineBase {
     kp.sharedMemBytes = 0;
     kp.kernelParams = args;
     cudaGraphNode_t knode;
-    TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&knode, body, nullptr, 0, &kp));
+    TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&knode, g, dep, ndep, &kp));
     cudaGraphNodeParams ip = {};
     ip.type = cudaGraphNodeTypeConditional;
-    ip.conditional.handle = h_reb;
+    ip.conditional.handle = h;
     ip.conditional.type = cudaGraphCondTypeIf;
     ip.conditional.size = 1;
     cudaGraphNode_t inode;
-    TDEM_CUDA_TRY(&err, cudaGraphAddNode(&inode, body, &knode, nullptr, 1, &ip));
+    TDEM_CUDA_TRY(&err, cudaGraphAddNode(&inode, g, &knode, nullptr, 1, &ip));
     cudaGraph_t rb = ip.conditional.phGraph_out[0];
     TDEM_CUDA_TRY(&err, cudaStreamBeginCaptureToGraph(cap_stream, rb, nullptr, nullptr, 0,
                                                       cudaStreamCaptureModeThreadLocal));
     launch_rebuild(cap_stream);
     cudaGraph_t got = nullptr;
     TDEM_CUDA_TRY(&err, cudaStreamEndCapture(cap_stream, &got));
+    return TDEM_OK;
+  }
+
+  // Two graphs: one step (kernel -> IF rebuild), and n steps
+  // (set target -> WHILE { kernel -> IF rebuild }).
+  int build_graph() {
+    int rc;
+    TDEM_CUDA_TRY(&err, cudaGraphCreate(&graph1, 0));
+    TDEM_CUDA_TRY(&err, cudaGraphConditionalHandleCreate(&h_reb1, graph1, 0, cudaGraphCondAssignDefault));
+    if ((rc = add_step_and_rebuild(graph1, nullptr, 0, h_reb1, 0, 1))) return rc;
+    TDEM_CUDA_TRY(&err, cudaGraphInstantiate(&exec1, graph1, 0));
+
+    TDEM_CUDA_TRY(&err, cudaGraphCreate(&graph, 0));
+    TDEM_CUDA_TRY(&err, cudaGraphConditionalHandleCreate(&h_loop, graph, 1, cudaGraphCondAssignDefault));
+    long long n0 = 1;
+    void* targs[] = {&B.ctl, &n0};
+    cudaKernelNodeParams tp = {};
+    tp.func = reinterpret_cast<void*>(&set_target_kernel);
+    tp.gridDim = dim3(1);
+    tp.blockDim = dim3(1);
+    tp.kernelParams = targs;
+    TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&target_node, graph, nullptr, 0, &tp));
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    TDEM_CUDA_TRY(&err, cudaGraphAddNode(&wnode, graph, &target_node, nullptr, 1, &wp));
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    TDEM_CUDA_TRY(&err, cudaGraphConditionalHandleCreate(&h_reb, body, 0, cudaGraphCondAssignDefault));
+    if ((rc = add_step_and_rebuild(body, nullptr, 0, h_reb, h_loop, 3))) return rc;
     TDEM_CUDA_TRY(&err, cudaGraphInstantiate(&exec, graph, 0));
+    exec_target = 1;
+    return TDEM_OK;
+  }
+
+  // Point the n-step graph's target node at n (only when n changes).
+  int set_graph_target(long long n) {
+    if (n == exec_target) return TDEM_OK;
+    long long nn = n;
+    void* targs[] = {&B.ctl, &nn};
+    cudaKernelNodeParams tp = {};
+    tp.func = reinterpret_cast<void*>(&set_target_kernel);
+    tp.gridDim = dim3(1);
+    tp.blockDim = dim3(1);
+    tp.kernelParams = targs;
+    TDEM_CUDA_TRY(&err, cudaGraphExecKernelNodeSetParams(exec, target_node, &tp));
+    exec_target = n;
     return TDEM_OK;
   }
 
@@ -1154,14 +1274,20 @@ struct Engine final : EngineBase {
     }
     if (graph_on && !graph_failed && !exec) {
       if (build_graph() != TDEM_OK) {
+        // fall back to plain launches (same kernels, same results)
+        graph_error = err;
         graph_failed = true;
+        destroy_graphs();
         cudaGetLastError();
       }
     }
     if (graph_on && exec) {
-      // target = evals + n, set on the stream so that it orders with the graph
-      set_target_kernel<<<1, 1, 0, s>>>(B.ctl, n);
-      TDEM_CUDA_TRY(&err, cudaGetLastError());
+      if (n == 1) {
+        TDEM_CUDA_TRY(&err, cudaGraphLaunch(exec1, s));
+        return TDEM_OK;
+      }
+      int rc = set_graph_target(n);
+      if (rc) return rc;
       TDEM_CUDA_TRY(&err, cudaGraphLaunch(exec, s));
       return TDEM_OK;
     }
@@ -1234,6 +1360,8 @@ struct Engine final : EngineBase {
     v[TDEM_HM_L_REBUILDS] = (double)host_ctl->rebuilds;
     v[TDEM_HM_L_MAX_NEIGHBORS] = (double)host_ctl->max_cnt;
     v[TDEM_HM_L_STATUS] = (double)host_ctl->status;
+    v[TDEM_HM_L_GRAPH] = (exec != nullptr) ? 1.0 : 0.0;
+    v[TDEM_HM_L_VARIANT] = (double)variant;
     std::memcpy(out, v, std::min(count, (int)TDEM_HM_L_COUNT) * sizeof(double));
     return TDEM_OK;
   }
@@ -1247,6 +1375,7 @@ struct Engine final : EngineBase {
       return tdem::fail(&err, TDEM_ERR_CAPACITY,
                         "neighbour capacity exceeded (max_neighbors=" + std::to_string(P.W) + ")");
     if (st & kStatusEscaped) return tdem::fail(&err, TDEM_ERR_CAPACITY, "a particle left the cell grid");
+    if (st & kStatusTimeout) return tdem::fail(&err, TDEM_ERR_CUDA, "a bounded wait on a bulk copy timed out");
     if (st & kStatusInertia)
       return tdem::fail(&err, TDEM_ERR_BADARG, "moment of inertia must be inertia_factor * m * r^2");
     return TDEM_OK;
@@ -1276,14 +1405,25 @@ struct Engine final : EngineBase {
     return TDEM_OK;
   }
 
+  int step_kernel(cudaStream_t s) override {
+    if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "step before set_state");
+    if (!primed) return prime(s);
+    step_fn<T>(variant, kStep)<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
+    TDEM_CUDA_TRY(&err, cudaGetLastError());
+    return TDEM_OK;
+  }
+
+  int rebuild_pending(cudaStream_t s) override {
+    TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_ctl, B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
+    return host_ctl->rebuild_pending ? 1 : 0;
+  }
+
   int set_variant(int v) override {
     if (v < 0 || v >= kVariants) return tdem::fail(&err, TDEM_ERR_BADARG, "unknown step-kernel variant");
     if (v != variant) {
       variant = v;
-      if (exec) cudaGraphExecDestroy(exec);
-      if (graph) cudaGraphDestroy(graph);
-      exec = nullptr;
-      graph = nullptr;
+      destroy_graphs();
     }
     return TDEM_OK;
   }
@@ -1451,6 +1591,17 @@ int tdem_hm_read_history(tdem_hm* h, int32_t* pairs, double* xi, int64_t capacit
   const int rc = h->e->read_history(pairs, xi, (long long)capacity, &c, reinterpret_cast<cudaStream_t>(stream));
   *count = (int64_t)c;
   return rc;
+}
+
+int tdem_hm_step_kernel(tdem_hm* h, void* stream) {
+  if (!h) return TDEM_ERR_BADARG;
+  return h->e->step_kernel(reinterpret_cast<cudaStream_t>(stream));
+}
+
+int tdem_hm_rebuild_pending(tdem_hm* h, void* stream) {
+  if (!h) return -TDEM_ERR_BADARG;
+  const int r = h->e->rebuild_pending(reinterpret_cast<cudaStream_t>(stream));
+  return r;
 }
 
 int tdem_hm_num_variants(void) { return kVariants; }

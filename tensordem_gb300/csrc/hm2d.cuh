@@ -40,6 +40,7 @@ enum Status : int {
   kStatusNonfinite = 2,  // non-finite position or velocity
   kStatusEscaped = 4,    // a particle left the cell grid by more than a cell
   kStatusInertia = 8,    // an uploaded moment of inertia was not kappa m r^2
+  kStatusTimeout = 16,   // a bounded wait on a bulk copy ran out
 };
 
 template <class T>

@@ -232,7 +232,7 @@ class HM2D:
         v = list(buf)
         return dict(kinetic=v[0], potential=v[1], elastic_normal=v[2], elastic_tangential=v[3],
                     total=v[4], dissipated=v[5], evals=int(v[6]), rebuilds=int(v[7]),
-                    max_neighbors=int(v[8]), status=int(v[9]))
+                    max_neighbors=int(v[8]), status=int(v[9]), graph=bool(v[10]), variant=int(v[11]))
 
     def pairs(self) -> np.ndarray:
         """Current candidate pairs (original ids, i < j), sorted, as an (M, 2) array."""
@@ -287,3 +287,16 @@ class HM2D:
         _lib.check(rc, self._h, "tdem_hm_autotune")
         self.steps += nv * (int(steps) + 2)
         return {v: float(ms[v]) for v in range(nv)}
+
+    def step_kernel(self) -> None:
+        """One step as a single plain launch of the step kernel (no rebuild)."""
+        rc = self._lib.tdem_hm_step_kernel(self._h, self._stream())
+        _lib.check(rc, self._h, "tdem_hm_step_kernel")
+        self.steps += 1
+
+    def rebuild_pending(self) -> bool:
+        """Synchronize and report whether the list must be rebuilt before the next step."""
+        r = int(self._lib.tdem_hm_rebuild_pending(self._h, self._stream()))
+        if r < 0:
+            _lib.check(-r, self._h, "tdem_hm_rebuild_pending")
+        return r == 1
