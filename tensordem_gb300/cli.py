@@ -1,0 +1,179 @@
+"""Command line: ``python -m tensordem_gb300 <command>``.
+
+* ``dem-2d`` - the reference's 2-D ice-breaking demo
+  (src/tensordem/cli.py:42-110, 254-285), same flags and the same outputs
+  (history.csv, trajectory.pt, accounting.json), stepped by the FP64 CUDA
+  reference-mode kernel.
+* ``hm2d`` - the Hertz-Mindlin disc settling case on the GB300 engine: run,
+  time and report (used for profiling runs as well).
+"""
+
+from __future__ import annotations
+
+import argparse
+import csv
+import json
+import sys
+import time
+from dataclasses import asdict
+from pathlib import Path
+
+import torch
+
+
+def read_hull_profile(path: Path) -> torch.Tensor:
+    """x,y CSV of local hull vertices in metres (src/tensordem/cli.py:15-39)."""
+    try:
+        with path.open(newline="", encoding="utf-8-sig") as stream:
+            reader = csv.DictReader(stream)
+            if reader.fieldnames is None or not {"x", "y"}.issubset(reader.fieldnames):
+                raise ValueError("hull profile CSV must contain x,y column headers")
+            points = []
+            for line_number, row in enumerate(reader, start=2):
+                try:
+                    points.append((float(row["x"]), float(row["y"])))
+                except (TypeError, ValueError) as exc:
+                    raise ValueError(f"invalid x,y value in hull profile CSV line {line_number}") from exc
+    except OSError as exc:
+        raise ValueError(f"cannot read hull profile CSV: {exc}") from exc
+    if len(points) < 2:
+        raise ValueError("hull profile CSV must contain at least two vertices")
+    profile = torch.tensor(points, dtype=torch.float64)
+    if not bool(torch.isfinite(profile).all()):
+        raise ValueError("hull profile coordinates must be finite")
+    if bool((torch.linalg.vector_norm(profile[1:] - profile[:-1], dim=1) <= 1e-12).any()):
+        raise ValueError("hull profile must not contain zero-length segments")
+    return profile
+
+
+def _cmd_dem_2d(args: argparse.Namespace) -> None:
+    from .dem import DEMConfig, IceDEM
+
+    if args.steps < 1 or args.save_every < 1:
+        sys.exit("--steps and --save-every must be positive")
+    try:
+        hull_profile = read_hull_profile(args.hull_profile) if args.hull_profile else None
+        hull_speed = (args.hull_velocity_x**2 + args.hull_velocity_y**2) ** 0.5
+        speed_bound = max(args.speed, hull_speed, 1e-12)
+        config = DEMConfig(nx=args.nx, ny=args.ny, dt=args.dt, tool_speed=speed_bound,
+                           breaking_strain=args.breaking_strain,
+                           shear_breaking_strain=args.shear_breaking_strain, device=args.device)
+        if hull_profile is None:
+            simulation = IceDEM(config)
+        else:
+            simulation = IceDEM(config, hull_profile=hull_profile,
+                                hull_start=(args.hull_start_x, args.hull_start_y),
+                                hull_velocity=(args.hull_velocity_x, args.hull_velocity_y))
+    except (ValueError, RuntimeError, TypeError) as exc:
+        sys.exit(str(exc))
+    args.output.mkdir(parents=True, exist_ok=True)
+    frames, velocities, bonds, tool_positions, times = [], [], [], [], []
+    with (args.output / "history.csv").open("w", newline="", encoding="utf-8") as stream:
+        row = simulation.diagnostics()
+        writer = csv.DictWriter(stream, fieldnames=list(row))
+        writer.writeheader()
+        step = 0
+        while step <= args.steps:
+            if step % args.save_every == 0 or step == args.steps:
+                row = simulation.diagnostics()
+                writer.writerow(row)
+                frames.append(simulation.positions.cpu().clone())
+                velocities.append(simulation.velocities.cpu().clone())
+                bonds.append(simulation.alive[simulation.bonded].cpu().clone())
+                tool_positions.append(simulation.tool_position.cpu().clone())
+                times.append(simulation.time)
+            if step == args.steps:
+                break
+            # advance to the next sample point in one kernel launch
+            nxt = min(args.steps, (step // args.save_every + 1) * args.save_every)
+            simulation.run(nxt - step)
+            step = nxt
+    torch.save({
+        "config": asdict(simulation.config),
+        "dt": simulation.dt,
+        "times": torch.tensor(times, dtype=torch.float64),
+        "positions": torch.stack(frames),
+        "velocities": torch.stack(velocities),
+        "bond_pairs": simulation.pairs[simulation.bonded].cpu(),
+        "bond_alive": torch.stack(bonds),
+        "fixed": simulation.fixed.cpu(),
+        "tool_positions": torch.stack(tool_positions),
+        "hull_profile": None if simulation.hull_profile is None else simulation.hull_profile.cpu(),
+        "hull_velocity": simulation.hull_velocity.cpu(),
+    }, args.output / "trajectory.pt")
+    accounting_data = dict(simulation.accounting)
+    accounting_data["total_bonds"] = int(simulation.bonded.sum().item())
+    accounting_data["broken_bonds"] = simulation.broken_bonds
+    accounting_data["failure_energy_sum_J"] = float(simulation.failure_energy_J.sum().item())
+    accounting_data["total_mass_kg"] = float(simulation.config.mass * len(simulation.positions))
+    accounting_data["dt"] = simulation.dt
+    accounting_data["steps"] = simulation.step_count
+    with (args.output / "accounting.json").open("w", encoding="utf-8") as f:
+        f.write(json.dumps(accounting_data, indent=2, sort_keys=True, allow_nan=False))
+    print(f"done: t={simulation.time:.6f} s, dt={simulation.dt:.6g} s, "
+          f"broken bonds={simulation.broken_bonds}/{int(simulation.bonded.sum().item())}; "
+          f"output: {args.output}")
+
+
+def _cmd_hm2d(args: argparse.Namespace) -> None:
+    from .hm2d import HM2D, granular_gas_case
+
+    cfg, st = granular_gas_case(args.n_side, seed=args.seed, precision=args.precision,
+                                max_neighbors=args.max_neighbors)
+    eng = HM2D(cfg)
+    if args.no_graph:
+        eng.use_graph(False)
+    eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
+    if args.variant is not None:
+        eng.variant = args.variant
+    elif args.autotune:
+        eng.autotune(steps=10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.step(args.steps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    led = eng.ledger()
+    print(json.dumps({"discs": cfg.n, "steps": args.steps, "seconds": dt,
+                      "particle_steps_per_s": cfg.n * args.steps / dt, "ledger": led}))
+
+
+def main(argv: list[str] | None = None) -> None:
+    parser = argparse.ArgumentParser(description="tensordem_gb300: GB300 2-D DEM step")
+    sub = parser.add_subparsers(dest="command")
+    d = sub.add_parser("dem-2d", help="2-D ice-breaking DEM simulation (reference mode, FP64)")
+    d.add_argument("--nx", type=int, default=21)
+    d.add_argument("--ny", type=int, default=5)
+    d.add_argument("--steps", type=int, default=2000)
+    d.add_argument("--dt", type=float, default=None)
+    d.add_argument("--speed", type=float, default=1.0)
+    d.add_argument("--hull-profile", type=Path, default=None)
+    d.add_argument("--hull-start-x", type=float, default=0.0)
+    d.add_argument("--hull-start-y", type=float, default=0.0)
+    d.add_argument("--hull-velocity-x", type=float, default=0.0)
+    d.add_argument("--hull-velocity-y", type=float, default=0.0)
+    d.add_argument("--breaking-strain", type=float, default=0.015)
+    d.add_argument("--shear-breaking-strain", type=float, default=0.03)
+    d.add_argument("--device", default="cuda")
+    d.add_argument("--output", type=Path, default=Path("results"))
+    d.add_argument("--save-every", type=int, default=20)
+    d.set_defaults(func=_cmd_dem_2d)
+    h = sub.add_parser("hm2d", help="Hertz-Mindlin disc settling case on the GPU engine")
+    h.add_argument("--n-side", type=int, default=1024)
+    h.add_argument("--steps", type=int, default=100)
+    h.add_argument("--seed", type=int, default=0)
+    h.add_argument("--precision", type=int, choices=(32, 64), default=32)
+    h.add_argument("--max-neighbors", type=int, default=16)
+    h.add_argument("--variant", type=int, default=None)
+    h.add_argument("--autotune", action="store_true")
+    h.add_argument("--no-graph", action="store_true", help="plain launches (visible to profilers)")
+    h.set_defaults(func=_cmd_hm2d)
+    args = parser.parse_args(argv)
+    if not hasattr(args, "func"):
+        parser.print_help()
+        sys.exit(1)
+    args.func(args)
+
+
+if __name__ == "__main__":
+    main()
