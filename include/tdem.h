@@ -270,6 +270,34 @@ int tdem_hm_set_variant(tdem_hm* h, int variant);
 int tdem_hm_get_variant(const tdem_hm* h);
 int tdem_hm_autotune(tdem_hm* h, int steps, float* ms_out, void* stream);
 
+/* Allocation-free contact forces. No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory, such as code running while
+ * another solver's CUDA graph is being captured, real-time coupling loops and
+ * plug-ins whose host application owns all device memory.
+ *
+ * One Hertz-Mindlin force evaluation of `cfg->n` discs given in original order
+ * as device arrays (positions (n,2), velocities (n,2), omega, radius, mass,
+ * inertia; FP64): cell list, candidate lists and the contact, wall and gravity
+ * forces with zero tangential history, as tdem_hm_set_state followed by
+ * tdem_hm_read_state would report them. Writes the total force (n,2) and
+ * torque (n) to the device arrays out_force / out_torque. FP32 only.
+ *
+ * It calls no cudaMalloc or cudaFree: its scratch is one 8 MiB device array
+ * inside this library, which every GPU that loads the library holds until the
+ * process exits. Limits: n <= 16384 discs, grids up to 256 x 256 cells, at
+ * most 8 candidate partners per disc; larger inputs are rejected with
+ * TDEM_ERR_BADARG (or TDEM_ERR_CAPACITY for a crowded disc) and a message in
+ * err_buf (optional, err_len bytes). The first call on a device resolves the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. All calls share the one array, which keeps the last
+ * call's contents (each call clears what must start at zero): calls that
+ * overlap on the GPU, on any streams or threads, race. The call synchronizes
+ * `stream` to read the evaluation's status. */
+int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos, const double* vel,
+                                   const double* omega, const double* radius, const double* mass,
+                                   const double* inertia, double* out_force, double* out_torque,
+                                   char* err_buf, size_t err_len, void* stream);
+
 /* 1 (default): steps run as one conditional CUDA graph launch; 0: plain launches. */
 int tdem_hm_use_graph(tdem_hm* h, int on);
 

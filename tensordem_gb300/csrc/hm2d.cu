@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -950,6 +951,61 @@ struct EngineBase {
   std::string err;
 };
 
+// Engine parameters from the public configuration (material constants as in
+// oracle-independent closed forms: E* = E/(2(1-nu^2)), G* = E/(4(2-nu)(1+nu)),
+// Tsuji beta from the restitution coefficient).
+template <class T>
+void make_params(const tdem_hm_config& c, int slots, Params<T>& P) {
+  P.n = c.n;
+  P.W = slots;
+  P.ncx = c.ncx;
+  P.ncy = c.ncy;
+  P.tiles_x = (c.ncx + 31) / 32;
+  const int tiles_y = (c.ncy + 31) / 32;
+  P.nkeys = P.tiles_x * tiles_y * 1024;
+  P.walls = c.walls;
+  P.cell = (T)c.cell;
+  P.inv_cell = (T)(1.0 / (double)P.cell);
+  P.skin = (T)c.skin;
+  P.dt = (T)c.dt;
+  P.half_dt = (T)(0.5 * c.dt);
+  const double estar = c.young / (2.0 * (1.0 - c.poisson * c.poisson));
+  const double gstar = c.young / (4.0 * (2.0 - c.poisson) * (1.0 + c.poisson));
+  double beta = 0.0;
+  if (c.restitution < 1.0) {
+    const double le = std::log(c.restitution);
+    beta = -le / std::sqrt(le * le + M_PI * M_PI);
+  }
+  P.estar2 = (T)(2.0 * estar);
+  P.gstar8 = (T)(8.0 * gstar);
+  P.damp = (T)(2.0 * std::sqrt(5.0 / 6.0) * beta);
+  P.mu = (T)c.mu;
+  P.mu_wall = (T)c.mu_wall;
+  P.gx = (T)c.gravity[0];
+  P.gy = (T)c.gravity[1];
+  P.kinv = (T)(1.0 / c.inertia_factor);
+  P.rebuild_disp = (float)(0.5 * c.skin * 0.98);
+}
+
+// The rebuild pipeline (every kernel a no-op unless ctl->rebuild_pending).
+template <class T>
+void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
+  const int nb = (P.n + kThreads - 1) / kThreads;
+  const int nk = (P.nkeys + kThreads - 1) / kThreads;
+  const int sb = (P.nkeys + kScanChunk - 1) / kScanChunk;
+  bin_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
+  scan_blocks_kernel<<<sb, kScanThreads, 0, s>>>(B.ctl, B.cell_count, B.cell_start, B.block_sums, P.nkeys);
+  scan_top_kernel<<<1, kScanThreads, 0, s>>>(B.ctl, B.block_sums, sb);
+  scan_add_kernel<<<sb, kScanThreads, 0, s>>>(B.ctl, B.cell_start, B.block_sums, P.nkeys);
+  scatter_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
+  cellsort_kernel<T><<<nk, kThreads, 0, s>>>(P, B);
+  gather_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
+  build_nbr_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
+  link_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
+  clear_keys_kernel<T><<<nk, kThreads, 0, s>>>(P, B);
+  rebuild_flip_kernel<<<1, 1, 0, s>>>(B.ctl);
+}
+
 // Step-kernel variants the autotuner chooses from: 0 = one thread per
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
 // block shapes.
@@ -1050,35 +1106,7 @@ struct Engine final : EngineBase {
   }
 
   int init(const tdem_hm_config& c) {
-    P.n = c.n;
-    P.W = c.max_neighbors;
-    P.ncx = c.ncx;
-    P.ncy = c.ncy;
-    P.tiles_x = (c.ncx + 31) / 32;
-    const int tiles_y = (c.ncy + 31) / 32;
-    P.nkeys = P.tiles_x * tiles_y * 1024;
-    P.walls = c.walls;
-    P.cell = (T)c.cell;
-    P.inv_cell = (T)(1.0 / (double)P.cell);
-    P.skin = (T)c.skin;
-    P.dt = (T)c.dt;
-    P.half_dt = (T)(0.5 * c.dt);
-    const double estar = c.young / (2.0 * (1.0 - c.poisson * c.poisson));
-    const double gstar = c.young / (4.0 * (2.0 - c.poisson) * (1.0 + c.poisson));
-    double beta = 0.0;
-    if (c.restitution < 1.0) {
-      const double le = std::log(c.restitution);
-      beta = -le / std::sqrt(le * le + M_PI * M_PI);
-    }
-    P.estar2 = (T)(2.0 * estar);
-    P.gstar8 = (T)(8.0 * gstar);
-    P.damp = (T)(2.0 * std::sqrt(5.0 / 6.0) * beta);
-    P.mu = (T)c.mu;
-    P.mu_wall = (T)c.mu_wall;
-    P.gx = (T)c.gravity[0];
-    P.gy = (T)c.gravity[1];
-    P.kinv = (T)(1.0 / c.inertia_factor);
-    P.rebuild_disp = (float)(0.5 * c.skin * 0.98);
+    make_params<T>(c, c.max_neighbors, P);
     const size_t n = (size_t)c.n, W = (size_t)c.max_neighbors;
     nblocks = (int)((n + kThreads - 1) / kThreads);
     scan_blocks = (P.nkeys + kScanChunk - 1) / kScanChunk;
@@ -1125,20 +1153,7 @@ struct Engine final : EngineBase {
   dim3 grid_n() const { return dim3((unsigned)nblocks); }
   dim3 grid_keys() const { return dim3((unsigned)((P.nkeys + kThreads - 1) / kThreads)); }
 
-  void launch_rebuild(cudaStream_t s) {
-    bin_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
-    scan_blocks_kernel<<<scan_blocks, kScanThreads, 0, s>>>(B.ctl, B.cell_count, B.cell_start, B.block_sums,
-                                                            P.nkeys);
-    scan_top_kernel<<<1, kScanThreads, 0, s>>>(B.ctl, B.block_sums, scan_blocks);
-    scan_add_kernel<<<scan_blocks, kScanThreads, 0, s>>>(B.ctl, B.cell_start, B.block_sums, P.nkeys);
-    scatter_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
-    cellsort_kernel<T><<<grid_keys(), kThreads, 0, s>>>(P, B);
-    gather_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
-    build_nbr_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
-    link_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
-    clear_keys_kernel<T><<<grid_keys(), kThreads, 0, s>>>(P, B);
-    rebuild_flip_kernel<<<1, 1, 0, s>>>(B.ctl);
-  }
+  void launch_rebuild(cudaStream_t s) { launch_rebuild_seq<T>(P, B, s); }
 
   int set_state(const double* pos, const double* vel, const double* omega, const double* radius,
                 const double* mass, const double* inertia, int host, cudaStream_t s) override {
@@ -1629,6 +1644,171 @@ int tdem_hm_last_error(const tdem_hm* h, char* buf, size_t len) {
   const size_t m = std::min(len - 1, e.size());
   std::memcpy(buf, e.data(), m);
   buf[m] = '\0';
+  return TDEM_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Allocation-free contact-force evaluation
+//
+// For callers that must not allocate device memory: code that runs while
+// another solver's CUDA graph is being captured (a cudaMalloc there breaks
+// the capture), host callbacks and real-time coupling loops where an
+// allocation's latency or failure is not acceptable, and plug-ins whose host
+// application owns all device memory. The scratch lives in one file-scope
+// device array that every GPU loading this library holds until the process
+// exits.
+// ===========================================================================
+namespace {
+
+constexpr int kNoAllocMaxDiscs = 16384;      // discs per call
+constexpr int kNoAllocSlots = 8;             // candidate partners per disc
+constexpr int kNoAllocMaxKeys = 65536;       // cell keys: grids up to 256 x 256 cells
+constexpr size_t kNoAllocBytes = 8u << 20;   // 8 MiB
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char tdem_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Bump carving of the scratch array, 256-byte aligned pieces.
+struct Carver {
+  unsigned char* base;
+  size_t off;
+  size_t cap;
+  template <class U>
+  U* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    U* p = reinterpret_cast<U*>(base + off);
+    off += std::max<size_t>(1, count) * sizeof(U);
+    return p;
+  }
+};
+
+__global__ void noalloc_clear_kernel(Ctl* ctl, int* cell_count, int* cell_fill, int nkeys) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nkeys) {
+    cell_count[k] = 0;
+    cell_fill[k] = 0;
+  }
+  if (k == 0) {
+    Ctl z{};
+    z.rebuild_pending = 1;
+    *ctl = z;
+  }
+}
+
+__global__ void noalloc_status_kernel(const Ctl* ctl, int* status_out) { *status_out = ctl->status; }
+
+// Error text into the caller's buffer, without touching the heap.
+int noalloc_fail(char* buf, size_t len, int code, const char* fmt, long long a = 0, long long b = 0) {
+  if (buf && len) snprintf(buf, len, fmt, a, b);
+  return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos, const double* vel,
+                                   const double* omega, const double* radius, const double* mass,
+                                   const double* inertia, double* out_force, double* out_torque, char* err_buf,
+                                   size_t err_len, void* stream) {
+  if (err_buf && err_len) err_buf[0] = '\0';
+  if (!cfg || !pos || !vel || !omega || !radius || !mass || !inertia || !out_force || !out_torque)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG, "null argument");
+  if (cfg->precision != 32)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG, "the allocation-free path is FP32 only");
+  if (cfg->n < 1 || cfg->n > kNoAllocMaxDiscs)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG,
+                        "the allocation-free path holds at most %lld discs per call, got %lld",
+                        (long long)kNoAllocMaxDiscs, (long long)cfg->n);
+  if (cfg->ncx < 1 || cfg->ncy < 1 || !(cfg->cell > 0) || !(cfg->inertia_factor > 0) || !(cfg->young > 0) ||
+      !(cfg->restitution > 0) || !(cfg->restitution <= 1) || !(cfg->poisson > -1.0) || !(cfg->poisson < 0.5))
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG, "invalid cell grid or material");
+  Params<float> P{};
+  make_params<float>(*cfg, kNoAllocSlots, P);
+  if (P.nkeys > kNoAllocMaxKeys)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG,
+                        "the allocation-free path holds cell grids up to 256 x 256 cells; this grid is %lld x %lld",
+                        (long long)cfg->ncx, (long long)cfg->ncy);
+  // device address of the scratch array, resolved once per device
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_CUDA, "cannot query the current device");
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_base[dev]) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, tdem_noalloc_scratch);
+      if (e != cudaSuccess)
+        return noalloc_fail(err_buf, err_len, TDEM_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed (%lld)",
+                            (long long)e);
+      g_noalloc_base[dev] = p;
+    }
+    base = g_noalloc_base[dev];
+  }
+  const size_t n = (size_t)cfg->n;
+  const size_t W = kNoAllocSlots;
+  const int nb = (int)((n + kThreads - 1) / kThreads);
+  const int sb = (P.nkeys + kScanChunk - 1) / kScanChunk;
+  Carver c{static_cast<unsigned char*>(base), 0, kNoAllocBytes};
+  Bufs<float> B{};
+  for (int b = 0; b < 2; ++b) {
+    B.pos[b] = c.take<V4<float>>(n);
+    B.vel[b] = c.take<V4<float>>(n);
+    B.head[b] = c.take<uint4>(n);
+    B.nbr[b] = c.take<unsigned>((W - kHeadSlots) * n);
+    B.hist[b] = c.take<V2<float>>(W * n);
+    B.orig[b] = c.take<int>(n);
+    B.whist[b] = c.take<V2<float>>(4 * n);
+  }
+  B.cell_count = c.take<int>((size_t)P.nkeys);
+  B.cell_start = c.take<int>((size_t)P.nkeys);
+  B.cell_fill = c.take<int>((size_t)P.nkeys);
+  B.perm = c.take<int>(n);
+  B.block_sums = c.take<int>((size_t)sb);
+  B.tmp_cell = c.take<int>(n);
+  B.tmp_off = c.take<V2<float>>(n);
+  B.diss_part = c.take<double>((size_t)nb * (kThreads / 32));
+  B.peek_part = c.take<double>((size_t)nb * 8);
+  B.peek_vel = c.take<V4<float>>(n);
+  B.peek_force = c.take<V4<float>>(n);
+  B.ctl = c.take<Ctl>(1);
+  int* status_dev = c.take<int>(1);
+  if (c.off > c.cap)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_CAPACITY, "scratch too small: %lld of %lld bytes needed",
+                        (long long)c.off, (long long)c.cap);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  // the array keeps the previous call's contents: clear what must start at zero
+  noalloc_clear_kernel<<<(P.nkeys + kThreads - 1) / kThreads, kThreads, 0, s>>>(B.ctl, B.cell_count,
+                                                                               B.cell_fill, P.nkeys);
+  pack_kernel<float><<<nb, kThreads, 0, s>>>(P, B, pos, vel, omega, radius, mass, inertia);
+  launch_rebuild_seq<float>(P, B, s);
+  force_kernel<float, kPeek><<<nb, kThreads, 0, s>>>(P, B, 0, 0, 0, 0);
+  unpack_kernel<float><<<nb, kThreads, 0, s>>>(P, B, nullptr, nullptr, nullptr, out_force, out_torque);
+  noalloc_status_kernel<<<1, 1, 0, s>>>(B.ctl, status_dev);
+  cudaError_t e = cudaGetLastError();
+  int status = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status, status_dev, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_CUDA, "CUDA error %lld during the evaluation", (long long)e);
+  if (status & kStatusNonfinite) return noalloc_fail(err_buf, err_len, TDEM_ERR_NONFINITE, "non-finite disc state");
+  if (status & kStatusCapacity)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_CAPACITY, "a disc has more than %lld candidate partners",
+                        (long long)kNoAllocSlots);
+  if (status & kStatusEscaped)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_CAPACITY, "a disc lies outside the cell grid");
+  if (status & kStatusInertia)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG, "moment of inertia must be inertia_factor * m * r^2");
   return TDEM_OK;
 }
 
