@@ -181,6 +181,17 @@ typedef struct {
   double young, poisson, restitution, mu, mu_wall;
   double gravity[2];      /* m/s^2 */
   double inertia_factor;  /* I = inertia_factor * m * r^2 (0.5 for uniform discs) */
+  /* bonded-particle model (max_bonds == 0: none; bonds come from tdem_hm_set_bonds) */
+  int32_t max_bonds;      /* bond slots per disc, 0..8 */
+  double bond_kn, bond_ks;  /* bond normal / shear stiffness (N/m) */
+  double bond_damping;    /* damping ratio zeta: c = 2 zeta sqrt(k m*) */
+  double breaking_strain; /* tensile (d - L0)/L0 threshold, times the bond's strength */
+  double shear_breaking_strain; /* objective shear threshold, times the strength */
+  /* rigid circular indenter (radius 0: none): Hertz normal + dashpot, frictionless */
+  double indenter_center[2];   /* at t = 0 (m) */
+  double indenter_velocity[2]; /* m/s */
+  double indenter_radius;      /* m */
+  int32_t load_capacity;  /* evaluations whose indenter reaction is recorded */
 } tdem_hm_config;
 
 /* Ledger slots of tdem_hm_read_ledger (J unless noted). */
@@ -197,6 +208,10 @@ enum {
   TDEM_HM_L_STATUS = 9,      /* device status bits */
   TDEM_HM_L_GRAPH = 10,      /* 1 when steps run as conditional CUDA graphs */
   TDEM_HM_L_VARIANT = 11,    /* step-kernel variant in use */
+  TDEM_HM_L_BOND_ELASTIC = 12, /* stored bond energy of intact bonds */
+  TDEM_HM_L_FRACTURE = 13,   /* cumulative spring energy released by breaks */
+  TDEM_HM_L_TOOL_WORK = 14,  /* cumulative work of the indenter on the discs */
+  TDEM_HM_L_BROKEN = 15,     /* bonds broken so far */
   TDEM_HM_L_COUNT = 16
 };
 
@@ -231,6 +246,25 @@ int tdem_hm_read_state(tdem_hm* h, double* pos, double* vel, double* omega, doub
  * Mirrors FloeBed.energy_ledger (kernel.py:483-487) plus the dissipation
  * ledger of DiskSystem (granular2d/engine.py:576-588). */
 int tdem_hm_read_ledger(tdem_hm* h, double* out_host, int count, void* stream);
+
+/* Bonds between discs of the uploaded state (call after tdem_hm_set_state,
+ * before the first step): `pairs` (count, 2) original ids and a strength
+ * factor per bond (host arrays). Rest vectors are the current positions'
+ * differences; each disc's bond covariance pseudo-inverse is precomputed
+ * (src/tensordem/dem.py:119-129, 194-202). Replaces the bond build of
+ * IceDEM.__init__ for arbitrary lattices (hexagonal sheets included). */
+int tdem_hm_set_bonds(tdem_hm* h, const int32_t* pairs, const double* strength, int64_t count, void* stream);
+
+/* Bond states, one entry per bond as original ids (lo, hi) into pairs
+ * ((capacity, 2) int32, host) and (mode, evaluation of failure) into state
+ * ((capacity, 2) int32): mode 0 intact, 1 tensile, 2 shear, 3 both; -1 for an
+ * intact bond's evaluation (the reference's fracture ledger, dem.py:131-136). */
+int tdem_hm_read_bonds(tdem_hm* h, int32_t* pairs, int32_t* state, int64_t capacity, int64_t* count,
+                       void* stream);
+
+/* Indenter reaction (ice on indenter, x, y) of each committed evaluation,
+ * up to load_capacity evaluations, into out ((capacity, 2) double, host). */
+int tdem_hm_read_load(tdem_hm* h, double* out, int64_t capacity, int64_t* count, void* stream);
 
 /* Synchronize and map the device status: TDEM_ERR_NONFINITE, TDEM_ERR_CAPACITY. */
 int tdem_hm_status(tdem_hm* h, void* stream);

@@ -144,6 +144,10 @@ class HM2DOracle:
         self.radius = np.array(radius, dtype=np.float64)
         self.mass = np.array(mass, dtype=np.float64)
         self.inertia = np.array(inertia, dtype=np.float64)
+        # clamped discs carry infinite mass and inertia: zero inverse mass
+        with np.errstate(divide="ignore"):
+            self.inv_mass = np.where(np.isfinite(self.mass), 1.0 / self.mass, 0.0)
+            self.inv_inertia = np.where(np.isfinite(self.inertia), 1.0 / self.inertia, 0.0)
         self.p = params
         self.n = len(self.pos)
         self.state = ContactState()
@@ -190,11 +194,16 @@ class HM2DOracle:
         force = np.zeros((n, 2))
         torque = np.zeros(n)
         diss = 0.0
+        self.before_contacts(pos, advance=advance)
         i, j = self.candidate_pairs()
         d = pos[j] - pos[i]
         dist = np.sqrt((d * d).sum(axis=1))
         delta = self.radius[i] + self.radius[j] - dist
         act = delta > 0.0
+        excl = self.contact_exclusions()
+        if excl is not None and len(excl):
+            act &= ~np.isin(i * n + j, excl)
+        act &= (self.inv_mass[i] + self.inv_mass[j]) > 0  # two clamped discs exchange no force
         i, j, d, dist, delta = i[act], j[act], d[act], dist[act], delta[act]
         keys = i * n + j
         xi = np.zeros((len(i), 2))
@@ -208,7 +217,7 @@ class HM2DOracle:
             tng = np.stack((-nrm[:, 1], nrm[:, 0]), axis=1)
             ra, rb = self.radius[i], self.radius[j]
             reff = ra * rb / (ra + rb)
-            meff = self.mass[i] * self.mass[j] / (self.mass[i] + self.mass[j])
+            meff = 1.0 / (self.inv_mass[i] + self.inv_mass[j])
             sq = np.sqrt(reff * delta)
             s_n = 2.0 * p.estar * sq
             f_el = (2.0 / 3.0) * s_n * delta
@@ -260,7 +269,7 @@ class HM2DOracle:
                     perp = np.array([-nw[1], nw[0]])
                     v_c = vel[idx] - (omega[idx] * r)[:, None] * perp[None, :]
                     v_n = -(v_c @ nw)
-                    f_n = np.maximum(f_el + p.damp * np.sqrt(s_n * self.mass[idx]) * v_n, 0.0)
+                    f_n = np.maximum(f_el + p.damp * np.sqrt(s_n / self.inv_mass[idx]) * v_n, 0.0)
                     v_t = v_c - (v_c @ nw)[:, None] * nw[None, :]
                     xw = self.wall_xi[w, idx] + v_t * dt
                     xw = xw - (xw @ nw)[:, None] * nw[None, :]
@@ -278,7 +287,19 @@ class HM2DOracle:
                     new_xi[idx] = xw
                 if advance:
                     self.wall_xi[w] = new_xi
-        force += self.mass[:, None] * np.asarray(p.gravity)[None, :]
+        force, torque, diss = self.extra_forces(pos, vel, omega, force, torque, diss, advance=advance)
+        free = self.inv_mass > 0
+        force[free] += self.mass[free, None] * np.asarray(p.gravity)[None, :]
+        return force, torque, diss
+
+    # hooks for the bonded engine
+    def before_contacts(self, pos, *, advance):
+        pass
+
+    def contact_exclusions(self):
+        return None
+
+    def extra_forces(self, pos, vel, omega, force, torque, diss, *, advance):
         return force, torque, diss
 
     # ----------------------------------------------------------- integration
@@ -292,22 +313,24 @@ class HM2DOracle:
             self.prime()
         h = 0.5 * self.p.dt
         for _ in range(n):
-            self.vel = self.vel + h * self.force / self.mass[:, None]
-            self.omega = self.omega + h * self.torque / self.inertia
+            self.vel = self.vel + h * self.force * self.inv_mass[:, None]
+            self.omega = self.omega + h * self.torque * self.inv_inertia
             self.pos = self.pos + self.p.dt * self.vel
+            self.steps += 1
             self.force, self.torque, d = self.evaluate(self.pos, self.vel, self.omega, advance=True)
             self.dissipated += d
-            self.vel = self.vel + h * self.force / self.mass[:, None]
-            self.omega = self.omega + h * self.torque / self.inertia
+            self.vel = self.vel + h * self.force * self.inv_mass[:, None]
+            self.omega = self.omega + h * self.torque * self.inv_inertia
             self.time += self.p.dt
-            self.steps += 1
 
     # ---------------------------------------------------------------- ledger
     def energies(self) -> dict:
         """Kinetic, gravitational, Hertz elastic and tangential spring energy (J)."""
         p = self.p
-        ke = 0.5 * float(np.sum(self.mass * (self.vel**2).sum(axis=1)) + np.sum(self.inertia * self.omega**2))
-        pe = -float(np.sum(self.mass * (self.pos @ np.asarray(p.gravity))))
+        free = self.inv_mass > 0
+        ke = 0.5 * float(np.sum(self.mass[free] * (self.vel[free]**2).sum(axis=1))
+                         + np.sum(self.inertia[free] * self.omega[free]**2))
+        pe = -float(np.sum(self.mass[free] * (self.pos[free] @ np.asarray(p.gravity))))
         un = ut = 0.0
         i, j = self.candidate_pairs()
         d = self.pos[j] - self.pos[i]
@@ -338,8 +361,198 @@ class HM2DOracle:
                     sq = np.sqrt(self.radius[idx] * dw[idx])
                     un += float(np.sum(0.4 * (2.0 / 3.0) * 2.0 * p.estar * sq * dw[idx] ** 2))
                     ut += float(np.sum(0.5 * 8.0 * p.gstar * sq * (self.wall_xi[w, idx] ** 2).sum(axis=1)))
+        extra = self.extra_energies()
+        total = ke + pe + un + ut + self.dissipated + sum(extra.values())
         return dict(kinetic=ke, potential=pe, elastic_normal=un, elastic_tangential=ut,
-                    dissipated=self.dissipated, total=ke + pe + un + ut + self.dissipated)
+                    dissipated=self.dissipated, **extra, total=total)
+
+    def extra_energies(self) -> dict:
+        return {}
 
     def active_pairs(self) -> set[tuple[int, int]]:
         return set(zip(*(x.tolist() for x in divmod(self.state.keys, self.n))))
+
+
+def pinv_sym2(a: float, b: float, c: float) -> np.ndarray:
+    """Pseudo-inverse of [[a, b], [b, c]] (cutoff 2 eps sigma_max as torch.linalg.pinv)."""
+    return np.linalg.pinv(np.array([[a, b], [b, c]], dtype=np.float64))
+
+
+class BondedHM2DOracle(HM2DOracle):
+    """FP64 bonded discs: the reference's bond model on top of Hertz-Mindlin contacts.
+
+    * Bonds carry a normal spring ``k_n (d - L0)`` (the central bond of
+      src/tensordem/dem.py:286-288) plus a shear spring ``k_s u_s`` on the
+      incremental tangential displacement and dashpots ``2 zeta sqrt(k m*)``.
+    * Irreversible breakage on tensile strain ``(d - L0)/L0 > eps_t f`` or on
+      the bond's objective shear ``(s_i + s_j)/2 > eps_s f`` (dem.py:243-268),
+      with ``f`` the bond's strength factor and ``s`` the per-disc
+      Green-Lagrange shear invariant of the least-squares deformation gradient
+      over the disc's initial bonds (dem.py:182-208), written as
+      ``E = (G + G^T + G^T G)/2`` with ``G = F - I``.
+    * A broken (or never bonded) pair interacts through the Hertz contact.
+    * A rigid circular indenter (Hertz normal + dashpot, frictionless) moves at
+      constant velocity (dem.py:294-312); its work on the discs is booked.
+    """
+
+    def __init__(self, pos, vel, omega, radius, mass, inertia, params: HMParams, *, bonds, strength,
+                 k_n, k_s, zeta, eps_t, eps_s, indenter=None):
+        super().__init__(pos, vel, omega, radius, mass, inertia, params)
+        b = np.asarray(bonds, dtype=np.int64).reshape(-1, 2)
+        self.bi = np.minimum(b[:, 0], b[:, 1])
+        self.bj = np.maximum(b[:, 0], b[:, 1])
+        self.ref = self.pos[self.bj] - self.pos[self.bi]
+        self.l0 = np.sqrt((self.ref * self.ref).sum(axis=1))
+        self.strength = np.asarray(strength, dtype=np.float64)
+        self.alive = np.ones(len(self.bi), dtype=bool)
+        self.us = np.zeros((len(self.bi), 2))
+        self.fail_eval = np.full(len(self.bi), -1, dtype=np.int64)
+        self.fail_mode = np.zeros(len(self.bi), dtype=np.uint8)
+        self.k_n, self.k_s, self.zeta = float(k_n), float(k_s), float(zeta)
+        self.eps_t, self.eps_s = float(eps_t), float(eps_s)
+        self.fracture_released = 0.0
+        self.tool_work = 0.0
+        self.indenter = indenter  # dict(center=(x, y), velocity=(vx, vy), radius=R)
+        self.evals = 0
+        self.reaction = np.zeros(2)
+        # constant pseudo-inverse of each disc's bond covariance
+        n = self.n
+        cov = np.zeros((n, 2, 2))
+        outer = self.ref[:, :, None] * self.ref[:, None, :]
+        np.add.at(cov, self.bi, outer)
+        np.add.at(cov, self.bj, outer)
+        self.pinv = np.linalg.pinv(cov)
+        self.bond_keys = np.sort(self.bi * n + self.bj)
+
+    def contact_exclusions(self):
+        # bonds intact after this evaluation's break test (dem.py:251 precedes
+        # the pair forces: a bond broken now already acts as a contact)
+        return (self.bi * self.n + self.bj)[self._alive_now]
+
+    def before_contacts(self, pos, *, advance):
+        """Break test at this evaluation's positions (dem.py:243-277)."""
+        p = self.p
+        s = self.strains(pos)
+        i, j = self.bi, self.bj
+        cur = pos[j] - pos[i]
+        d = np.sqrt((cur * cur).sum(axis=1))
+        u = cur - self.ref
+        ext = (2.0 * (self.ref * u).sum(axis=1) + (u * u).sum(axis=1)) / (d + self.l0)
+        tensile = ext / self.l0
+        shear = 0.5 * (s[i] + s[j])
+        tf = tensile > self.eps_t * self.strength
+        sf = shear > self.eps_s * self.strength
+        new = self.alive & (tf | sf)
+        self._ext = ext
+        self._alive_now = self.alive & ~new
+        if advance and new.any():
+            self.fail_eval[new] = self.evals
+            self.fail_mode[new] = tf[new].astype(np.uint8) + 2 * sf[new].astype(np.uint8)
+            # spring energy released, minus the Hertz energy a still-overlapping
+            # pair acquires as a contact at once (dem.py:270-277 books both)
+            ov = np.maximum(self.radius[i[new]] + self.radius[j[new]] - d[new], 0.0)
+            reff = self.radius[i[new]] * self.radius[j[new]] / (self.radius[i[new]] + self.radius[j[new]])
+            acquired = 0.4 * (2.0 / 3.0) * 2.0 * p.estar * np.sqrt(reff * ov) * ov * ov
+            self.fracture_released += float(np.sum(0.5 * self.k_n * ext[new] ** 2
+                                                    + 0.5 * self.k_s * (self.us[new] ** 2).sum(axis=1)
+                                                    - acquired))
+
+    def strains(self, pos) -> np.ndarray:
+        """Objective shear invariant per disc (dem.py:182-208, displacement form)."""
+        cur = pos[self.bj] - pos[self.bi]
+        u = cur - self.ref
+        g = np.zeros((self.n, 2, 2))
+        m = u[:, :, None] * self.ref[:, None, :]
+        np.add.at(g, self.bi, m)
+        np.add.at(g, self.bj, m)
+        g = g @ self.pinv
+        e = 0.5 * (g + np.transpose(g, (0, 2, 1)) + np.transpose(g, (0, 2, 1)) @ g)
+        return np.sqrt((e[:, 0, 0] - e[:, 1, 1]) ** 2 + 4.0 * e[:, 0, 1] ** 2)
+
+    def extra_forces(self, pos, vel, omega, force, torque, diss, *, advance):
+        p = self.p
+        dt = p.dt
+        i, j = self.bi, self.bj
+        cur = pos[j] - pos[i]
+        d = np.sqrt((cur * cur).sum(axis=1))
+        ext = self._ext
+        alive = self._alive_now
+        a = np.flatnonzero(alive & ((self.inv_mass[i] + self.inv_mass[j]) > 0))
+        if len(a):
+            ia, ja = i[a], j[a]
+            nrm = cur[a] / d[a, None]
+            tng = np.stack((-nrm[:, 1], nrm[:, 0]), axis=1)
+            ra, rb = self.radius[ia], self.radius[ja]
+            meff = 1.0 / (self.inv_mass[ia] + self.inv_mass[ja])
+            v_rel = vel[ia] - vel[ja] + (omega[ia] * ra + omega[ja] * rb)[:, None] * tng
+            v_n = (v_rel * nrm).sum(axis=1)
+            v_t = v_rel - v_n[:, None] * nrm
+            us = self.us[a] + v_t * dt
+            us = us - (us * nrm).sum(axis=1)[:, None] * nrm
+            c_n = 2.0 * self.zeta * np.sqrt(self.k_n * meff)
+            c_s = 2.0 * self.zeta * np.sqrt(self.k_s * meff)
+            f_a = (self.k_n * ext[a] - c_n * v_n)[:, None] * nrm - self.k_s * us - c_s[:, None] * v_t
+            cr = nrm[:, 0] * f_a[:, 1] - nrm[:, 1] * f_a[:, 0]
+            np.add.at(force, ia, f_a)
+            np.add.at(force, ja, -f_a)
+            np.add.at(torque, ia, ra * cr)
+            np.add.at(torque, ja, rb * cr)
+            diss += float(np.sum(c_n * v_n**2 + c_s * (v_t * v_t).sum(axis=1))) * dt
+            if advance:
+                self.us[a] = us
+        if advance:
+            self.alive = alive
+        # indenter
+        self.reaction = np.zeros(2)
+        if self.indenter is not None:
+            t = self.evals * dt
+            c = np.asarray(self.indenter["center"]) + t * np.asarray(self.indenter["velocity"])
+            R = float(self.indenter["radius"])
+            dv = pos - c[None, :]
+            dd = np.sqrt((dv * dv).sum(axis=1))
+            delta = R + self.radius - dd
+            k = np.flatnonzero(delta > 0)
+            if len(k):
+                nw = dv[k] / dd[k, None]
+                r = self.radius[k]
+                reff = R * r / (R + r)
+                sq = np.sqrt(reff * delta[k])
+                s_n = 2.0 * p.estar * sq
+                f_el = (2.0 / 3.0) * s_n * delta[k]
+                v_app = -((vel[k] - np.asarray(self.indenter["velocity"])) * nw).sum(axis=1)
+                meff = np.where(self.inv_mass[k] > 0, 1.0 / np.maximum(self.inv_mass[k], 1e-300), 0.0)
+                f_n = np.maximum(f_el + p.damp * np.sqrt(s_n * meff) * v_app, 0.0)
+                f = f_n[:, None] * nw
+                np.add.at(force, k, f)
+                self.reaction = -f.sum(axis=0)
+                diss += float(np.sum((f_n - f_el) * v_app)) * dt
+                if advance:
+                    self.tool_work += dt * float(-(self.reaction @ np.asarray(self.indenter["velocity"])))
+        if advance:
+            self.evals += 1
+        return force, torque, diss
+
+    def extra_energies(self) -> dict:
+        i, j = self.bi, self.bj
+        cur = self.pos[j] - self.pos[i]
+        d = np.sqrt((cur * cur).sum(axis=1))
+        u = cur - self.ref
+        ext = (2.0 * (self.ref * u).sum(axis=1) + (u * u).sum(axis=1)) / (d + self.l0)
+        a = self.alive & ((self.inv_mass[i] + self.inv_mass[j]) > 0)
+        bond = float(np.sum(0.5 * self.k_n * ext[a] ** 2 + 0.5 * self.k_s * (self.us[a] ** 2).sum(axis=1)))
+        # Hertz energy stored at the indenter (state at t = (evals - 1) dt)
+        tool_elastic = 0.0
+        if self.indenter is not None and self.evals > 0:
+            t = (self.evals - 1) * self.p.dt
+            c = np.asarray(self.indenter["center"]) + t * np.asarray(self.indenter["velocity"])
+            R = float(self.indenter["radius"])
+            dd = np.sqrt(((self.pos - c[None, :]) ** 2).sum(axis=1))
+            delta = R + self.radius - dd
+            k = (delta > 0) & (self.inv_mass > 0)
+            if k.any():
+                reff = R * self.radius[k] / (R + self.radius[k])
+                sq = np.sqrt(reff * delta[k])
+                tool_elastic = float(np.sum(0.4 * (2.0 / 3.0) * 2.0 * self.p.estar * sq * delta[k] ** 2))
+        # fracture release leaves the mechanical budget; the tool feeds it
+        return dict(bond_elastic=bond, tool_elastic=tool_elastic, fracture_released=self.fracture_released,
+                    tool_work=-self.tool_work)

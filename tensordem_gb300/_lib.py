@@ -72,6 +72,11 @@ class HMConfigC(C.Structure):
         ("young", C.c_double), ("poisson", C.c_double), ("restitution", C.c_double),
         ("mu", C.c_double), ("mu_wall", C.c_double), ("gravity", C.c_double * 2),
         ("inertia_factor", C.c_double),
+        ("max_bonds", C.c_int32), ("bond_kn", C.c_double), ("bond_ks", C.c_double),
+        ("bond_damping", C.c_double), ("breaking_strain", C.c_double),
+        ("shear_breaking_strain", C.c_double), ("indenter_center", C.c_double * 2),
+        ("indenter_velocity", C.c_double * 2), ("indenter_radius", C.c_double),
+        ("load_capacity", C.c_int32),
     ]
 
 
@@ -110,6 +115,9 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_hm_use_graph": (i32, [vp, i32]),
         "tdem_hm_num_variants": (i32, []),
         "tdem_hm_step_kernel": (i32, [vp, vp]),
+        "tdem_hm_set_bonds": (i32, [vp, vp, vp, C.c_int64, vp]),
+        "tdem_hm_read_bonds": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
+        "tdem_hm_read_load": (i32, [vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_hm_rebuild_pending": (i32, [vp, vp]),
         "tdem_hm_set_variant": (i32, [vp, i32]),
         "tdem_hm_get_variant": (i32, [vp]),

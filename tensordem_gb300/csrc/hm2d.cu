@@ -78,6 +78,11 @@ __device__ __forceinline__ PairOut<T> pair_force(const Params<T>& P, const Geo<T
                                                  V2<T> xi) {
   PairOut<T> o;
   o.active = true;
+  if (!(va.w + vb.w > T(0))) {  // two clamped discs exchange no force
+    o.fx = o.fy = o.cr = o.diss = o.un = o.ut = T(0);
+    o.xi = V2<T>{T(0), T(0)};
+    return o;
+  }
   const T d = dev_sqrt(g.d2);
   const T delta = g.rs - d;
   const T nx = g.dx / d, ny = g.dy / d;
@@ -250,22 +255,240 @@ __device__ __forceinline__ void do_slot(const Params<T>& P, const V4<T>* __restr
   tq.add(p.z * o.cr);
 }
 
+// Symmetric 2x2 pseudo-inverse (eigen-decomposition, cutoff 2 eps sigma_max).
+template <class T>
+__device__ __forceinline__ V4<T> pinv_sym2_dev(T a, T b, T c) {
+  const T eps = sizeof(T) == 4 ? T(1.1920929e-07) : T(2.220446049250313e-16);
+  const T mean = T(0.5) * (a + c), half = T(0.5) * (a - c);
+  const T rad = dev_sqrt(half * half + b * b);
+  const T l1 = mean + rad, l2 = mean - rad;
+  const T smax = fmax(fabs(l1), fabs(l2));
+  const T cut = T(2) * eps * smax;
+  if (fabs(l1) > cut && fabs(l2) > cut) {
+    const T det = a * c - b * b;
+    return V4<T>{c / det, -b / det, -b / det, a / det};
+  }
+  if (!(fabs(l1) > cut)) return V4<T>{T(0), T(0), T(0), T(0)};
+  T vx, vy;
+  if (fabs(b) > T(0)) {
+    vx = l1 - c;
+    vy = b;
+  } else if (a >= c) {
+    vx = T(1);
+    vy = T(0);
+  } else {
+    vx = T(0);
+    vy = T(1);
+  }
+  const T nv = dev_sqrt(vx * vx + vy * vy);
+  vx /= nv;
+  vy /= nv;
+  return V4<T>{vx * vx / l1, vx * vy / l1, vx * vy / l1, vy * vy / l1};
+}
+
+// b - a of two discs through their cell origins (any order).
+template <class T>
+__device__ __forceinline__ V2<T> cell_delta(const Params<T>& P, const V4<T>& a, const V4<T>& b) {
+  const int ca = lane_to_cell(a.w), cb = lane_to_cell(b.w);
+  return V2<T>{fma((T)((cb & 0xFFFF) - (ca & 0xFFFF)), P.cell, b.x - a.x),
+               fma((T)((cb >> 16) - (ca >> 16)), P.cell, b.y - a.y)};
+}
+
+// Per-disc objective shear invariant over the disc's initial bonds (broken or
+// not), the reference's local Green-Lagrange measure (dem.py:182-208) written
+// with G = F - I: E = (G + G^T + G^T G) / 2.
+template <class T>
+__global__ void strain_kernel(Params<T> P, Bufs<T> B) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const int sp = B.ctl->sp, lp = B.ctl->lp;
+  const int bc = B.bcnt[lp][i];
+  T sv = T(0);
+  if (bc > 0) {
+    const V4<T>* pos = B.pos[sp];
+    const V4<T> p = pos[i];
+    T g00 = 0, g01 = 0, g10 = 0, g11 = 0;
+    for (int s = 0; s < bc; ++s) {
+      const size_t k = (size_t)s * P.n + i;
+      const int j = (int)(B.bpart[lp][k] & kBondIdx);
+      const V2<T> cur = cell_delta<T>(P, p, pos[j]);
+      const V2<T> r = B.bref[lp][k];
+      const T ux = cur.x - r.x, uy = cur.y - r.y;
+      g00 += ux * r.x;
+      g01 += ux * r.y;
+      g10 += uy * r.x;
+      g11 += uy * r.y;
+    }
+    const V4<T> q = B.bpinv[lp][i];
+    const T f00 = g00 * q.x + g01 * q.z, f01 = g00 * q.y + g01 * q.w;
+    const T f10 = g10 * q.x + g11 * q.z, f11 = g10 * q.y + g11 * q.w;
+    const T e00 = T(0.5) * (T(2) * f00 + f00 * f00 + f10 * f10);
+    const T e11 = T(0.5) * (T(2) * f11 + f01 * f01 + f11 * f11);
+    const T e01 = T(0.5) * ((f01 + f10) + f00 * f01 + f10 * f11);
+    const T dd = e00 - e11;
+    sv = dev_sqrt(dd * dd + T(4) * (e01 * e01));
+  }
+  B.strain[i] = sv;
+}
+
 // Per-thread ledger terms of the particles a thread processed.
 template <class T>
 struct ThreadLedger {
   float vmax2 = 0.0f;
   T diss = T(0), un = T(0), ut = T(0);
+  T ub = T(0), frac = T(0);   // bond elastic energy, fracture release
+  T ifx = T(0), ify = T(0);  // indenter force on this thread's discs
+  int broke = 0;
   double ke = 0.0, pe = 0.0;
   bool bad = false;
 };
 
+// One bond slot s of disc i: the break test (FP64 comparison of the strains
+// against the bond's thresholds), then the bond law while intact, or the Hertz
+// contact with the slot's history once broken (dem.py:243-292 semantics: a
+// bond broken at this evaluation already acts as a contact).
+template <class T, int MODE>
+__device__ __forceinline__ void do_bond(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i, int s,
+                                        long long eval, const V4<T>& p, const V4<T>& v, Acc<T>& fx, Acc<T>& fy,
+                                        Acc<T>& tq, ThreadLedger<T>& L, int primed) {
+  constexpr bool COMMIT = MODE != kPeek;
+  const size_t k = (size_t)s * P.n + i;
+  const unsigned w = B.bpart[lp][k];
+  const int j = (int)(w & kBondIdx);
+  const V4<T> q = B.pos[sp][j];
+  const V4<T> wv = B.vel[sp][j];
+  const bool owner = i < j;
+  const V4<T>& a = owner ? p : q;
+  const V4<T>& b = owner ? q : p;
+  const V4<T>& va = owner ? v : wv;
+  const V4<T>& vb = owner ? wv : v;
+  const V2<T> rs = B.bref[lp][k];
+  const V2<T> ref = owner ? rs : V2<T>{-rs.x, -rs.y};
+  const Geo<T> g = pair_geo<T>(P, a, b);
+  bool broken = (w & kBondBroken) != 0u;
+  V2<T> us = B.bus[lp][k];
+  if (!broken) {
+    const T ux = g.dx - ref.x, uy = g.dy - ref.y;
+    const T d = dev_sqrt(g.d2);
+    const T l0 = dev_sqrt(ref.x * ref.x + ref.y * ref.y);
+    const T ext = (T(2) * (ref.x * ux + ref.y * uy) + (ux * ux + uy * uy)) / (d + l0);
+    const T tensile = ext / l0;
+    const T shear = T(0.5) * (B.strain[i] + B.strain[j]);
+    const double str = (double)B.bstr[lp][k];
+    const bool bt = (double)tensile > P.eps_t * str;
+    const bool bs = (double)shear > P.eps_s * str;
+    if (bt || bs) {
+      broken = true;
+      if (owner) {
+        // spring energy released, minus the Hertz energy a still-overlapping
+        // pair acquires as a contact at once (dem.py:270-277 books both)
+        const T ov = fmax(g.rs - d, T(0));
+        const T acquired = T(0.4) * (T(2) / T(3)) * P.estar2 * dev_sqrt(a.z * b.z / g.rs * ov) * ov * ov;
+        L.frac += T(0.5) * P.kn * ext * ext + T(0.5) * P.ks * (us.x * us.x + us.y * us.y) - acquired;
+        L.broke += 1;
+      }
+      if (COMMIT) {
+        const unsigned mode = (bt ? 1u : 0u) | (bs ? 2u : 0u);
+        B.bpart[lp][k] = (w & kBondIdx) | (mode << kBondModeShift) | kBondBroken;
+        B.bfail[lp][k] = (int)eval;
+      }
+      us = V2<T>{T(0), T(0)};  // the contact starts without tangential history
+    } else if (va.w + vb.w > T(0)) {
+      const T nx = g.dx / d, ny = g.dy / d;
+      const T meff = T(1) / (va.w + vb.w);
+      const T wsum = va.z * a.z + vb.z * b.z;
+      const T vrx = (va.x - vb.x) - wsum * ny;
+      const T vry = (va.y - vb.y) + wsum * nx;
+      const T vn = vrx * nx + vry * ny;
+      const T vtx = vrx - vn * nx, vty = vry - vn * ny;
+      T sx = us.x + vtx * P.dt, sy = us.y + vty * P.dt;
+      const T sn = sx * nx + sy * ny;
+      sx -= sn * nx;
+      sy -= sn * ny;
+      const T cn = T(2) * P.bzeta * dev_sqrt(P.kn * meff);
+      const T cs = T(2) * P.bzeta * dev_sqrt(P.ks * meff);
+      const T fnm = P.kn * ext - cn * vn;
+      const T fax = fnm * nx - P.ks * sx - cs * vtx;
+      const T fay = fnm * ny - P.ks * sy - cs * vty;
+      const T cr = nx * fay - ny * fax;
+      if (owner) {
+        fx.add(fax);
+        fy.add(fay);
+        L.diss += (cn * vn * vn + cs * (vtx * vtx + vty * vty)) * P.dt;
+        L.ub += T(0.5) * P.kn * ext * ext + T(0.5) * P.ks * (sx * sx + sy * sy);
+      } else {
+        fx.add(-fax);
+        fy.add(-fay);
+      }
+      tq.add(p.z * cr);
+      if (COMMIT) B.bus[lp][k] = V2<T>{sx, sy};
+      return;
+    } else {
+      return;  // intact bond between two clamped discs
+    }
+  }
+  // broken: Hertz-Mindlin contact with the slot's history
+  const bool stored = (us.x != T(0)) || (us.y != T(0));
+  if (!(g.d2 < g.rs * g.rs)) {
+    if (COMMIT && stored) B.bus[lp][k] = V2<T>{T(0), T(0)};
+    return;
+  }
+  const PairOut<T> o = pair_force<T>(P, g, a, va, b, vb, us);
+  if (COMMIT) B.bus[lp][k] = o.xi;
+  if (owner) {
+    fx.add(o.fx);
+    fy.add(o.fy);
+    L.diss += o.diss;
+    L.un += o.un;
+    L.ut += (MODE == kPeek && !primed) ? T(0) : o.ut;
+  } else {
+    fx.add(-o.fx);
+    fy.add(-o.fy);
+  }
+  tq.add(p.z * o.cr);
+}
+
+// Rigid circular indenter, Hertz normal + Tsuji dashpot, frictionless
+// (the reference's tool, dem.py:294-312, with the Hertz law of the contacts).
+// Distances in FP64 from the integer cell origin, only for discs near it.
+template <class T>
+__device__ __forceinline__ void indenter_contact(const Params<T>& P, long long eval, const V4<T>& p, const V4<T>& v,
+                                                 Acc<T>& fx, Acc<T>& fy, ThreadLedger<T>& L) {
+  const int c = lane_to_cell(p.w);
+  const double t = (double)eval * (double)P.dt;
+  const double cx = P.ind_x0 + t * P.ind_vx, cy = P.ind_y0 + t * P.ind_vy;
+  const double x = (double)(c & 0xFFFF) * (double)P.cell + (double)p.x;
+  const double y = (double)(c >> 16) * (double)P.cell + (double)p.y;
+  const double dx = x - cx, dy = y - cy;
+  const double R = (double)P.irad, r = (double)p.z;
+  const double reach = R + r;
+  if (fabs(dx) >= reach || fabs(dy) >= reach) return;
+  const double dd = sqrt(dx * dx + dy * dy);
+  const double delta = reach - dd;
+  if (!(delta > 0.0) || !(v.w > T(0))) return;
+  const double nx = dx / dd, ny = dy / dd;
+  const double reff = R * r / reach;
+  const double sq = sqrt(reff * delta);
+  const double sn = 2.0 * ((double)P.estar2 * 0.5) * sq;
+  const double fel = (2.0 / 3.0) * sn * delta;
+  const double vapp = -(((double)v.x - P.ind_vx) * nx + ((double)v.y - P.ind_vy) * ny);
+  const double m = 1.0 / (double)v.w;
+  const double fn = fmax(fel + (double)P.damp * sqrt(sn * m) * vapp, 0.0);
+  fx.add((T)(fn * nx));
+  fy.add((T)(fn * ny));
+  L.ifx += (T)(fn * nx);
+  L.ify += (T)(fn * ny);
+  L.diss += (T)((fn - fel) * vapp * (double)P.dt);
+  L.un += (T)(0.4 * fel * delta);
+}
+
 // Everything one particle does in one evaluation: its candidate slots, the
 // walls, and (committing modes) the velocity-Verlet update into the other
 // buffers. p, v, hd are the particle's own loads (already issued).
-template <class T, int MODE>
+template <class T, int MODE, bool FEAT>
 __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i,
                                                  const V4<T>& p, const V4<T>& v, const uint4& hd, int primed,
-                                                 ThreadLedger<T>& L) {
+                                                 long long eval, ThreadLedger<T>& L) {
   constexpr bool COMMIT = MODE != kPeek;
   const int n = P.n;
   const V4<T>* __restrict__ pos = B.pos[sp];
@@ -281,6 +504,10 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
   if (cnt > 2) q2 = pos[hd.w];
   unsigned nmask = 0u;
   Acc<T> fx, fy, tq;
+  if (FEAT && P.BMAX > 0) {
+    const int bc = B.bcnt[lp][i];
+    for (int s = 0; s < bc; ++s) do_bond<T, MODE>(P, B, sp, lp, i, s, eval, p, v, fx, fy, tq, L, primed);
+  }
   if (cnt > 0)
     do_slot<T, MODE>(P, vel, hist, i, (int)hd.y, 0, (size_t)i, p, v, q0, mask, nmask, fx, fy, tq, L.diss, L.un,
                      L.ut, primed);
@@ -298,7 +525,8 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
   }
   if (COMMIT && nmask != mask) B.head[lp][i].x = (hd.x & 0xFFu) | (nmask << 8);
   const int c = lane_to_cell(p.w);
-  if (P.walls) {
+  if (FEAT && P.irad > T(0)) indenter_contact<T>(P, eval, p, v, fx, fy, L);
+  if (P.walls && v.w > T(0)) {
     const int cx = c & 0xFFFF, cy = c >> 16;
     if ((cx == 0 || cx == P.ncx - 1 || cy == 0 || cy == P.ncy - 1)) {
       V2<T>* wh = B.whist[lp];
@@ -317,23 +545,26 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
     }
   }
   const T Fx = fx.get(), Fy = fy.get(), Tz = tq.get();
-  const T inv_m = v.w;
+  const T inv_m = v.w;  // 0 for a clamped disc
+  const bool free = inv_m > T(0);
   const T inv_i = inv_m * P.kinv / (p.z * p.z);
-  const T ax = Fx * inv_m + P.gx;
-  const T ay = Fy * inv_m + P.gy;
+  const T ax = free ? Fx * inv_m + P.gx : T(0);
+  const T ay = free ? Fy * inv_m + P.gy : T(0);
   const T al = Tz * inv_i;
   if (MODE == kPeek) {
     const T h = primed ? P.half_dt : T(0);
     const T vx = v.x + h * ax, vy = v.y + h * ay, om = v.z + h * al;
     B.peek_vel[i] = V4<T>{vx, vy, om, T(0)};
-    B.peek_force[i] = V4<T>{Fx + P.gx / inv_m, Fy + P.gy / inv_m, Tz, T(0)};
+    B.peek_force[i] = free ? V4<T>{Fx + P.gx / inv_m, Fy + P.gy / inv_m, Tz, T(0)} : V4<T>{Fx, Fy, Tz, T(0)};
     // energies in FP64: the potential needs absolute positions
-    const double m = 1.0 / (double)inv_m;
-    const double r = (double)p.z;
-    L.ke += 0.5 * m * ((double)vx * vx + (double)vy * vy) + 0.5 * (m * r * r / (double)P.kinv) * (double)om * om;
-    const double x = (double)(c & 0xFFFF) * (double)P.cell + (double)p.x;
-    const double y = (double)(c >> 16) * (double)P.cell + (double)p.y;
-    L.pe += -m * ((double)P.gx * x + (double)P.gy * y);
+    if (free) {
+      const double m = 1.0 / (double)inv_m;
+      const double r = (double)p.z;
+      L.ke += 0.5 * m * ((double)vx * vx + (double)vy * vy) + 0.5 * (m * r * r / (double)P.kinv) * (double)om * om;
+      const double x = (double)(c & 0xFFFF) * (double)P.cell + (double)p.x;
+      const double y = (double)(c >> 16) * (double)P.cell + (double)p.y;
+      L.pe += -m * ((double)P.gx * x + (double)P.gy * y);
+    }
   } else {
     T vx, vy, om;
     if (MODE == kPrime) {
@@ -354,20 +585,28 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
   }
 }
 
-// Commit epilogue: per-warp ledger partial and speed bound, then the last
-// warp of the last block does the step bookkeeping and sets the graph's
-// conditions. No block-wide barrier: warps retire as soon as they are done.
-template <class T>
+// Commit epilogue: per-warp ledger partials and the speed bound, then the
+// last warp of the last block does the step bookkeeping (indenter reaction,
+// rebuild trigger) and sets the graph's conditions. No block-wide barrier:
+// warps retire as soon as they are done.
+template <class T, bool FEAT>
 __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T>& B, int sp,
                                                 const ThreadLedger<T>& L, cudaGraphConditionalHandle h_rebuild,
                                                 cudaGraphConditionalHandle h_loop, int use_cond) {
   Ctl* ctl = B.ctl;
   float wm = L.vmax2;
-  T wd = L.diss;
+  T wd = L.diss, wf = L.frac, wix = L.ifx, wiy = L.ify;
+  int wb = L.broke;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, off));
     wd += __shfl_xor_sync(0xffffffffu, wd, off);
+    if (FEAT) {
+      wf += __shfl_xor_sync(0xffffffffu, wf, off);
+      wix += __shfl_xor_sync(0xffffffffu, wix, off);
+      wiy += __shfl_xor_sync(0xffffffffu, wiy, off);
+      wb += __shfl_xor_sync(0xffffffffu, wb, off);
+    }
   }
   if (__any_sync(0xffffffffu, L.bad) && (threadIdx.x & 31) == 0) atomicOr(&ctl->status, (int)kStatusNonfinite);
   __shared__ unsigned s_warps_done;
@@ -376,6 +615,14 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
   if ((threadIdx.x & 31) != 0) return;
   const size_t gw = (size_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   if (wd != T(0)) B.diss_part[gw] += (double)wd;
+  if (FEAT && wf != T(0)) B.frac_part[gw] += (double)wf;
+  if (FEAT && wb) atomicAdd(&ctl->broken, wb);
+  if (FEAT && (wix != T(0) || wiy != T(0))) {
+    const unsigned e = atomicAdd(&ctl->load_entries, 1u);
+    B.ind_part[3 * (size_t)e] = (double)gw;
+    B.ind_part[3 * (size_t)e + 1] = (double)wix;
+    B.ind_part[3 * (size_t)e + 2] = (double)wiy;
+  }
   const unsigned bits = __float_as_uint(wm);
   if (bits > *reinterpret_cast<volatile unsigned*>(&ctl->vmax2_bits)) atomicMax(&ctl->vmax2_bits, bits);
   __threadfence();
@@ -386,6 +633,37 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
   if (t != gridDim.x - 1) return;
   // last block of the grid
   __threadfence();
+  if (FEAT && P.irad > T(0)) {
+    // sum the indenter partials in warp order (deterministic)
+    const unsigned m = *reinterpret_cast<volatile unsigned*>(&ctl->load_entries);
+    double* e = B.ind_part;
+    for (unsigned a = 1; a < m; ++a) {
+      const double k0 = e[3 * a], k1 = e[3 * a + 1], k2 = e[3 * a + 2];
+      unsigned b = a;
+      while (b > 0 && e[3 * (b - 1)] > k0) {
+        e[3 * b] = e[3 * (b - 1)];
+        e[3 * b + 1] = e[3 * (b - 1) + 1];
+        e[3 * b + 2] = e[3 * (b - 1) + 2];
+        --b;
+      }
+      e[3 * b] = k0;
+      e[3 * b + 1] = k1;
+      e[3 * b + 2] = k2;
+    }
+    double sx = 0.0, sy = 0.0;
+    for (unsigned a = 0; a < m; ++a) {
+      sx += e[3 * a + 1];
+      sy += e[3 * a + 2];
+    }
+    ctl->reaction_x = -sx;
+    ctl->reaction_y = -sy;
+    ctl->tool_work += (double)P.dt * (sx * P.ind_vx + sy * P.ind_vy);
+    if (ctl->evals < (long long)P.load_cap) {
+      B.load[2 * ctl->evals] = -sx;
+      B.load[2 * ctl->evals + 1] = -sy;
+    }
+    ctl->load_entries = 0u;
+  }
   const float vmax = sqrtf(__uint_as_float(atomicExch(&ctl->vmax2_bits, 0u)));
   ctl->ticket = 0;
   ctl->sp = sp ^ 1;
@@ -402,7 +680,7 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
 }
 
 // One thread per particle (variant 0) and the read-back kernel.
-template <class T, int MODE>
+template <class T, int MODE, bool FEAT>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel(Params<T> P, Bufs<T> B,
                                                             cudaGraphConditionalHandle h_rebuild,
                                                             cudaGraphConditionalHandle h_loop, int use_cond,
@@ -414,7 +692,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel
     const V4<T> p = B.pos[sp][i];
     const V4<T> v = B.vel[sp][i];
     const uint4 hd = B.head[lp][i];
-    process_particle<T, MODE>(P, B, sp, lp, i, p, v, hd, primed, L);
+    process_particle<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, primed, B.ctl->evals, L);
   }
   if (MODE == kPeek) {
     const double k = block_sum_d(L.ke);
@@ -422,29 +700,38 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel
     const double a = block_sum_t<T>(L.un);
     const double b = block_sum_t<T>(L.ut);
     const double d = block_sum_t<T>(primed ? L.diss : T(0));
+    const double ub = block_sum_t<T>(L.ub);
+    const double fr = block_sum_t<T>(L.frac);
+    const double tw = block_sum_t<T>((L.ifx * (T)P.ind_vx + L.ify * (T)P.ind_vy) * P.dt);
+    const double nb = block_sum_t<T>((T)L.broke);
     if (threadIdx.x == 0) {
-      double* o = B.peek_part + (size_t)blockIdx.x * 8;
+      double* o = B.peek_part + (size_t)blockIdx.x * 12;
       o[0] = k;
       o[1] = g;
       o[2] = a;
       o[3] = b;
       o[4] = d;
+      o[5] = ub;
+      o[6] = fr;
+      o[7] = tw;
+      o[8] = nb;
     }
     return;
   }
-  commit_epilogue<T>(P, B, sp, L, h_rebuild, h_loop, use_cond);
+  commit_epilogue<T, FEAT>(P, B, sp, L, h_rebuild, h_loop, use_cond);
 }
 
 // Persistent grid-stride variant: while a thread works on particle i it has
 // the loads of its next particle already in flight (twice the memory-level
 // parallelism of variant 0 at the cost of a dozen registers).
-template <class T, int MODE, int BLOCK, int MINB>
+template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
 __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs<T> B,
                                                                cudaGraphConditionalHandle h_rebuild,
                                                                cudaGraphConditionalHandle h_loop, int use_cond,
                                                                int primed) {
   static_assert(MODE != kPeek, "read-back uses force_kernel");
   const int sp = B.ctl->sp, lp = B.ctl->lp;
+  const long long eval = B.ctl->evals;
   const int stride = gridDim.x * BLOCK;
   int i = blockIdx.x * BLOCK + threadIdx.x;
   ThreadLedger<T> L;
@@ -464,13 +751,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
       vn = B.vel[sp][nx];
       hn = B.head[lp][nx];
     }
-    process_particle<T, MODE>(P, B, sp, lp, i, p, v, hd, primed, L);
+    process_particle<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, primed, eval, L);
     i = nx;
     p = pn;
     v = vn;
     hd = hn;
   }
-  commit_epilogue<T>(P, B, sp, L, h_rebuild, h_loop, use_cond);
+  commit_epilogue<T, FEAT>(P, B, sp, L, h_rebuild, h_loop, use_cond);
 }
 
 // Bulk-copy variant: each block streams its tiles of own-particle state
@@ -480,7 +767,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
 // gathered from global memory (mostly L2 hits thanks to the cell sort).
 constexpr long long kWaitBudget = 2000000000LL;  // ~1 s of SM clock per wait
 
-template <class T, int MODE, int BLOCK, int MINB>
+template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
 __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bufs<T> B,
                                                                  cudaGraphConditionalHandle h_rebuild,
                                                                  cudaGraphConditionalHandle h_loop, int use_cond,
@@ -491,6 +778,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bu
   __shared__ alignas(128) uint4 s_head[2][BLOCK];
   __shared__ alignas(8) uint64_t s_bar[2];
   const int sp = B.ctl->sp, lp = B.ctl->lp;
+  const long long eval = B.ctl->evals;
   const int n = P.n;
   const int ntiles = (n + BLOCK - 1) / BLOCK;
   ThreadLedger<T> L;
@@ -527,11 +815,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bu
       const V4<T> p = s_pos[buf][threadIdx.x];
       const V4<T> v = s_vel[buf][threadIdx.x];
       const uint4 hd = s_head[buf][threadIdx.x];
-      process_particle<T, MODE>(P, B, sp, lp, i, p, v, hd, primed, L);
+      process_particle<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, primed, eval, L);
     }
     __syncthreads();
   }
-  commit_epilogue<T>(P, B, sp, L, h_rebuild, h_loop, use_cond);
+  commit_epilogue<T, FEAT>(P, B, sp, L, h_rebuild, h_loop, use_cond);
 }
 
 // ---------------------------------------------------------------------------
@@ -695,8 +983,38 @@ __global__ void gather_kernel(Params<T> P, Bufs<T> B) {
   B.pos[sp ^ 1][p] = V4<T>{off.x, off.y, q.z, cell_to_lane(B.tmp_cell[i], T(0))};
   B.vel[sp ^ 1][p] = B.vel[sp][i];
   B.orig[lp ^ 1][p] = B.orig[lp][i];
+  B.invperm[i] = p;
   const size_t n = (size_t)P.n;
   for (int w = 0; w < 4; ++w) B.whist[lp ^ 1][w * n + p] = B.whist[lp][w * n + i];
+}
+
+// 5b. bond slots follow their disc; partners are renamed to the new order
+template <class T>
+__global__ void bond_gather_kernel(Params<T> P, Bufs<T> B) {
+  Ctl* ctl = B.ctl;
+  if (!ctl->rebuild_pending || P.BMAX == 0) return;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.n) return;
+  const int lp = ctl->lp;
+  const int i = B.perm[p];
+  const size_t n = (size_t)P.n;
+  const int bc = B.bcnt[lp][i];
+  B.bcnt[lp ^ 1][p] = bc;
+  B.bpinv[lp ^ 1][p] = B.bpinv[lp][i];
+  for (int s = 0; s < bc; ++s) {
+    const size_t ko = (size_t)s * n + i, kn = (size_t)s * n + p;
+    const unsigned w = B.bpart[lp][ko];
+    const int jo = (int)(w & kBondIdx);
+    const int jn = B.invperm[jo];
+    B.bpart[lp ^ 1][kn] = (w & ~kBondIdx) | (unsigned)jn;
+    B.bref[lp ^ 1][kn] = B.bref[lp][ko];
+    B.bstr[lp ^ 1][kn] = B.bstr[lp][ko];
+    // the shear displacement is kept in the orientation of the pair's lower
+    // sorted index: flip it when the re-sort swapped the pair's sides
+    const V2<T> u = B.bus[lp][ko];
+    B.bus[lp ^ 1][kn] = ((i < jo) != (p < jn)) ? V2<T>{-u.x, -u.y} : u;
+    B.bfail[lp ^ 1][kn] = B.bfail[lp][ko];
+  }
 }
 
 // 6. candidate partners: the 3x3 cells around each particle, fixed order
@@ -714,6 +1032,8 @@ __global__ void build_nbr_kernel(Params<T> P, Bufs<T> B) {
   const int c = lane_to_cell(a.w);
   const int cx = c & 0xFFFF, cy = c >> 16;
   const size_t n = (size_t)P.n;
+  // bonded partners are handled through their bond slot (intact or broken)
+  const int bc = P.BMAX > 0 ? B.bcnt[lp1][p] : 0;
   int cnt = 0;
   for (int dy = -1; dy <= 1; ++dy) {
     const int y = cy + dy;
@@ -726,6 +1046,10 @@ __global__ void build_nbr_kernel(Params<T> P, Bufs<T> B) {
       const int num = B.cell_count[key];
       for (int q = start; q < start + num; ++q) {
         if (q == p) continue;
+        bool bonded = false;
+        for (int t = 0; t < bc; ++t)
+          if ((int)(B.bpart[lp1][(size_t)t * n + p] & kBondIdx) == q) bonded = true;
+        if (bonded) continue;
         const V4<T> b = pos[q];
         const T ddx = fma((T)dx, P.cell, b.x - a.x);
         const T ddy = fma((T)dy, P.cell, b.y - a.y);
@@ -828,14 +1152,17 @@ __global__ void pack_kernel(Params<T> P, Bufs<T> B, const double* pos, const dou
   const int cx = (int)fmin(fmax(fx, 0.0), (double)(P.ncx - 1));
   const int cy = (int)fmin(fmax(fy, 0.0), (double)(P.ncy - 1));
   const double r = radius[i], m = mass[i];
+  const bool clamped = isinf(m) && m > 0.0;  // infinite mass: a clamped disc
   B.pos[sp][i] = V4<T>{(T)(x - cx * c), (T)(y - cy * c), (T)r, cell_to_lane(cx | (cy << 16), T(0))};
-  B.vel[sp][i] = V4<T>{(T)vel[2 * i], (T)vel[2 * i + 1], (T)omega[i], (T)(1.0 / m)};
+  B.vel[sp][i] = clamped ? V4<T>{T(0), T(0), T(0), T(0)}
+                         : V4<T>{(T)vel[2 * i], (T)vel[2 * i + 1], (T)omega[i], (T)(1.0 / m)};
+  if (B.bcnt[lp]) B.bcnt[lp][i] = 0;
   B.head[lp][i] = make_uint4(0u, 0u, 0u, 0u);
   B.orig[lp][i] = i;
   for (int w = 0; w < 4; ++w) B.whist[lp][(size_t)w * P.n + i] = V2<T>{T(0), T(0)};
   // the engine models I = kappa m r^2 with one kappa
   const double want = m * r * r / (double)P.kinv;
-  if (!(fabs(inertia[i] - want) <= 1e-6 * fabs(want))) atomicOr(&ctl->status, (int)kStatusInertia);
+  if (!clamped && !(fabs(inertia[i] - want) <= 1e-6 * fabs(want))) atomicOr(&ctl->status, (int)kStatusInertia);
 }
 
 template <class T>
@@ -942,6 +1269,9 @@ struct EngineBase {
   virtual int read_pairs(int* out, long long capacity, long long* count, cudaStream_t s) = 0;
   virtual int use_graph(int on) = 0;
   virtual int set_variant(int v) = 0;
+  virtual int set_bonds(const int* pairs, const double* strength, long long count, cudaStream_t s) = 0;
+  virtual int read_bonds(int* pairs, int* state, long long capacity, long long* count, cudaStream_t s) = 0;
+  virtual int read_load(double* out, long long capacity, long long* count, cudaStream_t s) = 0;
   virtual int step_kernel(cudaStream_t s) = 0;
   virtual int rebuild_pending(cudaStream_t s) = 0;
   virtual int get_variant() const = 0;
@@ -985,6 +1315,82 @@ void make_params(const tdem_hm_config& c, int slots, Params<T>& P) {
   P.gy = (T)c.gravity[1];
   P.kinv = (T)(1.0 / c.inertia_factor);
   P.rebuild_disp = (float)(0.5 * c.skin * 0.98);
+  P.BMAX = c.max_bonds;
+  P.kn = (T)c.bond_kn;
+  P.ks = (T)c.bond_ks;
+  P.bzeta = (T)c.bond_damping;
+  P.eps_t = c.breaking_strain;
+  P.eps_s = c.shear_breaking_strain;
+  P.ind_x0 = c.indenter_center[0];
+  P.ind_y0 = c.indenter_center[1];
+  P.ind_vx = c.indenter_velocity[0];
+  P.ind_vy = c.indenter_velocity[1];
+  P.irad = (T)c.indenter_radius;
+  P.load_cap = c.indenter_radius > 0.0 ? std::max(c.load_capacity, 0) : 0;
+}
+
+// Bond slots from per-disc lists in original order (partner original id per
+// slot, -1 for none): partners renamed to sorted indices, reference vectors
+// from the current positions, and each disc's constant covariance pseudo-inverse.
+template <class T>
+__global__ void sorted_of_orig_kernel(Params<T> P, Bufs<T> B, int* out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < P.n) out[B.orig[B.ctl->lp][p]] = p;
+}
+
+template <class T>
+__global__ void bond_init_kernel(Params<T> P, Bufs<T> B, const int* part_orig, const float* strength,
+                                 const int* sorted_of_orig) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.n) return;
+  const int sp = B.ctl->sp, lp = B.ctl->lp;
+  const size_t n = (size_t)P.n;
+  const int o = B.orig[lp][p];
+  const V4<T> a = B.pos[sp][p];
+  int bc = 0;
+  T c00 = 0, c01 = 0, c11 = 0;
+  for (int s = 0; s < P.BMAX; ++s) {
+    const int qo = part_orig[(size_t)s * n + o];
+    if (qo < 0) break;
+    const int q = sorted_of_orig[qo];
+    const V2<T> r = cell_delta<T>(P, a, B.pos[sp][q]);
+    const size_t k = (size_t)s * n + p;
+    B.bpart[lp][k] = (unsigned)q;
+    B.bref[lp][k] = r;
+    B.bstr[lp][k] = (T)strength[(size_t)s * n + o];
+    B.bus[lp][k] = V2<T>{T(0), T(0)};
+    B.bfail[lp][k] = -1;
+    c00 += r.x * r.x;
+    c01 += r.x * r.y;
+    c11 += r.y * r.y;
+    ++bc;
+  }
+  B.bcnt[lp][p] = bc;
+  B.bpinv[lp][p] = pinv_sym2_dev<T>(c00, c01, c11);
+}
+
+// Bond states as original ids (lo, hi), read from the pair's lower sorted index.
+template <class T>
+__global__ void bonds_out_kernel(Params<T> P, Bufs<T> B, int* pairs, int* state, long long capacity,
+                                 unsigned long long* count) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P.n) return;
+  const int lp = B.ctl->lp;
+  const size_t n = (size_t)P.n;
+  const int bc = B.bcnt[lp][p];
+  for (int s = 0; s < bc; ++s) {
+    const size_t k = (size_t)s * n + p;
+    const unsigned w = B.bpart[lp][k];
+    const int q = (int)(w & kBondIdx);
+    if (p >= q) continue;
+    const unsigned long long e = atomicAdd(count, 1ull);
+    if ((long long)e >= capacity) continue;
+    const int a = B.orig[lp][p], b = B.orig[lp][q];
+    pairs[2 * e] = min(a, b);
+    pairs[2 * e + 1] = max(a, b);
+    state[2 * e] = (w & kBondBroken) ? (int)((w >> kBondModeShift) & 3u) : 0;  // 0 intact, else mode
+    state[2 * e + 1] = B.bfail[lp][k];
+  }
 }
 
 // The rebuild pipeline (every kernel a no-op unless ctl->rebuild_pending).
@@ -1000,6 +1406,7 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
   scatter_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
   cellsort_kernel<T><<<nk, kThreads, 0, s>>>(P, B);
   gather_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
+  bond_gather_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
   build_nbr_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
   link_kernel<T><<<nb, kThreads, 0, s>>>(P, B);
   clear_keys_kernel<T><<<nk, kThreads, 0, s>>>(P, B);
@@ -1021,26 +1428,33 @@ struct StepKernel {
 template <class T>
 using StepFn = void (*)(Params<T>, Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int);
 
-template <class T>
-StepFn<T> step_fn(int variant, int mode) {
+template <class T, bool F>
+StepFn<T> step_fn_feat(int variant, int mode) {
   if (mode == kPrime) {
     switch (variant) {
-      case 1: return &force_kernel_pf<T, kPrime, 256, 3>;
-      case 2: return &force_kernel_pf<T, kPrime, 128, 6>;
-      case 3: return &force_kernel_pf<T, kPrime, 256, 2>;
-      case 4: return &force_kernel_bulk<T, kPrime, 256, 3>;
-      case 5: return &force_kernel_bulk<T, kPrime, 128, 6>;
-      default: return &force_kernel<T, kPrime>;
+      case 1: return &force_kernel_pf<T, kPrime, 256, 3, F>;
+      case 2: return &force_kernel_pf<T, kPrime, 128, 6, F>;
+      case 3: return &force_kernel_pf<T, kPrime, 256, 2, F>;
+      case 4: return &force_kernel_bulk<T, kPrime, 256, 3, F>;
+      case 5: return &force_kernel_bulk<T, kPrime, 128, 6, F>;
+      default: return &force_kernel<T, kPrime, F>;
     }
   }
   switch (variant) {
-    case 1: return &force_kernel_pf<T, kStep, 256, 3>;
-    case 2: return &force_kernel_pf<T, kStep, 128, 6>;
-    case 3: return &force_kernel_pf<T, kStep, 256, 2>;
-    case 4: return &force_kernel_bulk<T, kStep, 256, 3>;
-    case 5: return &force_kernel_bulk<T, kStep, 128, 6>;
-    default: return &force_kernel<T, kStep>;
+    case 1: return &force_kernel_pf<T, kStep, 256, 3, F>;
+    case 2: return &force_kernel_pf<T, kStep, 128, 6, F>;
+    case 3: return &force_kernel_pf<T, kStep, 256, 2, F>;
+    case 4: return &force_kernel_bulk<T, kStep, 256, 3, F>;
+    case 5: return &force_kernel_bulk<T, kStep, 128, 6, F>;
+    default: return &force_kernel<T, kStep, F>;
   }
+}
+
+// FEAT kernels carry the bonded-particle model and the indenter; the plain
+// granular kernels compile without them (fewer registers).
+template <class T>
+StepFn<T> step_fn(int variant, int mode, bool feat) {
+  return feat ? step_fn_feat<T, true>(variant, mode) : step_fn_feat<T, false>(variant, mode);
 }
 
 inline int variant_block(int variant) { return (variant == 2 || variant == 5) ? 128 : 256; }
@@ -1075,6 +1489,7 @@ struct Engine final : EngineBase {
   Ctl* host_ctl = nullptr;        // pinned mirror
   double* host_part = nullptr;    // pinned peek partials
   double* host_diss = nullptr;    // pinned committed partials
+  double* host_frac = nullptr;    // pinned committed fracture partials
 
   ~Engine() override {
     destroy_graphs();
@@ -1084,6 +1499,7 @@ struct Engine final : EngineBase {
     cudaFreeHost(host_ctl);
     cudaFreeHost(host_part);
     cudaFreeHost(host_diss);
+    cudaFreeHost(host_frac);
   }
 
   void destroy_graphs() {
@@ -1120,7 +1536,7 @@ struct Engine final : EngineBase {
       int per_sm = 0;
       const int bs = variant_block(v);
       TDEM_CUDA_TRY(&err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, reinterpret_cast<const void*>(step_fn<T>(v, kStep)), bs, 0));
+                              &per_sm, reinterpret_cast<const void*>(step_fn<T>(v, kStep, feat())), bs, 0));
       const int need = (int)((n + bs - 1) / bs);
       vgrid[v] = std::max(1, std::min(need, per_sm * sms));
       nwarp_slots = std::max(nwarp_slots, vgrid[v] * (bs / 32));
@@ -1137,19 +1553,32 @@ struct Engine final : EngineBase {
         (rc = alloc(&B.cell_fill, (size_t)P.nkeys)) || (rc = alloc(&B.perm, n)) ||
         (rc = alloc(&B.block_sums, (size_t)scan_blocks)) || (rc = alloc(&B.tmp_cell, n)) ||
         (rc = alloc(&B.tmp_off, n)) || (rc = alloc(&B.diss_part, (size_t)nwarp_slots)) ||
-        (rc = alloc(&B.peek_part, (size_t)nblocks * 8)) || (rc = alloc(&B.peek_vel, n)) ||
-        (rc = alloc(&B.peek_force, n)) || (rc = alloc(&B.ctl, 1)))
+        (rc = alloc(&B.peek_part, (size_t)nblocks * 12)) || (rc = alloc(&B.peek_vel, n)) ||
+        (rc = alloc(&B.peek_force, n)) || (rc = alloc(&B.ctl, 1)) || (rc = alloc(&B.invperm, n)) ||
+        (rc = alloc(&B.frac_part, (size_t)nwarp_slots)) || (rc = alloc(&B.ind_part, 3 * (size_t)nwarp_slots)) ||
+        (rc = alloc(&B.load, 2 * (size_t)std::max(P.load_cap, 1))))
       return rc;
+    if (P.BMAX > 0) {
+      const size_t BS = (size_t)P.BMAX * n;
+      for (int b = 0; b < 2; ++b)
+        if ((rc = alloc(&B.bpart[b], BS)) || (rc = alloc(&B.bref[b], BS)) || (rc = alloc(&B.bstr[b], BS)) ||
+            (rc = alloc(&B.bus[b], BS)) || (rc = alloc(&B.bfail[b], BS)) || (rc = alloc(&B.bcnt[b], n)) ||
+            (rc = alloc(&B.bpinv[b], n)))
+          return rc;
+      if ((rc = alloc(&B.strain, n))) return rc;
+    }
     stage_elems = 8 * n;
     if ((rc = alloc(&stage, stage_elems))) return rc;
     TDEM_CUDA_TRY(&err, cudaMallocHost(&host_stage, stage_elems * sizeof(double)));
     TDEM_CUDA_TRY(&err, cudaMallocHost(&host_ctl, sizeof(Ctl)));
-    TDEM_CUDA_TRY(&err, cudaMallocHost(&host_part, (size_t)nblocks * 8 * sizeof(double)));
+    TDEM_CUDA_TRY(&err, cudaMallocHost(&host_part, (size_t)nblocks * 12 * sizeof(double)));
+    TDEM_CUDA_TRY(&err, cudaMallocHost(&host_frac, (size_t)nwarp_slots * sizeof(double)));
     TDEM_CUDA_TRY(&err, cudaMallocHost(&host_diss, (size_t)nwarp_slots * sizeof(double)));
     TDEM_CUDA_TRY(&err, cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
     return TDEM_OK;
   }
 
+  bool feat() const { return P.BMAX > 0 || P.irad > T(0); }
   dim3 grid_n() const { return dim3((unsigned)nblocks); }
   dim3 grid_keys() const { return dim3((unsigned)((P.nkeys + kThreads - 1) / kThreads)); }
 
@@ -1182,6 +1611,7 @@ struct Engine final : EngineBase {
     zero.rebuild_pending = 1;
     TDEM_CUDA_TRY(&err, cudaMemcpyAsync(B.ctl, &zero, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     TDEM_CUDA_TRY(&err, cudaMemsetAsync(B.diss_part, 0, (size_t)nwarp_slots * sizeof(double), s));
+    TDEM_CUDA_TRY(&err, cudaMemsetAsync(B.frac_part, 0, (size_t)nwarp_slots * sizeof(double), s));
     pack_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, d[0], d[1], d[2], d[3], d[4], d[5]);
     launch_rebuild(s);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
@@ -1198,11 +1628,23 @@ struct Engine final : EngineBase {
     int prim = 1;
     void* args[] = {&P, &B, &h, &hl, &cond_bits, &prim};
     cudaKernelNodeParams kp = {};
-    kp.func = reinterpret_cast<void*>(step_fn<T>(variant, kStep));
+    kp.func = reinterpret_cast<void*>(step_fn<T>(variant, kStep, feat()));
     kp.gridDim = dim3((unsigned)vgrid[variant]);
     kp.blockDim = dim3((unsigned)variant_block(variant));
     kp.sharedMemBytes = 0;
     kp.kernelParams = args;
+    cudaGraphNode_t snode;
+    if (P.BMAX > 0) {
+      void* sargs[] = {&P, &B};
+      cudaKernelNodeParams sk = {};
+      sk.func = reinterpret_cast<void*>(&strain_kernel<T>);
+      sk.gridDim = grid_n();
+      sk.blockDim = dim3(kThreads);
+      sk.kernelParams = sargs;
+      TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&snode, g, dep, ndep, &sk));
+      dep = &snode;
+      ndep = 1;
+    }
     cudaGraphNode_t knode;
     TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&knode, g, dep, ndep, &kp));
     cudaGraphNodeParams ip = {};
@@ -1270,8 +1712,13 @@ struct Engine final : EngineBase {
     return TDEM_OK;
   }
 
+  void launch_strain(cudaStream_t s) {
+    if (P.BMAX > 0) strain_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
+  }
+
   int prime(cudaStream_t s) {
-    step_fn<T>(variant, kPrime)<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
+    launch_strain(s);
+    step_fn<T>(variant, kPrime, feat())<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
     launch_rebuild(s);  // runs only if the prime step tripped the trigger
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     primed = true;
@@ -1307,7 +1754,8 @@ struct Engine final : EngineBase {
       return TDEM_OK;
     }
     for (long long k = 0; k < n; ++k) {
-      step_fn<T>(variant, kStep)<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
+      launch_strain(s);
+      step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
       launch_rebuild(s);
     }
     TDEM_CUDA_TRY(&err, cudaGetLastError());
@@ -1315,7 +1763,11 @@ struct Engine final : EngineBase {
   }
 
   int peek(cudaStream_t s) {
-    force_kernel<T, kPeek><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, primed ? 1 : 0);
+    launch_strain(s);
+    if (feat())
+      force_kernel<T, kPeek, true><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, primed ? 1 : 0);
+    else
+      force_kernel<T, kPeek, false><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, primed ? 1 : 0);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     return TDEM_OK;
   }
@@ -1348,7 +1800,9 @@ struct Engine final : EngineBase {
     if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "read before set_state");
     int rc = peek(s);
     if (rc) return rc;
-    TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_part, B.peek_part, (size_t)nblocks * 8 * sizeof(double),
+    TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_part, B.peek_part, (size_t)nblocks * 12 * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s));
+    TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_frac, B.frac_part, (size_t)nwarp_slots * sizeof(double),
                                         cudaMemcpyDeviceToHost, s));
     const int nwarps = nwarp_slots;
     TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_diss, B.diss_part, (size_t)nwarps * sizeof(double),
@@ -1367,10 +1821,17 @@ struct Engine final : EngineBase {
       }
       return sum + comp;
     };
-    for (int k = 0; k < 5; ++k) v[k] = csum([&](int b) { return host_part[(size_t)b * 8 + k]; }, nblocks);
-    v[TDEM_HM_L_DISSIPATED] = csum([&](int b) { return host_diss[b]; }, nwarps) + v[4];
-    v[4] = v[TDEM_HM_L_KINETIC] + v[TDEM_HM_L_POTENTIAL] + v[TDEM_HM_L_HERTZ] + v[TDEM_HM_L_TANGENTIAL] +
-           v[TDEM_HM_L_DISSIPATED];
+    double part[9];
+    for (int k = 0; k < 9; ++k) part[k] = csum([&](int b) { return host_part[(size_t)b * 12 + k]; }, nblocks);
+    for (int k = 0; k < 4; ++k) v[k] = part[k];
+    v[TDEM_HM_L_DISSIPATED] = csum([&](int b) { return host_diss[b]; }, nwarps) + part[4];
+    v[TDEM_HM_L_BOND_ELASTIC] = part[5];
+    v[TDEM_HM_L_FRACTURE] = csum([&](int b) { return host_frac[b]; }, nwarps) + part[6];
+    v[TDEM_HM_L_TOOL_WORK] = host_ctl->tool_work + (primed ? part[7] : 0.0);
+    v[TDEM_HM_L_BROKEN] = (double)host_ctl->broken + part[8];
+    v[TDEM_HM_L_TOTAL] = v[TDEM_HM_L_KINETIC] + v[TDEM_HM_L_POTENTIAL] + v[TDEM_HM_L_HERTZ] +
+                         v[TDEM_HM_L_TANGENTIAL] + v[TDEM_HM_L_DISSIPATED] + v[TDEM_HM_L_BOND_ELASTIC] +
+                         v[TDEM_HM_L_FRACTURE] - v[TDEM_HM_L_TOOL_WORK];
     v[TDEM_HM_L_EVALS] = (double)host_ctl->evals;
     v[TDEM_HM_L_REBUILDS] = (double)host_ctl->rebuilds;
     v[TDEM_HM_L_MAX_NEIGHBORS] = (double)host_ctl->max_cnt;
@@ -1423,7 +1884,8 @@ struct Engine final : EngineBase {
   int step_kernel(cudaStream_t s) override {
     if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "step before set_state");
     if (!primed) return prime(s);
-    step_fn<T>(variant, kStep)<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
+    launch_strain(s);
+    step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     return TDEM_OK;
   }
@@ -1432,6 +1894,89 @@ struct Engine final : EngineBase {
     TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_ctl, B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
     return host_ctl->rebuild_pending ? 1 : 0;
+  }
+
+  int set_bonds(const int* pairs, const double* strength, long long count, cudaStream_t s) override {
+    if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "set_bonds before set_state");
+    if (P.BMAX <= 0) return tdem::fail(&err, TDEM_ERR_BADARG, "engine created with max_bonds = 0");
+    if (primed) return tdem::fail(&err, TDEM_ERR_STATE, "set_bonds must follow set_state, before stepping");
+    const size_t n = (size_t)P.n;
+    std::vector<int> part((size_t)P.BMAX * n, -1);
+    std::vector<float> str((size_t)P.BMAX * n, 1.0f);
+    std::vector<int> fill(n, 0);
+    for (long long b = 0; b < count; ++b) {
+      const int a = pairs[2 * b], c = pairs[2 * b + 1];
+      if (a < 0 || c < 0 || a >= P.n || c >= P.n || a == c)
+        return tdem::fail(&err, TDEM_ERR_BADARG, "bond " + std::to_string(b) + " has an invalid disc index");
+      if (!(strength[b] > 0.0)) return tdem::fail(&err, TDEM_ERR_BADARG, "bond strength factors must be positive");
+      for (int e : {a, c}) {
+        const int o = e == a ? c : a;
+        if (fill[e] >= P.BMAX)
+          return tdem::fail(&err, TDEM_ERR_BADARG,
+                            "disc " + std::to_string(e) + " has more than max_bonds = " + std::to_string(P.BMAX) +
+                                " bonds");
+        part[(size_t)fill[e] * n + e] = o;
+        str[(size_t)fill[e] * n + e] = (float)strength[b];
+        ++fill[e];
+      }
+    }
+    int* dpart = nullptr;
+    float* dstr = nullptr;
+    TDEM_CUDA_TRY(&err, cudaMalloc(&dpart, part.size() * sizeof(int)));
+    TDEM_CUDA_TRY(&err, cudaMalloc(&dstr, str.size() * sizeof(float)));
+    cudaMemcpyAsync(dpart, part.data(), part.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dstr, str.data(), str.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    sorted_of_orig_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, B.invperm);
+    bond_init_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, dpart, dstr, B.invperm);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    cudaFree(dpart);
+    cudaFree(dstr);
+    TDEM_CUDA_TRY(&err, e);
+    TDEM_CUDA_TRY(&err, cudaGetLastError());
+    // bonded pairs leave the contact candidates: rebuild the list now
+    request_rebuild_kernel<<<1, 1, 0, s>>>(B.ctl);
+    launch_rebuild(s);
+    TDEM_CUDA_TRY(&err, cudaGetLastError());
+    return TDEM_OK;
+  }
+
+  int read_bonds(int* pairs, int* state, long long capacity, long long* count, cudaStream_t s) override {
+    if (P.BMAX <= 0) {
+      *count = 0;
+      return TDEM_OK;
+    }
+    unsigned long long* dcount = nullptr;
+    int *dpairs = nullptr, *dstate = nullptr;
+    const size_t cap = (size_t)std::max<long long>(1, capacity);
+    TDEM_CUDA_TRY(&err, cudaMalloc(&dcount, sizeof(unsigned long long)));
+    TDEM_CUDA_TRY(&err, cudaMalloc(&dpairs, cap * 2 * sizeof(int)));
+    TDEM_CUDA_TRY(&err, cudaMalloc(&dstate, cap * 2 * sizeof(int)));
+    cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), s);
+    bonds_out_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, dpairs, dstate, capacity, dcount);
+    unsigned long long c = 0;
+    cudaMemcpyAsync(&c, dcount, sizeof(c), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const size_t m = (size_t)std::min<long long>((long long)c, capacity);
+    if (m) {
+      cudaMemcpy(pairs, dpairs, m * 2 * sizeof(int), cudaMemcpyDeviceToHost);
+      cudaMemcpy(state, dstate, m * 2 * sizeof(int), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dcount);
+    cudaFree(dpairs);
+    cudaFree(dstate);
+    *count = (long long)c;
+    TDEM_CUDA_TRY(&err, cudaGetLastError());
+    return TDEM_OK;
+  }
+
+  int read_load(double* out, long long capacity, long long* count, cudaStream_t s) override {
+    TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_ctl, B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
+    const long long have = std::min<long long>(host_ctl->evals, (long long)P.load_cap);
+    const long long m = std::min(have, capacity);
+    if (m > 0) TDEM_CUDA_TRY(&err, cudaMemcpy(out, B.load, (size_t)m * 2 * sizeof(double), cudaMemcpyDeviceToHost));
+    *count = have;
+    return TDEM_OK;
   }
 
   int set_variant(int v) override {
@@ -1529,6 +2074,12 @@ int tdem_hm_create(const tdem_hm_config* c, tdem_hm** out) {
   if (c->max_neighbors < 1 || c->max_neighbors > kMaxSlots)
     return tdem::fail(err, TDEM_ERR_BADARG, "max_neighbors must be in 1..24");
   if (!(c->inertia_factor > 0.0)) return tdem::fail(err, TDEM_ERR_BADARG, "inertia_factor must be positive");
+  if (c->max_bonds < 0 || c->max_bonds > kMaxBondSlots)
+    return tdem::fail(err, TDEM_ERR_BADARG, "max_bonds must be in 0..8");
+  if (c->max_bonds > 0 && (!(c->bond_kn > 0) || !(c->bond_ks >= 0) || !(c->bond_damping >= 0) ||
+                           !(c->breaking_strain > 0) || !(c->shear_breaking_strain > 0)))
+    return tdem::fail(err, TDEM_ERR_BADARG, "invalid bond stiffness, damping or break strain");
+  if (!(c->indenter_radius >= 0)) return tdem::fail(err, TDEM_ERR_BADARG, "indenter_radius must be >= 0");
   if (c->ncx < 1 || c->ncy < 1 || c->ncx > 32768 || c->ncy > 32768)
     return tdem::fail(err, TDEM_ERR_BADARG, "cell grid must be 1..32768 per axis");
   if (!(c->cell > 0) || !(c->skin >= 0) || !(c->dt > 0) || !(c->young > 0) || !(c->poisson > -1.0) ||
@@ -1604,6 +2155,28 @@ int tdem_hm_read_history(tdem_hm* h, int32_t* pairs, double* xi, int64_t capacit
   if (!h || !pairs || !xi || !count) return TDEM_ERR_BADARG;
   long long c = 0;
   const int rc = h->e->read_history(pairs, xi, (long long)capacity, &c, reinterpret_cast<cudaStream_t>(stream));
+  *count = (int64_t)c;
+  return rc;
+}
+
+int tdem_hm_set_bonds(tdem_hm* h, const int32_t* pairs, const double* strength, int64_t count, void* stream) {
+  if (!h || (count > 0 && (!pairs || !strength)) || count < 0) return TDEM_ERR_BADARG;
+  return h->e->set_bonds(pairs, strength, (long long)count, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int tdem_hm_read_bonds(tdem_hm* h, int32_t* pairs, int32_t* state, int64_t capacity, int64_t* count,
+                       void* stream) {
+  if (!h || !pairs || !state || !count) return TDEM_ERR_BADARG;
+  long long c = 0;
+  const int rc = h->e->read_bonds(pairs, state, (long long)capacity, &c, reinterpret_cast<cudaStream_t>(stream));
+  *count = (int64_t)c;
+  return rc;
+}
+
+int tdem_hm_read_load(tdem_hm* h, double* out, int64_t capacity, int64_t* count, void* stream) {
+  if (!h || !out || !count) return TDEM_ERR_BADARG;
+  long long c = 0;
+  const int rc = h->e->read_load(out, (long long)capacity, &c, reinterpret_cast<cudaStream_t>(stream));
   *count = (int64_t)c;
   return rc;
 }
@@ -1734,6 +2307,9 @@ int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos,
     return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG, "invalid cell grid or material");
   Params<float> P{};
   make_params<float>(*cfg, kNoAllocSlots, P);
+  P.BMAX = 0;  // contacts, walls and gravity only: no bond slots live in the scratch
+  P.irad = 0.0f;
+  P.load_cap = 0;
   if (P.nkeys > kNoAllocMaxKeys)
     return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG,
                         "the allocation-free path holds cell grids up to 256 x 256 cells; this grid is %lld x %lld",
@@ -1778,9 +2354,10 @@ int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos,
   B.tmp_cell = c.take<int>(n);
   B.tmp_off = c.take<V2<float>>(n);
   B.diss_part = c.take<double>((size_t)nb * (kThreads / 32));
-  B.peek_part = c.take<double>((size_t)nb * 8);
+  B.peek_part = c.take<double>((size_t)nb * 12);
   B.peek_vel = c.take<V4<float>>(n);
   B.peek_force = c.take<V4<float>>(n);
+  B.invperm = c.take<int>(n);
   B.ctl = c.take<Ctl>(1);
   int* status_dev = c.take<int>(1);
   if (c.off > c.cap)
@@ -1792,7 +2369,7 @@ int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos,
                                                                                B.cell_fill, P.nkeys);
   pack_kernel<float><<<nb, kThreads, 0, s>>>(P, B, pos, vel, omega, radius, mass, inertia);
   launch_rebuild_seq<float>(P, B, s);
-  force_kernel<float, kPeek><<<nb, kThreads, 0, s>>>(P, B, 0, 0, 0, 0);
+  force_kernel<float, kPeek, false><<<nb, kThreads, 0, s>>>(P, B, 0, 0, 0, 0);
   unpack_kernel<float><<<nb, kThreads, 0, s>>>(P, B, nullptr, nullptr, nullptr, out_force, out_torque);
   noalloc_status_kernel<<<1, 1, 0, s>>>(B.ctl, status_dev);
   cudaError_t e = cudaGetLastError();

@@ -19,7 +19,17 @@
 //               arithmetic on the same operands, so the copies stay identical
 //   orig[2][N]  int original particle id
 //   whist[2][4N] V2 wall tangential history (4 walls)
-// head / nbr / hist / orig / whist swap at a rebuild. Position =
+//   bond slots (bonded sheets only), slot-major [BMAX*N], swapped at a rebuild:
+//   bpart       uint32 partner sorted index (bits 0..28), failure mode
+//               (bits 29..30: 1 tensile, 2 shear, 3 both) and broken (bit 31)
+//   bref        V2 reference bond vector x0(partner) - x0(self)
+//   bstr        T  strength factor of the bond (scales both break strains)
+//   bus         V2 shear displacement of the bond, in the orientation of the
+//               pair's lower sorted index (one copy per side, kept identical)
+//   bfail       int evaluation index at which the bond broke (-1: intact)
+//   bcnt[N]     int initial bonds of the disc; bpinv[N] V4 constant
+//               pseudo-inverse of the disc's bond covariance (row major)
+// head / nbr / hist / orig / whist / bond slots swap at a rebuild. Position =
 // (cx * cell + x offset, cy * cell + y offset): FP32 offsets from an integer
 // cell origin keep contact geometry exact to ~ulp(cell) anywhere in a large
 // box. The moment of inertia is kappa m r^2 with one kappa per engine.
@@ -68,7 +78,21 @@ struct Params {
   T gx, gy;       // gravity (acceleration)
   T kinv;         // 1 / kappa, with I = kappa m r^2
   float rebuild_disp;  // rebuild once the displacement bound exceeds this
+  // bonded-particle model (BMAX == 0: no bonds)
+  int BMAX;
+  T kn, ks;       // bond normal and shear stiffness (N/m)
+  T bzeta;        // bond damping ratio: c = 2 zeta sqrt(k m*)
+  double eps_t, eps_s;  // tensile and objective-shear break strains
+  // rigid circular indenter (irad == 0: none), Hertz normal + dashpot
+  double ind_x0, ind_y0, ind_vx, ind_vy;
+  T irad;
+  int load_cap;   // capacity of the per-evaluation indenter load record
 };
+
+constexpr unsigned kBondIdx = (1u << 29) - 1u;
+constexpr unsigned kBondBroken = 1u << 31;
+constexpr int kBondModeShift = 29;
+constexpr int kMaxBondSlots = 8;
 
 // Device control block: buffer parities, the rebuild trigger and status.
 struct Ctl {
@@ -84,6 +108,10 @@ struct Ctl {
   int pad;
   long long evals;         // force evaluations committed (prime + steps)
   long long target;        // stop the step loop at this many evaluations
+  double tool_work;        // work done by the indenter on the discs (J)
+  double reaction_x, reaction_y;  // ice-on-indenter force of the last evaluation
+  unsigned load_entries;   // entries in the per-evaluation indenter list
+  int broken;              // bonds broken so far
 };
 
 template <class T>
@@ -109,6 +137,21 @@ struct Bufs {
   V4<T>* peek_vel;     // integer-time velocity (vx, vy, omega, -)
   V4<T>* peek_force;   // integer-time force (fx, fy, torque, -)
   Ctl* ctl;
+  // bonded-particle model
+  unsigned* bpart[2];
+  V2<T>* bref[2];
+  T* bstr[2];
+  V2<T>* bus[2];
+  int* bfail[2];
+  int* bcnt[2];
+  V4<T>* bpinv[2];
+  T* strain;           // per-disc objective shear invariant of this evaluation
+  int* invperm;        // rebuild: old sorted index -> new
+  double* frac_part;   // per step-kernel warp: fracture energy released (J)
+  double* peek_bond;   // per block: bond elastic energy (read-back)
+  // indenter: per-evaluation partial reactions (warp id, fx, fy) and the load record
+  double* ind_part;    // [3 * nwarp_slots]
+  double* load;        // [2 * load_cap]: reaction (x, y) per evaluation
 };
 
 // The cell id rides in the last lane of the position vector: bit-cast for

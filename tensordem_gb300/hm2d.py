@@ -51,6 +51,18 @@ class HM2DConfig:
     precision: int = 32
     max_neighbors: int = 16
     inertia_factor: float = 0.5
+    # bonded-particle model (max_bonds == 0: none)
+    max_bonds: int = 0
+    bond_kn: float = 0.0
+    bond_ks: float = 0.0
+    bond_damping: float = 0.0
+    breaking_strain: float = 0.01
+    shear_breaking_strain: float = 0.02
+    # rigid circular indenter (radius 0: none)
+    indenter_center: tuple[float, float] = (0.0, 0.0)
+    indenter_velocity: tuple[float, float] = (0.0, 0.0)
+    indenter_radius: float = 0.0
+    load_capacity: int = 0
 
     @property
     def box(self) -> tuple[float, float]:
@@ -66,6 +78,13 @@ class HM2DConfig:
         c.mu, c.mu_wall = self.mu, self.mu_wall
         c.gravity[0], c.gravity[1] = self.gravity
         c.inertia_factor = self.inertia_factor
+        c.max_bonds = self.max_bonds
+        c.bond_kn, c.bond_ks, c.bond_damping = self.bond_kn, self.bond_ks, self.bond_damping
+        c.breaking_strain, c.shear_breaking_strain = self.breaking_strain, self.shear_breaking_strain
+        c.indenter_center[0], c.indenter_center[1] = self.indenter_center
+        c.indenter_velocity[0], c.indenter_velocity[1] = self.indenter_velocity
+        c.indenter_radius = self.indenter_radius
+        c.load_capacity = self.load_capacity
         return c
 
 
@@ -232,7 +251,8 @@ class HM2D:
         v = list(buf)
         return dict(kinetic=v[0], potential=v[1], elastic_normal=v[2], elastic_tangential=v[3],
                     total=v[4], dissipated=v[5], evals=int(v[6]), rebuilds=int(v[7]),
-                    max_neighbors=int(v[8]), status=int(v[9]), graph=bool(v[10]), variant=int(v[11]))
+                    max_neighbors=int(v[8]), status=int(v[9]), graph=bool(v[10]), variant=int(v[11]),
+                    bond_elastic=v[12], fracture_released=v[13], tool_work=v[14], broken=int(v[15]))
 
     def pairs(self) -> np.ndarray:
         """Current candidate pairs (original ids, i < j), sorted, as an (M, 2) array."""
@@ -300,3 +320,111 @@ class HM2D:
         if r < 0:
             _lib.check(-r, self._h, "tdem_hm_rebuild_pending")
         return r == 1
+
+    def set_bonds(self, pairs, strength) -> None:
+        """Bonds (original ids, (B, 2)) with a strength factor each; after set_state."""
+        pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        st = np.ascontiguousarray(np.asarray(strength, dtype=np.float64).reshape(-1))
+        if len(st) != len(pr):
+            raise ValueError("one strength factor per bond")
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_set_bonds(self._h, pr.ctypes.data, st.ctypes.data, len(pr), self._stream())
+        _lib.check(rc, self._h, "tdem_hm_set_bonds")
+        self.check()
+
+    def bonds(self) -> dict[str, np.ndarray]:
+        """Bond states sorted by (lo, hi) original ids: mode (0 intact) and failure evaluation."""
+        cap = self.config.n * max(self.config.max_bonds, 1)
+        pairs = np.empty((cap, 2), dtype=np.int32)
+        state = np.empty((cap, 2), dtype=np.int32)
+        count = C.c_int64()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_read_bonds(self._h, pairs.ctypes.data, state.ctypes.data, cap,
+                                              C.byref(count), self._stream())
+        _lib.check(rc, self._h, "tdem_hm_read_bonds")
+        m = min(int(count.value), cap)
+        order = np.lexsort((pairs[:m, 1], pairs[:m, 0]))
+        return dict(pairs=pairs[:m][order].astype(np.int64), mode=state[:m, 0][order],
+                    fail_eval=state[:m, 1][order])
+
+    def load_curve(self) -> np.ndarray:
+        """Indenter reaction (ice on indenter) per committed evaluation, (E, 2)."""
+        cap = max(self.config.load_capacity, 1)
+        out = np.empty((cap, 2))
+        count = C.c_int64()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_read_load(self._h, out.ctypes.data, cap, C.byref(count), self._stream())
+        _lib.check(rc, self._h, "tdem_hm_read_load")
+        return out[:min(int(count.value), cap)].copy()
+
+
+def ice_sheet_case(nx: int = 2048, ny: int = 512, *, radius: float = 0.05, density: float = 900.0,
+                   young: float = 5e9, poisson: float = 0.3, mu: float = 0.3, restitution: float = 0.5,
+                   bond_damping: float = 0.05, breaking_strain: float = 0.01,
+                   shear_breaking_strain: float = 0.02, strength_sigma: float = 0.1, seed: int = 0,
+                   indenter_radius: float = 2.0, indenter_speed: float = 0.5, dt_factor: float = 0.1,
+                   skin_factor: float = 0.1, precision: int = 32, steps: int = 20000,
+                   max_neighbors: int = 8) -> tuple[HM2DConfig, dict, np.ndarray, np.ndarray]:
+    """Bonded ice sheet on a hexagonal lattice, clamped at both short ends.
+
+    nx discs per row, ny rows (row spacing sqrt(3) r, odd rows shifted by r),
+    thickness 2r, 6-neighbour bonds with normal stiffness E t and shear
+    stiffness E t / (2 (1 + nu)), per-bond strength factor lognormal(0, sigma)
+    (numpy PCG64 ``seed``) scaling the break strains 0.01 / 0.02. The left and
+    right end columns are clamped (infinite mass). A rigid circular indenter of
+    radius 2 m starts just above the sheet's mid-span and moves down at
+    0.5 m/s. Returns (config, state, bond pairs, strength factors).
+    """
+    rng = np.random.default_rng(seed)
+    r = radius
+    jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    x = (2.0 * ii + (jj % 2)) * r + 2.0 * r
+    y = jj * math.sqrt(3.0) * r + 2.0 * r
+    pos = np.stack((x.ravel(), y.ravel()), axis=1)
+    n = nx * ny
+    idx = (jj * nx + ii)
+    pairs = [np.stack((idx[:, :-1].ravel(), idx[:, 1:].ravel()), axis=1)]  # along rows
+    for parity in (0, 1):
+        rows = np.arange(parity, ny - 1, 2)
+        if parity == 0:   # even row j: partners (i-1, j+1) and (i, j+1)
+            a = idx[rows][:, 1:]
+            pairs += [np.stack((a.ravel(), idx[rows + 1][:, :-1].ravel()), axis=1),
+                      np.stack((idx[rows].ravel(), idx[rows + 1].ravel()), axis=1)]
+        else:             # odd row j: partners (i, j+1) and (i+1, j+1)
+            pairs += [np.stack((idx[rows].ravel(), idx[rows + 1].ravel()), axis=1),
+                      np.stack((idx[rows][:, :-1].ravel(), idx[rows + 1][:, 1:].ravel()), axis=1)]
+    bonds = np.concatenate(pairs).astype(np.int64)
+    bonds = np.sort(bonds, axis=1)
+    bonds = bonds[np.lexsort((bonds[:, 1], bonds[:, 0]))]
+    strength = np.exp(rng.normal(0.0, strength_sigma, len(bonds)))
+    thickness = 2.0 * r
+    mass = np.full(n, density * math.pi * r * r * thickness)
+    clamped = (ii.ravel() == 0) | (ii.ravel() == nx - 1)
+    mass[clamped] = np.inf
+    inertia = 0.5 * mass * r * r
+    radius_arr = np.full(n, r)
+    kn = young * thickness
+    ks = kn / (2.0 * (1.0 + poisson))
+    dt = dt_factor * rayleigh_dt(r, density, young, poisson)
+    skin = skin_factor * r
+    width = (2.0 * nx + 1) * r + 4.0 * r
+    top = (ny - 1) * math.sqrt(3.0) * r + 2.0 * r
+    travel = indenter_speed * dt * steps
+    height = top + r + 2.0 * indenter_radius + travel + 4.0 * r
+    reach = 2.0 * r + skin
+    ncx = int(math.floor(width / reach))
+    ncy = int(math.floor(height / reach))
+    cell = max(width / ncx, height / ncy)
+    ncx = int(math.ceil(width / cell))
+    ncy = int(math.ceil(height / cell))
+    center = (0.5 * (x.min() + x.max()), top + r + indenter_radius + 0.02 * r)
+    cfg = HM2DConfig(n=n, ncx=ncx, ncy=ncy, cell=cell, skin=skin, dt=dt, young=young, poisson=poisson,
+                     restitution=restitution, mu=mu, mu_wall=mu, gravity=(0.0, 0.0), walls=0,
+                     precision=precision, max_neighbors=max_neighbors, max_bonds=6, bond_kn=kn,
+                     bond_ks=ks, bond_damping=bond_damping, breaking_strain=breaking_strain,
+                     shear_breaking_strain=shear_breaking_strain, indenter_center=center,
+                     indenter_velocity=(0.0, -indenter_speed), indenter_radius=indenter_radius,
+                     load_capacity=steps + 8)
+    state = dict(pos=pos, vel=np.zeros((n, 2)), omega=np.zeros(n), radius=radius_arr, mass=mass,
+                 inertia=inertia)
+    return cfg, state, bonds, strength

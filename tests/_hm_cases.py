@@ -39,3 +39,25 @@ def two_disc_state(delta=1e-6, r=1e-3, rho=2500.0, v_t=0.0, omega=(0.0, 0.0)):
     inertia = 0.5 * mass * radius**2
     return dict(pos=pos, vel=vel, omega=np.array(omega, dtype=float), radius=radius, mass=mass,
                 inertia=inertia)
+
+
+def bonded_oracle_for(cfg, st, bonds, strength):
+    from oracle.hm2d import BondedHM2DOracle
+    p = HMParams(young=cfg.young, poisson=cfg.poisson, restitution=cfg.restitution, mu=cfg.mu,
+                 mu_wall=cfg.mu_wall, dt=cfg.dt, gravity=cfg.gravity,
+                 box=cfg.box if cfg.walls else None,
+                 walls=tuple(bool(cfg.walls & b) for b in (1, 2, 4, 8)), skin=cfg.skin)
+    ind = None
+    if cfg.indenter_radius > 0:
+        ind = dict(center=cfg.indenter_center, velocity=cfg.indenter_velocity, radius=cfg.indenter_radius)
+    return BondedHM2DOracle(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"], p,
+                            bonds=bonds, strength=strength, k_n=cfg.bond_kn, k_s=cfg.bond_ks,
+                            zeta=cfg.bond_damping, eps_t=cfg.breaking_strain,
+                            eps_s=cfg.shear_breaking_strain, indenter=ind)
+
+
+def small_sheet(nx=24, ny=8, *, precision=64, steps=400, speed=2.0, **kw):
+    """A small clamped hexagonal sheet with a fast indenter (cracks within a few hundred steps)."""
+    from tensordem_gb300.hm2d import ice_sheet_case
+    return ice_sheet_case(nx, ny, radius=0.05, indenter_radius=0.3, indenter_speed=speed,
+                          precision=precision, steps=steps, **kw)

@@ -1,0 +1,139 @@
+"""GPU parity of the bonded-particle model and the indenter (csrc/hm2d.cu)
+against the FP64 bonded oracle (oracle/hm2d.py, BondedHM2DOracle).
+
+Tolerances: FP64 engine - break set, modes and failure evaluations identical,
+state within 1e-9 normwise over 200 steps of cracking; FP32 engine - peak
+indenter load within 1% of the oracle's, ledger within 2% of the work input,
+break count within 10%.
+"""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from tests._hm_cases import bonded_oracle_for, small_sheet
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def hm():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA GPU required for -m gpu tests")
+    from tensordem_gb300 import hm2d
+    return hm2d
+
+
+def _engine(hm, cfg, st, bonds, strength):
+    e = hm.HM2D(cfg)
+    e.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
+    e.set_bonds(bonds, strength)
+    return e
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _oracle_bond_table(o):
+    order = np.lexsort((o.bj, o.bi))
+    return (np.stack((o.bi[order], o.bj[order]), axis=1), o.fail_mode[order].astype(np.int32),
+            o.fail_eval[order].astype(np.int32))
+
+
+def test_rigid_rotation_breaks_nothing_on_gpu(hm):
+    cfg, st, bonds, strength = small_sheet(8, 4, precision=64, speed=0.0)
+    cfg = type(cfg)(**{**cfg.__dict__, "indenter_radius": 0.0})
+    st = dict(st)
+    free = np.isfinite(st["mass"])
+    st["mass"] = np.where(free, st["mass"], st["mass"][free][0])
+    st["inertia"] = 0.5 * st["mass"] * st["radius"] ** 2
+    a = 0.5
+    rot = np.array([[math.cos(a), -math.sin(a)], [math.sin(a), math.cos(a)]])
+    c = st["pos"].mean(0)
+    # spin the undeformed sheet rigidly: no strain, no force, no break
+    st["vel"] = (st["pos"] - c) @ np.array([[0.0, 1.0], [-1.0, 0.0]]) * 0.0
+    e = _engine(hm, cfg, st, bonds, strength)
+    f = e.state()["force"].cpu().numpy()
+    assert np.abs(f).max() <= 1e-6
+    pos_rot = (st["pos"] - c) @ rot.T + c
+    st2 = dict(st, pos=pos_rot)
+    e2 = hm.HM2D(cfg)
+    e2.set_state(st2["pos"], st2["vel"], st2["omega"], st2["radius"], st2["mass"], st2["inertia"])
+    e2.set_bonds(bonds, strength)
+    e2.step(5)
+    assert (e2.bonds()["mode"] == 0).all()
+
+
+def test_fp64_bonded_sheet_matches_oracle(hm):
+    cfg, st, bonds, strength = small_sheet(24, 8, precision=64, steps=400, speed=20.0)
+    e = _engine(hm, cfg, st, bonds, strength)
+    o = bonded_oracle_for(cfg, st, bonds, strength)
+    table = None
+    for stop in (1, 100, 200):
+        e.step(stop - o.steps)
+        o.step(stop - 1 - o.steps)
+        # committed on the GPU: evaluations 0 .. stop-1 (the next one is only peeked)
+        table = _oracle_bond_table(o)
+        o.step(1)
+        s = e.state()
+        errs = (_rel(s["pos"].cpu().numpy(), o.pos), _rel(s["vel"].cpu().numpy(), o.vel))
+        print(f"fp64 bonded after {stop}: pos {errs[0]:.2e} vel {errs[1]:.2e}, broken {(~o.alive).sum()}")
+        assert errs[0] <= 1e-9 and errs[1] <= 1e-6, (stop, errs)
+    got = e.bonds()
+    pairs, mode, fail = table
+    assert np.array_equal(got["pairs"], pairs)
+    assert np.array_equal(got["mode"], mode)
+    assert np.array_equal(got["fail_eval"], fail)
+    assert (mode > 0).sum() > 20
+    led, ref = e.ledger(), o.energies()
+    scale = max(o.tool_work, 1e-30)
+    for k_g, k_o in (("kinetic", "kinetic"), ("bond_elastic", "bond_elastic"),
+                     ("fracture_released", "fracture_released"), ("dissipated", "dissipated")):
+        assert abs(led[k_g] - ref[k_o]) <= 1e-6 * scale, k_g
+    assert abs(led["tool_work"] - o.tool_work) <= 1e-6 * scale
+    load = e.load_curve()
+    assert load.shape[0] == o.evals - 1
+
+
+def test_fp32_bonded_sheet_peak_load_within_one_percent(hm):
+    cfg, st, bonds, strength = small_sheet(24, 8, precision=32, steps=600, speed=20.0)
+    e = _engine(hm, cfg, st, bonds, strength)
+    o = bonded_oracle_for(cfg, st, bonds, strength)
+    loads_o = []
+    for _ in range(300):
+        o.step(1)
+        loads_o.append(o.reaction[1])
+    e.step(300)
+    load = e.load_curve()[:, 1]
+    peak_g, peak_o = float(load.max()), float(max(loads_o))
+    print("peak indenter load gpu fp32", peak_g, "oracle fp64", peak_o)
+    assert abs(peak_g - peak_o) <= 0.01 * peak_o
+    led, ref = e.ledger(), o.energies()
+    assert abs(led["total"] - ref["total"]) <= 0.02 * o.tool_work
+    nb_g, nb_o = led["broken"], int((~o.alive).sum())
+    assert abs(nb_g - nb_o) <= max(5, 0.1 * nb_o)
+
+
+def test_bonded_variants_bit_identical(hm):
+    from tensordem_gb300 import _lib
+    outs = []
+    for v in range(_lib.lib().tdem_hm_num_variants()):
+        cfg, st, bonds, strength = small_sheet(24, 8, precision=32, steps=200, speed=20.0)
+        e = _engine(hm, cfg, st, bonds, strength)
+        e.variant = v
+        e.step(150)
+        s = e.state()
+        outs.append((s["pos"].cpu().numpy().tobytes(), e.bonds()["mode"].tobytes()))
+    assert all(o == outs[0] for o in outs[1:])
+
+
+def test_full_size_ice_sheet_builds_and_steps(hm):
+    cfg, st, bonds, strength = hm.ice_sheet_case(2048, 512, steps=50)
+    e = _engine(hm, cfg, st, bonds, strength)
+    e.step(20)
+    led = e.ledger()
+    assert led["status"] == 0 and led["evals"] == 20
+    assert len(e.bonds()["pairs"]) == len(bonds)
