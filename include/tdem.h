@@ -337,6 +337,110 @@ int tdem_hm_use_graph(tdem_hm* h, int on);
 
 int tdem_hm_last_error(const tdem_hm* h, char* buf, size_t len);
 
+/* ========================================================================
+ * 3. Batched ragged engine ("batch"): many independent spec solves
+ * ====================================================================== */
+
+/* Many independent solves of uneven sizes (each described by a
+ * tdem_hm_config and its own state, material, walls, bonds and indenter)
+ * packed into one sorted SoA and advanced together: one persistent step
+ * kernel per step, one conditional CUDA graph launch per step block. Each
+ * instance owns a contiguous range of cell keys and so a contiguous range of
+ * the sorted arrays, cut into 32-particle tiles that a warp processes with
+ * the instance's parameters. Per-instance ledgers are summed in tile order:
+ * an instance's result does not depend on the other instances in the batch
+ * except through the (shared) rebuild schedule; with rebuild_every > 0 and no
+ * displacement-triggered rebuild the results are bit-identical alone and in
+ * any mix.
+ *
+ * The reference runs one `IceDEM` / engine object per solve
+ * (src/tensordem/dem.py:75); these entry points replace a loop over such
+ * objects (src/tensordem/sensitivity.py:36-75 runs that loop). */
+typedef struct tdem_batch tdem_batch;
+
+typedef struct {
+  int32_t precision;         /* 32: FP32 contacts, compensated sums, FP64 ledger; 64: plain FP64 */
+  int32_t max_neighbors;     /* candidate slots per particle, 1..24 */
+  int32_t max_bonds;         /* bond slots per particle, 0..8 */
+  int32_t max_instances;     /* instance slots */
+  int64_t particle_capacity; /* particles resident at once (live + retired awaiting compaction) */
+  int64_t key_capacity;      /* cell keys over all instances (an instance takes ncx * ncy) */
+  int32_t rebuild_every;     /* 0: rebuild on the displacement bound only; k > 0: also every k steps */
+} tdem_batch_config;
+
+/* Ledger slots of tdem_batch_read: TDEM_HM_L_* (per instance; EVALS counts
+ * the instance's own evaluations) followed by these. */
+enum {
+  TDEM_BATCH_L_PEAK_LOAD = 16,   /* max over evaluations of |indenter reaction| (N) */
+  TDEM_BATCH_L_PEAK_EVAL = 17,   /* instance evaluation index of that maximum */
+  TDEM_BATCH_L_REACTION_X = 18,  /* indenter reaction of the last evaluation (N) */
+  TDEM_BATCH_L_REACTION_Y = 19,
+  TDEM_BATCH_L_COUNT = 20
+};
+
+/* Slots of tdem_batch_info. */
+enum {
+  TDEM_BATCH_I_LIVE_PARTICLES = 0, TDEM_BATCH_I_LIVE_INSTANCES, TDEM_BATCH_I_EVALS, TDEM_BATCH_I_REBUILDS,
+  TDEM_BATCH_I_TILES, TDEM_BATCH_I_PARTICLE_CAPACITY, TDEM_BATCH_I_BYTES, TDEM_BATCH_I_KEY_HI,
+  TDEM_BATCH_I_STATUS, TDEM_BATCH_I_VARIANT, TDEM_BATCH_I_GRAPH, TDEM_BATCH_I_MAX_NEIGHBORS,
+  TDEM_BATCH_I_COUNT
+};
+
+/* Device bytes a batch with this configuration allocates (admission by HBM
+ * footprint sizes its capacities with this). */
+int tdem_batch_bytes(const tdem_batch_config* cfg, int64_t* bytes);
+
+/* Allocate every device buffer for the capacities in one allocation. */
+int tdem_batch_create(const tdem_batch_config* cfg, tdem_batch** out);
+void tdem_batch_destroy(tdem_batch* h);
+
+/* Admit one instance: its configuration (`n`, grid, cell, skin, dt, material,
+ * walls, gravity, bond law, indenter; `precision`, `max_neighbors`,
+ * `max_bonds` and `load_capacity` are the batch's), its state in host FP64
+ * arrays in local order (as tdem_hm_set_state), and optional bonds (pairs of
+ * local ids with strength factors). The instance joins at the next step
+ * boundary; its first step primes velocity-Verlet. Writes its id.
+ * Synchronizes `stream`. TDEM_ERR_CAPACITY when particles, keys or slots
+ * are exhausted. */
+int tdem_batch_admit(tdem_batch* h, const tdem_hm_config* inst, const double* pos, const double* vel,
+                     const double* omega, const double* radius, const double* mass, const double* inertia,
+                     const int32_t* bond_pairs, const double* bond_strength, int64_t n_bonds, int32_t* out_id,
+                     void* stream);
+
+/* Advance every live instance by n_steps (one graph launch). Asynchronous. */
+int tdem_batch_step(tdem_batch* h, int64_t n_steps, void* stream);
+
+/* Integer-time state of one instance in its local order (host FP64 outputs,
+ * any may be NULL) and its ledger (TDEM_BATCH_L_COUNT doubles). Runs one
+ * read-back evaluation of that instance only. Synchronizes `stream`. */
+int tdem_batch_read(tdem_batch* h, int32_t id, double* pos, double* vel, double* omega, double* force,
+                    double* torque, double* ledger, int32_t ledger_count, void* stream);
+
+/* Ledgers of `count` live instances (count x TDEM_BATCH_L_COUNT doubles,
+ * host) from one read-back evaluation of all of them. Synchronizes `stream`. */
+int tdem_batch_read_ledgers(tdem_batch* h, const int32_t* ids, int32_t count, double* out, void* stream);
+
+/* Retire an instance: it stops at once; its particles, slot and key range
+ * are reclaimed by the compaction rebuild at the next step boundary. */
+int tdem_batch_retire(tdem_batch* h, int32_t id, void* stream);
+
+/* Bond states of one instance: (lo, hi) local ids, (mode: 0 intact, 1
+ * tensile, 2 shear, 3 both; instance evaluation of the break or -1). */
+int tdem_batch_read_bonds(tdem_batch* h, int32_t id, int32_t* pairs, int32_t* state, int64_t capacity,
+                          int64_t* count, void* stream);
+
+/* Batch counters (TDEM_BATCH_I_COUNT int64). Synchronizes `stream`. */
+int tdem_batch_info(tdem_batch* h, int64_t* out, int32_t count, void* stream);
+
+/* Step-kernel variants (block shape, CTAs per SM) and the autotuner that
+ * times `steps` real steps of each and keeps the fastest. */
+int tdem_batch_num_variants(void);
+int tdem_batch_set_variant(tdem_batch* h, int variant);
+int tdem_batch_get_variant(const tdem_batch* h);
+int tdem_batch_autotune(tdem_batch* h, int steps, float* ms_out, void* stream);
+int tdem_batch_use_graph(tdem_batch* h, int on);
+int tdem_batch_last_error(const tdem_batch* h, char* buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,6 +80,20 @@ class HMConfigC(C.Structure):
     ]
 
 
+class BatchConfigC(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32), ("max_neighbors", C.c_int32), ("max_bonds", C.c_int32),
+        ("max_instances", C.c_int32), ("particle_capacity", C.c_int64), ("key_capacity", C.c_int64),
+        ("rebuild_every", C.c_int32),
+    ]
+
+
+# Batched engine: extra ledger slots (TDEM_BATCH_L_*) and info slots (TDEM_BATCH_I_*)
+BATCH_PEAK_LOAD, BATCH_PEAK_EVAL, BATCH_REACTION_X, BATCH_REACTION_Y = 16, 17, 18, 19
+BATCH_L_COUNT = 20
+BATCH_INFO = ("live_particles", "live_instances", "evals", "rebuilds", "tiles", "particle_capacity",
+              "bytes", "key_hi", "status", "variant", "graph", "max_neighbors")
+
 # Hertz-Mindlin ledger slots (TDEM_HM_L_*)
 HM_KINETIC, HM_POTENTIAL, HM_HERTZ, HM_TANGENTIAL, HM_TOTAL, HM_DISSIPATED = range(6)
 HM_EVALS, HM_REBUILDS, HM_MAX_NEIGHBORS, HM_STATUS = 6, 7, 8, 9
@@ -125,6 +139,23 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_hm_rebuild": (i32, [vp, vp]),
         "tdem_hm_read_history": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_hm_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "tdem_batch_bytes": (i32, [C.POINTER(BatchConfigC), C.POINTER(C.c_int64)]),
+        "tdem_batch_create": (i32, [C.POINTER(BatchConfigC), C.POINTER(vp)]),
+        "tdem_batch_destroy": (None, [vp]),
+        "tdem_batch_admit": (i32, [vp, C.POINTER(HMConfigC), vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64,
+                                   C.POINTER(C.c_int32), vp]),
+        "tdem_batch_step": (i32, [vp, C.c_int64, vp]),
+        "tdem_batch_read": (i32, [vp, C.c_int32, vp, vp, vp, vp, vp, vp, C.c_int32, vp]),
+        "tdem_batch_retire": (i32, [vp, C.c_int32, vp]),
+        "tdem_batch_read_ledgers": (i32, [vp, vp, C.c_int32, vp, vp]),
+        "tdem_batch_read_bonds": (i32, [vp, C.c_int32, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
+        "tdem_batch_info": (i32, [vp, C.POINTER(C.c_int64), C.c_int32, vp]),
+        "tdem_batch_num_variants": (i32, []),
+        "tdem_batch_set_variant": (i32, [vp, i32]),
+        "tdem_batch_get_variant": (i32, [vp]),
+        "tdem_batch_autotune": (i32, [vp, i32, C.POINTER(C.c_float), vp]),
+        "tdem_batch_use_graph": (i32, [vp, i32]),
+        "tdem_batch_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -152,6 +183,8 @@ def last_error(fn_name: str, handle) -> str:
     buf = C.create_string_buffer(1024)
     if fn_name.startswith("tdem_hm"):
         lib().tdem_hm_last_error(handle, buf, len(buf))
+    elif fn_name.startswith("tdem_batch"):
+        lib().tdem_batch_last_error(handle, buf, len(buf))
     else:
         lib().tdem_icedem_last_error(handle, buf, len(buf))
     return buf.value.decode(errors="replace")

@@ -48,7 +48,7 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> Path:
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + list((PKG.parent / "include").glob("*.h"))
+    headers = [*CSRC.glob("*.h"), *CSRC.glob("*.cuh"), *(PKG.parent / "include").glob("*.h")]
     jobs = []
     for src in sources():
         obj = BUILD / (src.stem + ".o")

@@ -6,6 +6,8 @@
   reference-mode kernel.
 * ``hm2d`` - the Hertz-Mindlin disc settling case on the GB300 engine: run,
   time and report (used for profiling runs as well).
+* ``ensemble`` - a seeded mixed ensemble of independent runs in the batched
+  engine, against the same runs one-by-one through the FP64 engine.
 """
 
 from __future__ import annotations
@@ -116,14 +118,22 @@ def _cmd_dem_2d(args: argparse.Namespace) -> None:
 
 
 def _cmd_hm2d(args: argparse.Namespace) -> None:
-    from .hm2d import HM2D, granular_gas_case
+    from .hm2d import HM2D, granular_gas_case, ice_sheet_case
 
-    cfg, st = granular_gas_case(args.n_side, seed=args.seed, precision=args.precision,
-                                max_neighbors=args.max_neighbors)
+    bonds = None
+    if args.case == "ice":
+        nx = args.n_side * 2
+        cfg, st, bonds, strength = ice_sheet_case(nx, max(2, args.n_side // 2), precision=args.precision,
+                                                  seed=args.seed, steps=max(args.steps, 1))
+    else:
+        cfg, st = granular_gas_case(args.n_side, seed=args.seed, precision=args.precision,
+                                    max_neighbors=args.max_neighbors)
     eng = HM2D(cfg)
     if args.no_graph:
         eng.use_graph(False)
     eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
+    if bonds is not None:
+        eng.set_bonds(bonds, strength)
     if args.variant is not None:
         eng.variant = args.variant
     elif args.autotune:
@@ -136,6 +146,18 @@ def _cmd_hm2d(args: argparse.Namespace) -> None:
     led = eng.ledger()
     print(json.dumps({"discs": cfg.n, "steps": args.steps, "seconds": dt,
                       "particle_steps_per_s": cfg.n * args.steps / dt, "ledger": led}))
+
+
+def _cmd_ensemble(args: argparse.Namespace) -> None:
+    import os
+
+    from . import ensemble
+
+    if args.no_graph:
+        os.environ["TDEM_GRAPH"] = "0"
+    out = ensemble.main(args)
+    if args.output:
+        Path(args.output).write_text(json.dumps(out, indent=1))
 
 
 def main(argv: list[str] | None = None) -> None:
@@ -159,6 +181,8 @@ def main(argv: list[str] | None = None) -> None:
     d.add_argument("--save-every", type=int, default=20)
     d.set_defaults(func=_cmd_dem_2d)
     h = sub.add_parser("hm2d", help="Hertz-Mindlin disc settling case on the GPU engine")
+    h.add_argument("--case", choices=("gas", "ice"), default="gas",
+                   help="gas: n-side^2 disc settling case; ice: (2 n-side) x (n-side / 2) bonded hex sheet")
     h.add_argument("--n-side", type=int, default=1024)
     h.add_argument("--steps", type=int, default=100)
     h.add_argument("--seed", type=int, default=0)
@@ -168,6 +192,21 @@ def main(argv: list[str] | None = None) -> None:
     h.add_argument("--autotune", action="store_true")
     h.add_argument("--no-graph", action="store_true", help="plain launches (visible to profilers)")
     h.set_defaults(func=_cmd_hm2d)
+    en = sub.add_parser("ensemble", help="mixed ensemble of 2-D runs: batched engine vs one-by-one FP64")
+    en.add_argument("--instances", type=int, default=4096)
+    en.add_argument("--steps", type=int, default=5000)
+    en.add_argument("--seed", type=int, default=0)
+    en.add_argument("--n-min", type=int, default=100)
+    en.add_argument("--n-max", type=int, default=20000)
+    en.add_argument("--precision", type=int, choices=(32, 64), default=32)
+    en.add_argument("--baseline-sample", type=int, default=64)
+    en.add_argument("--autotune-steps", type=int, default=2)
+    en.add_argument("--variant", type=int, default=None)
+    en.add_argument("--rebuild-every", type=int, default=0)
+    en.add_argument("--kind", choices=("all", "ice", "column"), default="all")
+    en.add_argument("--no-graph", action="store_true", help="plain launches (visible to profilers)")
+    en.add_argument("--output", type=Path, default=None)
+    en.set_defaults(func=_cmd_ensemble)
     args = parser.parse_args(argv)
     if not hasattr(args, "func"):
         parser.print_help()

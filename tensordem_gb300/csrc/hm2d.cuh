@@ -87,6 +87,15 @@ struct Params {
   double ind_x0, ind_y0, ind_vx, ind_vy;
   T irad;
   int load_cap;   // capacity of the per-evaluation indenter load record
+  // batched engine: one Params per instance (n = the particle capacity, the
+  // stride of every slot-major array)
+  int key_off;       // first cell key of the instance (key = key_off + cy * ncx + cx)
+  long long eval0;   // batch evaluation index of the instance's first step
+  // FP32 screens that keep FP64 off the common path (decisions unchanged):
+  // float brackets of the break strains (largest float <= eps, smallest >= eps)
+  float eps_t_lo, eps_t_hi, eps_s_lo, eps_s_hi;
+  // indenter centre at evaluation 0 and its displacement per evaluation
+  float ind_x0f, ind_y0f, ind_dxf, ind_dyf;
 };
 
 constexpr unsigned kBondIdx = (1u << 29) - 1u;
@@ -112,7 +121,23 @@ struct Ctl {
   double reaction_x, reaction_y;  // ice-on-indenter force of the last evaluation
   unsigned load_entries;   // entries in the per-evaluation indenter list
   int broken;              // bonds broken so far
+  // batched engine
+  int n_live;              // particles in the sorted arrays [0, n_live)
+  int n_old;               // n_live when the running rebuild started
+  int ntiles;              // 32-particle tiles of the live instances
+  int since;               // steps since the last rebuild
+  int key_hi;              // dead-particle key: one past the highest allocated cell key
+  int tile_next;           // next tile chunk handed out by the running step kernel
 };
+
+// Batched engine: per-instance state word (low byte: Status bits of the
+// instance) and the fixed tile width (one warp per tile).
+constexpr int kInstAlive = 1 << 8;   // stepped; cleared when the instance retires
+constexpr int kInstPeek = 1 << 9;    // selected for the next read-back evaluation
+constexpr int kInstRebuildShift = 16;  // Status bits found by a rebuild (bits 16..23)
+constexpr int kTile = 32;
+constexpr int kTileVals = 12;        // per-tile ledger partial row
+constexpr int kInstLedger = 24;      // per-instance ledger row (doubles)
 
 template <class T>
 struct Bufs {
@@ -152,6 +177,16 @@ struct Bufs {
   // indenter: per-evaluation partial reactions (warp id, fx, fy) and the load record
   double* ind_part;    // [3 * nwarp_slots]
   double* load;        // [2 * load_cap]: reaction (x, y) per evaluation
+  // batched engine (null for a single solve)
+  int* inst[2];        // instance slot of each particle, swapped at a rebuild
+  const Params<T>* iparams;  // per instance slot
+  int* istate;         // per instance slot: kInstAlive | kInstPeek | Status bits
+  int4* irange;        // per instance slot: {first sorted index, end, first tile, tiles}
+  int4* tiles;         // {instance, first sorted index, count, -} per tile
+  double* tpart;       // [tiles * kTileVals] per-tile ledger partials
+  unsigned* iticket;   // per instance slot: tiles finished in the running kernel
+  double* iled;        // [slots * kInstLedger] per-instance ledger
+  int* tmp_key;        // rebuild: cell key of each old particle
 };
 
 // The cell id rides in the last lane of the position vector: bit-cast for
