@@ -407,7 +407,8 @@ int tdem_batch_admit(tdem_batch* h, const tdem_hm_config* inst, const double* po
                      const int32_t* bond_pairs, const double* bond_strength, int64_t n_bonds, int32_t* out_id,
                      void* stream);
 
-/* Advance every live instance by n_steps (one graph launch). Asynchronous. */
+/* Advance every live instance by n_steps (one graph launch). Asynchronous.
+ * n_steps == 0 only sorts in admitted instances and compacts retired ones. */
 int tdem_batch_step(tdem_batch* h, int64_t n_steps, void* stream);
 
 /* Integer-time state of one instance in its local order (host FP64 outputs,
@@ -419,6 +420,12 @@ int tdem_batch_read(tdem_batch* h, int32_t id, double* pos, double* vel, double*
 /* Ledgers of `count` live instances (count x TDEM_BATCH_L_COUNT doubles,
  * host) from one read-back evaluation of all of them. Synchronizes `stream`. */
 int tdem_batch_read_ledgers(tdem_batch* h, const int32_t* ids, int32_t count, double* out, void* stream);
+
+/* Step limit of an instance (0: none): once it has taken `steps` steps it is
+ * frozen (state carried over unchanged, no forces, no ledger) until it is
+ * read and retired. Lets a serving loop run fixed-length step blocks while
+ * instances finish at their own step counts. */
+int tdem_batch_set_steps(tdem_batch* h, int32_t id, int64_t steps, void* stream);
 
 /* Retire an instance: it stops at once; its particles, slot and key range
  * are reclaimed by the compaction rebuild at the next step boundary. */

@@ -147,6 +147,7 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_batch_step": (i32, [vp, C.c_int64, vp]),
         "tdem_batch_read": (i32, [vp, C.c_int32, vp, vp, vp, vp, vp, vp, C.c_int32, vp]),
         "tdem_batch_retire": (i32, [vp, C.c_int32, vp]),
+        "tdem_batch_set_steps": (i32, [vp, C.c_int32, C.c_int64, vp]),
         "tdem_batch_read_ledgers": (i32, [vp, vp, C.c_int32, vp, vp]),
         "tdem_batch_read_bonds": (i32, [vp, C.c_int32, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_batch_info": (i32, [vp, C.POINTER(C.c_int64), C.c_int32, vp]),

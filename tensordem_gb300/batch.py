@@ -26,7 +26,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .hm2d import ALL_WALLS, WALL_BOTTOM, WALL_LEFT, WALL_RIGHT, HM2DConfig, rayleigh_dt
+from .hm2d import ALL_WALLS, HM2DConfig, rayleigh_dt
 
 LEDGER_NAMES = ("kinetic", "potential", "hertz", "tangential", "total", "dissipated", "evals", "rebuilds",
                 "max_neighbors", "status", "graph", "variant", "bond_elastic", "fracture_released",
@@ -180,6 +180,12 @@ class Batch:
         _lib.check(rc, self._h, "tdem_batch_read_ledgers")
         return [dict(zip(LEDGER_NAMES, row.tolist())) for row in out]
 
+    def set_steps(self, iid: int, steps: int) -> None:
+        """Freeze the instance once it has taken ``steps`` steps (0: no limit)."""
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_batch_set_steps(self._h, iid, int(steps), self._stream())
+        _lib.check(rc, self._h, "tdem_batch_set_steps")
+
     def retire(self, iid: int) -> None:
         with torch.cuda.device(self.device):
             rc = self._lib.tdem_batch_retire(self._h, iid, self._stream())
@@ -240,19 +246,26 @@ def ice_instance(n_target: int, rng: np.random.Generator, *, young: float, mu: f
                  r0: float = 0.05, density: float = 900.0, poisson: float = 0.3, restitution: float = 0.5,
                  bond_damping: float = 0.05, breaking_strain: float = 0.01, shear_breaking_strain: float = 0.02,
                  strength_sigma: float = 0.1, speed: float = 0.5, dt_factor: float = 0.1,
-                 skin_factor: float = 0.1) -> Instance:
+                 skin_factor: float = 0.5) -> Instance:
     """Bonded hexagonal ice strip (about 4:1, both short ends clamped), indented
     from above at mid-span by a rigid disc; radii U[0.8, 1.2] r0. The lattice
     spacing is 2 r_max = 2.4 r0, so bonded neighbours never overlap at rest
-    and a broken bond never starts as a compressed contact."""
+    and a broken bond never starts as a compressed contact. Fragments released
+    by brittle breaks fly off at metres per second, so the domain is a walled
+    tank, and the skin is 0.5 r0: an intact lattice has no candidate inside it
+    (bonded pairs are excluded, the next shell is at 4.2 r0), and the wide skin
+    keeps list rebuilds rare."""
     nx = max(4, int(round(math.sqrt(4.0 * n_target))))
     ny = max(2, int(round(n_target / nx)))
     n = nx * ny
     r_max = 1.2 * r0
     half = r_max  # half the lattice spacing
+    dt = dt_factor * rayleigh_dt(0.8 * r0, density, young, poisson)
+    travel = speed * dt * steps
+    below = travel + 4.0 * r_max  # room for the sheet to bend under the indenter
     jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
     x = (2.0 * ii + (jj % 2)) * half + 2.0 * r_max
-    y = jj * math.sqrt(3.0) * half + 2.0 * r_max
+    y = jj * math.sqrt(3.0) * half + below
     pos = np.stack((x.ravel(), y.ravel()), axis=1)
     idx = jj * nx + ii
     pairs = [np.stack((idx[:, :-1].ravel(), idx[:, 1:].ravel()), axis=1)]
@@ -277,17 +290,16 @@ def ice_instance(n_target: int, rng: np.random.Generator, *, young: float, mu: f
     inertia = 0.5 * mass * radius**2
     kn = young * thickness
     ks = kn / (2.0 * (1.0 + poisson))
-    dt = dt_factor * rayleigh_dt(0.8 * r0, density, young, poisson)
     skin = skin_factor * r0
     ind_r = max(2.0 * r0, 2.0 * nx / 2048.0)
     width = (2.0 * nx + 1) * half + 4.0 * r_max
-    top = (ny - 1) * math.sqrt(3.0) * half + 2.0 * r_max
-    travel = speed * dt * steps
+    top = (ny - 1) * math.sqrt(3.0) * half + below
     height = top + r_max + 2.0 * ind_r + travel + 4.0 * r_max
     ncx, ncy, cell = _grid(width, height, 2.0 * r_max + skin)
     center = (0.5 * (x.min() + x.max()), top + r_max + ind_r + 0.02 * r0)
     cfg = HM2DConfig(n=n, ncx=ncx, ncy=ncy, cell=cell, skin=skin, dt=dt, young=young, poisson=poisson,
-                     restitution=restitution, mu=mu, mu_wall=mu, gravity=(0.0, 0.0), walls=0, max_neighbors=8,
+                     restitution=restitution, mu=mu, mu_wall=mu, gravity=(0.0, 0.0), walls=ALL_WALLS,
+                     max_neighbors=8,
                      max_bonds=6, bond_kn=kn, bond_ks=ks, bond_damping=bond_damping,
                      breaking_strain=breaking_strain, shear_breaking_strain=shear_breaking_strain,
                      indenter_center=center, indenter_velocity=(0.0, -speed), indenter_radius=ind_r)
@@ -300,8 +312,8 @@ def column_instance(n_target: int, rng: np.random.Generator, *, young: float, mu
                     restitution: float = 0.8, area_fraction: float = 0.55, sigma_v: float = 0.1,
                     skin_factor: float = 0.1) -> Instance:
     """Granular column (height / width = ``aspect``) against the left wall of a
-    walled box with room to run out; jittered grid at area fraction 0.55,
-    Gaussian velocities, gravity; radii U[0.8, 1.2] r0."""
+    closed box with room to run out and head room above; jittered grid at area
+    fraction 0.55, Gaussian velocities, gravity; radii U[0.8, 1.2] r0."""
     nx = max(2, int(round(math.sqrt(n_target / aspect))))
     ny = max(2, int(round(n_target / nx)))
     n = nx * ny
@@ -311,7 +323,7 @@ def column_instance(n_target: int, rng: np.random.Generator, *, young: float, mu
     a = max(math.sqrt(math.pi * mean_r2 / area_fraction), 2.0 * r_max * 1.0001)
     skin = skin_factor * r0
     w, h = nx * a, ny * a
-    ncx, ncy, cell = _grid(w + h, 1.1 * h + 2.0 * a, 2.0 * r_max + skin)
+    ncx, ncy, cell = _grid(w + h, h + max(0.25 * h, 0.02) + 2.0 * a, 2.0 * r_max + skin)
     jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
     centre = np.stack(((ii.ravel() + 0.5) * a, (jj.ravel() + 0.5) * a), axis=1)
     room = np.maximum(0.5 * a - radius, 0.0)[:, None]
@@ -322,7 +334,7 @@ def column_instance(n_target: int, rng: np.random.Generator, *, young: float, mu
     dt = 0.2 * rayleigh_dt(r_min, density, young, poisson)
     cfg = HM2DConfig(n=n, ncx=ncx, ncy=ncy, cell=cell, skin=skin, dt=dt, young=young, poisson=poisson,
                      restitution=restitution, mu=mu, mu_wall=mu, gravity=(0.0, -9.81),
-                     walls=WALL_LEFT | WALL_RIGHT | WALL_BOTTOM, max_neighbors=12)
+                     walls=ALL_WALLS, max_neighbors=12)
     state = dict(pos=pos, vel=vel, omega=np.zeros(n), radius=radius, mass=mass, inertia=inertia)
     return Instance(cfg, state, None, None, steps, "column", {"nx": nx, "ny": ny, "aspect": aspect})
 

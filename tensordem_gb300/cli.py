@@ -8,6 +8,8 @@
   time and report (used for profiling runs as well).
 * ``ensemble`` - a seeded mixed ensemble of independent runs in the batched
   engine, against the same runs one-by-one through the FP64 engine.
+* ``serve`` - a Poisson trace of such runs served by continuous batching
+  under an HBM budget (time-to-completion percentiles, throughput).
 """
 
 from __future__ import annotations
@@ -160,6 +162,14 @@ def _cmd_ensemble(args: argparse.Namespace) -> None:
         Path(args.output).write_text(json.dumps(out, indent=1))
 
 
+def _cmd_serve(args: argparse.Namespace) -> None:
+    from . import serve
+
+    out = serve.main(args)
+    if args.output:
+        Path(args.output).write_text(json.dumps(out, indent=1))
+
+
 def main(argv: list[str] | None = None) -> None:
     parser = argparse.ArgumentParser(description="tensordem_gb300: GB300 2-D DEM step")
     sub = parser.add_subparsers(dest="command")
@@ -207,6 +217,21 @@ def main(argv: list[str] | None = None) -> None:
     en.add_argument("--no-graph", action="store_true", help="plain launches (visible to profilers)")
     en.add_argument("--output", type=Path, default=None)
     en.set_defaults(func=_cmd_ensemble)
+    sv = sub.add_parser("serve", help="Poisson request trace served by continuous batching")
+    sv.add_argument("--duration", type=float, default=600.0, help="arrival window (s)")
+    sv.add_argument("--load", type=float, default=0.8, help="fraction of the capacity offered")
+    sv.add_argument("--capacity", type=float, default=7.1e9,
+                    help="engine capacity in particle-steps/s (measured on the 4096-run ensemble)")
+    sv.add_argument("--budget-gb", type=float, default=150.0)
+    sv.add_argument("--block", type=int, default=100, help="steps per step block")
+    sv.add_argument("--rebuild-every", type=int, default=0)
+    sv.add_argument("--seed", type=int, default=0)
+    sv.add_argument("--n-min", type=int, default=500)
+    sv.add_argument("--n-max", type=int, default=200_000)
+    sv.add_argument("--s-min", type=int, default=1000)
+    sv.add_argument("--s-max", type=int, default=50_000)
+    sv.add_argument("--output", type=Path, default=None)
+    sv.set_defaults(func=_cmd_serve)
     args = parser.parse_args(argv)
     if not hasattr(args, "func"):
         parser.print_help()

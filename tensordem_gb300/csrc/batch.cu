@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
       hd = head[d.y + lane];
     }
   }
+  bool frozen = false;  // the open segment's instance has taken all its steps
   int seg_k = -1;  // instance of the open segment
   int seg_n = 0;   // tiles of the open segment processed by this warp
   bool run = false;
@@ -257,9 +259,20 @@ __global__ void __launch_bounds__(BLOCK, MINB)
         __syncwarp();
         le = eval - Q.eval0;
         primed = le > 0 ? 1 : 0;
+        // quarantine: an instance with a non-finite state, an escaped particle or
+        // an overflowed neighbour list stops (its status is reported), so it can
+        // neither slow the shared rebuild trigger nor spread garbage
+        const int bad = (st | (st >> kInstRebuildShift)) & (kStatusNonfinite | kStatusEscaped | kStatusCapacity);
+        frozen = MODE == kBatch && (le >= Q.stop || bad != 0);
       }
     }
-    if (run) {
+    if (run && frozen) {
+      // carry the state over unchanged (no forces, no ledger, no ticket)
+      if (lane < d.z) {
+        B.pos[sp ^ 1][d.y + lane] = p;
+        B.vel[sp ^ 1][d.y + lane] = v;
+      }
+    } else if (run) {
       ThreadLedger<T> L;
       if (lane < d.z) process_particle<T, MODE, true>(Q, B, sp, lp, d.y + lane, p, v, hd, primed, le, L);
       double* row = B.tpart + (size_t)t * kTileVals;
@@ -551,6 +564,7 @@ struct BatchBase {
   virtual int read(int id, double* pos, double* vel, double* omega, double* force, double* torque, double* ledger,
                    int count, cudaStream_t s) = 0;
   virtual int retire(int id, cudaStream_t s) = 0;
+  virtual int set_steps(int id, long long steps, cudaStream_t s) = 0;
   virtual int read_ledgers(const int* ids, int count, double* out, cudaStream_t s) = 0;
   virtual int read_bonds(int id, int* pairs, int* state, long long cap, long long* count, cudaStream_t s) = 0;
   virtual int info(long long* out, int count, cudaStream_t s) = 0;
@@ -999,6 +1013,7 @@ struct Batch final : BatchBase {
     I.par.load_cap = 0;
     I.par.key_off = key_off;
     I.par.eval0 = evals;
+    I.par.stop = LLONG_MAX;
     // stage and append
     double* h = stage_host;
     std::memcpy(h, pos, 2 * (size_t)m * sizeof(double));
@@ -1052,9 +1067,8 @@ struct Batch final : BatchBase {
   }
 
   int step(long long n, cudaStream_t s) override {
-    if (n <= 0) return TDEM_OK;
-    int rc = settle(s);
-    if (rc) return rc;
+    int rc = settle(s);  // n == 0 only settles admissions and retirements
+    if (rc || n <= 0) return rc;
     if (graph_on && !graph_failed && !exec) {
       if (build_graph() != TDEM_OK) {
         graph_failed = true;  // plain launches: the same kernels and results
@@ -1144,7 +1158,7 @@ struct Batch final : BatchBase {
     v[TDEM_HM_L_TOTAL] = v[TDEM_HM_L_KINETIC] + v[TDEM_HM_L_POTENTIAL] + v[TDEM_HM_L_HERTZ] +
                          v[TDEM_HM_L_TANGENTIAL] + v[TDEM_HM_L_DISSIPATED] + v[TDEM_HM_L_BOND_ELASTIC] +
                          v[TDEM_HM_L_FRACTURE] - v[TDEM_HM_L_TOOL_WORK];
-    v[TDEM_HM_L_EVALS] = (double)(evals - I.eval0);
+    v[TDEM_HM_L_EVALS] = (double)std::min(evals - I.eval0, I.par.stop);  // a frozen instance stops counting
     v[TDEM_HM_L_REBUILDS] = (double)host_ctl->rebuilds;
     v[TDEM_HM_L_MAX_NEIGHBORS] = (double)host_ctl->max_cnt;
     v[TDEM_HM_L_STATUS] = (double)((st | (st >> kInstRebuildShift)) & 0xFF);
@@ -1202,6 +1216,17 @@ struct Batch final : BatchBase {
     for (int j = 0; j < count; ++j)
       assemble_ledger(inst[(size_t)ids[j]], all_led_host + (size_t)ids[j] * kInstLedger, all_state_host[ids[j]],
                       out + (size_t)j * TDEM_BATCH_L_COUNT, TDEM_BATCH_L_COUNT);
+    return TDEM_OK;
+  }
+
+  int set_steps(int id, long long steps, cudaStream_t s) override {
+    int rc = check_id(id);
+    if (rc) return rc;
+    if (steps < 0) return tdem::fail(&err, TDEM_ERR_BADARG, "set_steps: steps must be >= 0");
+    Inst& I = inst[(size_t)id];
+    I.par.stop = steps == 0 ? LLONG_MAX : steps;
+    batch_set_params_kernel<T><<<1, 1, 0, s>>>(iparams + id, I.par);
+    TDEM_CUDA_TRY(&err, cudaGetLastError());
     return TDEM_OK;
   }
 
@@ -1392,6 +1417,11 @@ int tdem_batch_read(tdem_batch* h, int32_t id, double* pos, double* vel, double*
 int tdem_batch_read_ledgers(tdem_batch* h, const int32_t* ids, int32_t count, double* out, void* stream) {
   if (!h || (count > 0 && (!ids || !out))) return TDEM_ERR_BADARG;
   return h->e->read_ledgers(ids, count, out, static_cast<cudaStream_t>(stream));
+}
+
+int tdem_batch_set_steps(tdem_batch* h, int32_t id, int64_t steps, void* stream) {
+  if (!h) return TDEM_ERR_BADARG;
+  return h->e->set_steps(id, (long long)steps, static_cast<cudaStream_t>(stream));
 }
 
 int tdem_batch_retire(tdem_batch* h, int32_t id, void* stream) {

@@ -91,6 +91,7 @@ struct Params {
   // stride of every slot-major array)
   int key_off;       // first cell key of the instance (key = key_off + cy * ncx + cx)
   long long eval0;   // batch evaluation index of the instance's first step
+  long long stop;    // the instance's own step limit: frozen once it has taken `stop` steps
   // FP32 screens that keep FP64 off the common path (decisions unchanged):
   // float brackets of the break strains (largest float <= eps, smallest >= eps)
   float eps_t_lo, eps_t_hi, eps_s_lo, eps_s_hi;

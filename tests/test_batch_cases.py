@@ -55,3 +55,24 @@ def test_batch_config_footprint_is_host_computable():
     except RuntimeError:  # the native library is not built in this environment
         return
     assert 400 * 1_000_000 < nbytes < 2000 * 1_000_000
+
+
+def test_serving_trace_and_budget_sizing():
+    from tensordem_gb300.serve import engine_for_budget, make_trace, mean_log_uniform
+    tr = make_trace(duration=100.0, rate=5.0, seed=2)
+    assert 400 < len(tr) < 600
+    arr = np.array([r.arrival for r in tr])
+    assert (np.diff(arr) > 0).all() and arr[-1] < 100.0
+    assert min(r.n for r in tr) >= 500 and max(r.n for r in tr) <= 200_000
+    assert min(r.steps for r in tr) >= 1000 and max(r.steps for r in tr) <= 50_000
+    # the offered rate follows load x capacity / E[N S]
+    cap = 7e9
+    tr2 = make_trace(duration=1000.0, capacity=cap, load=0.8, seed=3)
+    want = 0.8 * cap / (mean_log_uniform(500, 200_000) * mean_log_uniform(1000, 50_000))
+    assert abs(len(tr2) / 1000.0 - want) < 0.15 * want
+    try:
+        cfg, per_p, per_k = engine_for_budget(int(150e9))
+    except RuntimeError:  # the native library is not built in this environment
+        return
+    assert cfg.bytes() <= 150e9 and cfg.particle_capacity > 1e8
+    assert 300 < per_p < 2000 and 4 < per_k < 64
