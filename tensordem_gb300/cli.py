@@ -220,8 +220,9 @@ def main(argv: list[str] | None = None) -> None:
     sv = sub.add_parser("serve", help="Poisson request trace served by continuous batching")
     sv.add_argument("--duration", type=float, default=600.0, help="arrival window (s)")
     sv.add_argument("--load", type=float, default=0.8, help="fraction of the capacity offered")
-    sv.add_argument("--capacity", type=float, default=7.1e9,
-                    help="engine capacity in particle-steps/s (measured on the 4096-run ensemble)")
+    sv.add_argument("--capacity", type=float, default=None,
+                    help="engine capacity in particle-steps/s (default: measured by a saturated calibration run)")
+    sv.add_argument("--calibrate-seconds", type=float, default=20.0)
     sv.add_argument("--budget-gb", type=float, default=150.0)
     sv.add_argument("--block", type=int, default=100, help="steps per step block")
     sv.add_argument("--rebuild-every", type=int, default=0)

@@ -117,6 +117,7 @@ def serve(trace: list[Request], *, budget_bytes: int, block: int = 100, rebuild_
     blocks = 0
     busy = 0.0
     input_waits = 0
+    processed = 0  # particle-steps advanced (finished or not)
     t0 = time.perf_counter()
 
     def clock():
@@ -167,6 +168,7 @@ def serve(trace: list[Request], *, budget_bytes: int, block: int = 100, rebuild_
             if nxt is not None:
                 time.sleep(max(0.0, min(nxt - clock(), 0.05)))
             continue
+        processed += sum(r.n * max(0, min(block, r.steps - (evals - r.eval0))) for r in live.values())
         peak_live_particles = max(peak_live_particles, sum(r.n for r in live.values()))
         peak_used = max(peak_used, used)
         ts = clock()
@@ -205,6 +207,7 @@ def serve(trace: list[Request], *, budget_bytes: int, block: int = 100, rebuild_
         "particle_steps_per_s": work / wall if wall > 0 else 0.0,
         "particle_steps_per_s_busy": work / busy if busy > 0 else 0.0,
         "completed_particle_steps": work,
+        "processed_particle_steps_per_s_busy": processed / busy if busy > 0 else 0.0,
         "blocks": blocks, "block_steps": block, "batch_steps": steps_run,
         "peak_live_particles": peak_live_particles, "peak_footprint_gb": peak_used / 1e9,
         "budget_gb": budget_bytes / 1e9, "engine_bytes": info["bytes"], "rebuilds": info["rebuilds"],
@@ -218,15 +221,30 @@ def serve(trace: list[Request], *, budget_bytes: int, block: int = 100, rebuild_
     }
 
 
+def calibrate(*, seconds: float, budget_bytes: int, block: int, seed: int, n_min: int, n_max: int, s_min: int,
+              s_max: int, guess: float = 1e10) -> float:
+    """Capacity of the engine on this request mix: particle-steps/s advanced
+    while requests are offered faster than it can serve them."""
+    trace = make_trace(duration=seconds, capacity=guess, load=2.0, seed=seed + 1000, n_min=n_min, n_max=n_max,
+                       s_min=s_min, s_max=s_max)
+    rep = serve(trace, budget_bytes=budget_bytes, block=block, time_limit=seconds)
+    return rep["processed_particle_steps_per_s_busy"]
+
+
 def main(args) -> dict:
     capacity = args.capacity
+    budget = int(args.budget_gb * 1e9)
+    calibrated = capacity is None
+    if calibrated:
+        capacity = calibrate(seconds=args.calibrate_seconds, budget_bytes=budget, block=args.block, seed=args.seed,
+                             n_min=args.n_min, n_max=args.n_max, s_min=args.s_min, s_max=args.s_max)
     trace = make_trace(duration=args.duration, capacity=capacity, load=args.load, seed=args.seed,
                        n_min=args.n_min, n_max=args.n_max, s_min=args.s_min, s_max=args.s_max)
-    rep = serve(trace, budget_bytes=int(args.budget_gb * 1e9), block=args.block, rebuild_every=args.rebuild_every,
+    rep = serve(trace, budget_bytes=budget, block=args.block, rebuild_every=args.rebuild_every,
                 time_limit=args.duration * 3 + 60)
     rep.pop("done")
     out = {"metric": "served time-to-completion and particle-steps/s", "load": args.load,
-           "capacity_particle_steps_per_s": capacity,
+           "capacity_particle_steps_per_s": capacity, "capacity_measured": calibrated,
            "arrival_rate_per_s": len(trace) / args.duration, "duration_s": args.duration, **rep}
     print(json.dumps(out))
     return out
