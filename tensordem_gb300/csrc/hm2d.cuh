@@ -82,6 +82,7 @@ struct Params {
   int BMAX;
   T kn, ks;       // bond normal and shear stiffness (N/m)
   T bzeta;        // bond damping ratio: c = 2 zeta sqrt(k m*)
+  T cn_k, cs_k;   // 2 zeta sqrt(kn), 2 zeta sqrt(ks): c = c_k / sqrt(1/m_a + 1/m_b)
   double eps_t, eps_s;  // tensile and objective-shear break strains
   // rigid circular indenter (irad == 0: none), Hertz normal + dashpot
   double ind_x0, ind_y0, ind_vx, ind_vy;

@@ -69,11 +69,23 @@ __device__ __forceinline__ PairOut<T> pair_force(const Params<T>& P, const Geo<T
     o.xi = V2<T>{T(0), T(0)};
     return o;
   }
-  const T d = dev_sqrt(g.d2);
+  const T d = dev_sqrt(g.d2);  // IEEE: the overlap rs - d is a small difference
   const T delta = g.rs - d;
-  const T nx = g.dx / d, ny = g.dy / d;
-  const T reff = pa.z * pb.z / g.rs;
-  const T meff = T(1) / (va.w + vb.w);
+  // FP32: reciprocals instead of divides (rcp_rn then a product: <= 1 ulp);
+  // _rn products are never fused, so every kernel computes the same bits
+  T nx, ny, reff, meff;
+  if constexpr (sizeof(T) == 4) {
+    const T inv_d = __frcp_rn(d);
+    nx = __fmul_rn(g.dx, inv_d);
+    ny = __fmul_rn(g.dy, inv_d);
+    reff = __fmul_rn(__fmul_rn(pa.z, pb.z), __frcp_rn(g.rs));
+    meff = __frcp_rn(va.w + vb.w);
+  } else {
+    nx = g.dx / d;
+    ny = g.dy / d;
+    reff = pa.z * pb.z / g.rs;
+    meff = T(1) / (va.w + vb.w);
+  }
   const T sq = dev_sqrt(reff * delta);
   const T sn = P.estar2 * sq;
   const T fel = (T(2) / T(3)) * sn * delta;
@@ -407,10 +419,28 @@ __device__ __forceinline__ void do_bond(const Params<T>& P, const Bufs<T>& B, in
   V2<T> us = in.us;
   if (!broken) {
     const T ux = g.dx - ref.x, uy = g.dy - ref.y;
-    const T d = dev_sqrt(g.d2);
-    const T l0 = dev_sqrt(ref.x * ref.x + ref.y * ref.y);
-    const T ext = (T(2) * (ref.x * ux + ref.y * uy) + (ux * ux + uy * uy)) / (d + l0);
-    const T tensile = ext / l0;
+    // FP32: bond lengths and directions from rsqrt / rcp (a few ulp; the
+    // extension is formed without cancellation); FP64: exact operations
+    T d, l0, inv_d, inv_l0, inv_dl;
+    if constexpr (sizeof(T) == 4) {
+      // _rn intrinsics are never fused into an FMA, so every kernel that
+      // inlines this computes the same bits
+      inv_d = rsqrtf(g.d2);
+      d = __fmul_rn(g.d2, inv_d);
+      const T l02 = __fadd_rn(__fmul_rn(ref.x, ref.x), __fmul_rn(ref.y, ref.y));
+      inv_l0 = rsqrtf(l02);
+      l0 = __fmul_rn(l02, inv_l0);
+      inv_dl = __frcp_rn(__fadd_rn(d, l0));
+    } else {
+      d = dev_sqrt(g.d2);
+      l0 = dev_sqrt(ref.x * ref.x + ref.y * ref.y);
+      inv_d = T(1) / d;
+      inv_l0 = T(1) / l0;
+      inv_dl = T(1) / (d + l0);
+    }
+    const T ext = sizeof(T) == 4 ? (T(2) * (ref.x * ux + ref.y * uy) + (ux * ux + uy * uy)) * inv_dl
+                                 : (T(2) * (ref.x * ux + ref.y * uy) + (ux * ux + uy * uy)) / (d + l0);
+    const T tensile = sizeof(T) == 4 ? ext * inv_l0 : ext / l0;
     const T shear = T(0.5) * (si + in.sj);
     const T sf = in.sf;
     const bool bt = exceeds<T>(tensile, P.eps_t, P.eps_t_lo, P.eps_t_hi, sf);
@@ -432,8 +462,8 @@ __device__ __forceinline__ void do_bond(const Params<T>& P, const Bufs<T>& B, in
       }
       us = V2<T>{T(0), T(0)};  // the contact starts without tangential history
     } else if (va.w + vb.w > T(0)) {
-      const T nx = g.dx / d, ny = g.dy / d;
-      const T meff = T(1) / (va.w + vb.w);
+      const T nx = sizeof(T) == 4 ? g.dx * inv_d : g.dx / d;
+      const T ny = sizeof(T) == 4 ? g.dy * inv_d : g.dy / d;
       const T wsum = va.z * a.z + vb.z * b.z;
       const T vrx = (va.x - vb.x) - wsum * ny;
       const T vry = (va.y - vb.y) + wsum * nx;
@@ -443,8 +473,16 @@ __device__ __forceinline__ void do_bond(const Params<T>& P, const Bufs<T>& B, in
       const T sn = sx * nx + sy * ny;
       sx -= sn * nx;
       sy -= sn * ny;
-      const T cn = T(2) * P.bzeta * dev_sqrt(P.kn * meff);
-      const T cs = T(2) * P.bzeta * dev_sqrt(P.ks * meff);
+      T cn, cs;
+      if constexpr (sizeof(T) == 4) {
+        const T rm = rsqrtf(va.w + vb.w);  // sqrt(m*)
+        cn = P.cn_k * rm;
+        cs = P.cs_k * rm;
+      } else {
+        const T meff = T(1) / (va.w + vb.w);
+        cn = T(2) * P.bzeta * dev_sqrt(P.kn * meff);
+        cs = T(2) * P.bzeta * dev_sqrt(P.ks * meff);
+      }
       const T fnm = P.kn * ext - cn * vn;
       const T fax = fnm * nx - P.ks * sx - cs * vtx;
       const T fay = fnm * ny - P.ks * sy - cs * vty;
@@ -1412,6 +1450,8 @@ inline void make_params(const tdem_hm_config& c, int slots, Params<T>& P) {
   P.kn = (T)c.bond_kn;
   P.ks = (T)c.bond_ks;
   P.bzeta = (T)c.bond_damping;
+  P.cn_k = (T)(2.0 * c.bond_damping * std::sqrt(c.bond_kn));
+  P.cs_k = (T)(2.0 * c.bond_damping * std::sqrt(c.bond_ks));
   P.eps_t = c.breaking_strain;
   P.eps_s = c.shear_breaking_strain;
   P.ind_x0 = c.indenter_center[0];
