@@ -59,6 +59,23 @@ def _dist():
     return world, rank, local
 
 
+def max_over_ranks(value: float, device) -> float:
+    """The largest value over all ranks (the slowest rank's time); the value
+    itself when no process group is running."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world: int, units_per_rank: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput: every rank's units over the slowest rank's time."""
+    return world * units_per_rank * steps / seconds
+
+
 def workload_config(seed: int = 0) -> dict:
     return {"workload": "2-D polydisperse Hertz-Mindlin disc settling, 1,048,576 discs "
                         "(1024x1024 jittered grid, area fraction 0.55, 4 walls, gravity), "
@@ -239,15 +256,13 @@ def run_ours(a) -> None:
     kernel_ms = sum(step_ms) / len(step_ms)
     total_ms = sum(step_ms) + sum(rebuild_ms)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, dev)
         torch.distributed.barrier()
     led1 = eng.ledger()
     rebuilds = led1["rebuilds"] - led0["rebuilds"]
     clk = clocks.summary()
     n = cfg.n
-    value = world * n * a.steps / (total_ms / 1e3)
+    value = aggregate_rate(world, n, a.steps, total_ms / 1e3)
 
     # contacts touching at the end of the run (for the algorithmic byte count)
     hist = eng.history()
@@ -276,12 +291,10 @@ def run_ours(a) -> None:
     e2e_s = time.perf_counter() - t0
     e2e_eng.check()
     if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, dev)
     h2d = 8 * n * (2 + 2 + 1 + 1 + 1 + 1)
     d2h = 8 * n * (2 + 2 + 1)
-    e2e = {"value": world * n * a.steps / e2e_s, "unit": UNIT,
+    e2e = {"value": aggregate_rate(world, n, a.steps, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
            "note": "one solve through tdem_hm_set_state/step/read_state with host arrays: upload, "
                    f"{a.steps} steps, download; L2 flushed before it"}

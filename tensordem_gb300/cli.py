@@ -150,6 +150,44 @@ def _cmd_hm2d(args: argparse.Namespace) -> None:
                       "particle_steps_per_s": cfg.n * args.steps / dt, "ledger": led}))
 
 
+def _cmd_scale(args: argparse.Namespace) -> None:
+    """Step-kernel time against disc count: plain launches between CUDA events
+    on the engine's stream, L2 flushed before each (one buffer larger than L2
+    written, another read), list rebuilds outside the brackets."""
+    from .hm2d import HM2D, granular_gas_case
+
+    dev = torch.device("cuda", 0)
+    flush_w = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    flush_r = torch.ones(64 << 20, dtype=torch.float32, device=dev)
+    rows = []
+    for side in args.sides:
+        cfg, st = granular_gas_case(side, seed=args.seed)
+        eng = HM2D(cfg, device=dev)
+        eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
+        for v in args.variants:
+            eng.variant = v
+            eng.step(5)
+            times = []
+            stream = torch.cuda.current_stream(dev)
+            for _ in range(args.repeats):
+                flush_w.fill_(1.0)
+                flush_r.sum()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                eng.step_kernel()
+                e1.record(stream)
+                if eng.rebuild_pending():
+                    eng.rebuild()
+                torch.cuda.synchronize(dev)
+                times.append(e0.elapsed_time(e1) * 1e3)
+            times.sort()
+            med = times[len(times) // 2]
+            rows.append({"discs": cfg.n, "variant": v, "us_median": med, "us_min": times[0],
+                         "alg_GBs": cfg.n * 80 / (med * 1e-6) / 1e9})
+            print(json.dumps(rows[-1]), flush=True)
+        del eng
+
+
 def _cmd_ensemble(args: argparse.Namespace) -> None:
     import os
 
@@ -202,6 +240,12 @@ def main(argv: list[str] | None = None) -> None:
     h.add_argument("--autotune", action="store_true")
     h.add_argument("--no-graph", action="store_true", help="plain launches (visible to profilers)")
     h.set_defaults(func=_cmd_hm2d)
+    sc = sub.add_parser("scale", help="step-kernel time against disc count (L2 flushed per launch)")
+    sc.add_argument("--sides", type=int, nargs="+", default=[362, 512, 724, 1024, 1448, 2048])
+    sc.add_argument("--variants", type=int, nargs="+", default=[1])
+    sc.add_argument("--repeats", type=int, default=100)
+    sc.add_argument("--seed", type=int, default=0)
+    sc.set_defaults(func=_cmd_scale)
     en = sub.add_parser("ensemble", help="mixed ensemble of 2-D runs: batched engine vs one-by-one FP64")
     en.add_argument("--instances", type=int, default=4096)
     en.add_argument("--steps", type=int, default=5000)

@@ -1,0 +1,53 @@
+"""Replica bench on several ranks: the host-side reduction, on CPU with gloo.
+
+The GB300 path runs one replica per rank (the path does not shard); the bench
+line reports every rank's discs over the slowest rank's time. Two gloo ranks
+check that reduction and the aggregate formula without a GPU.
+"""
+
+import os
+import socket
+
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank: int, world: int, port: int, out) -> None:
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    try:
+        w, r, _ = bench._dist()
+        assert (w, r) == (world, rank)
+        slowest = bench.max_over_ranks(1.0 + rank, "cpu")  # rank 1 is the slow one
+        rate = bench.aggregate_rate(w, 1000, 10, slowest)
+        out.put((rank, slowest, rate))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_ranks_report_aggregate_over_the_slowest_rank():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=5) for _ in range(2))
+    assert [g[1] for g in got] == [2.0, 2.0]
+    assert all(abs(g[2] - 2 * 1000 * 10 / 2.0) < 1e-9 for g in got)
+
+
+def test_single_process_reduction_is_identity():
+    import bench
+    assert bench.max_over_ranks(3.5, "cpu") == 3.5
+    assert bench.aggregate_rate(1, 100, 10, 2.0) == 500.0
