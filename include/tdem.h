@@ -266,6 +266,13 @@ int tdem_hm_read_bonds(tdem_hm* h, int32_t* pairs, int32_t* state, int64_t capac
  * up to load_capacity evaluations, into out ((capacity, 2) double, host). */
 int tdem_hm_read_load(tdem_hm* h, double* out, int64_t capacity, int64_t* count, void* stream);
 
+/* Fragments: connected components of the intact bonds (isolated discs are
+ * fragments of one). labels (n, host int32, original order) receives each
+ * disc's fragment label, the smallest original id in its fragment; count the
+ * number of fragments. Replaces IceDEM.fragments' host search
+ * (src/tensordem/dem.py:462-484) with a device union-find. Synchronizes. */
+int tdem_hm_fragments(tdem_hm* h, int32_t* labels, int64_t* count, void* stream);
+
 /* Synchronize and map the device status: TDEM_ERR_NONFINITE, TDEM_ERR_CAPACITY. */
 int tdem_hm_status(tdem_hm* h, void* stream);
 

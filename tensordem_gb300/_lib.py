@@ -132,6 +132,7 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_hm_set_bonds": (i32, [vp, vp, vp, C.c_int64, vp]),
         "tdem_hm_read_bonds": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_hm_read_load": (i32, [vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
+        "tdem_hm_fragments": (i32, [vp, vp, C.POINTER(C.c_int64), vp]),
         "tdem_hm_rebuild_pending": (i32, [vp, vp]),
         "tdem_hm_set_variant": (i32, [vp, i32]),
         "tdem_hm_get_variant": (i32, [vp]),

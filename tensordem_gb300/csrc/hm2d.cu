@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -51,6 +52,7 @@ struct EngineBase {
   virtual int set_bonds(const int* pairs, const double* strength, long long count, cudaStream_t s) = 0;
   virtual int read_bonds(int* pairs, int* state, long long capacity, long long* count, cudaStream_t s) = 0;
   virtual int read_load(double* out, long long capacity, long long* count, cudaStream_t s) = 0;
+  virtual int fragments(int* labels, long long* count, cudaStream_t s) = 0;
   virtual int step_kernel(cudaStream_t s) = 0;
   virtual int rebuild_pending(cudaStream_t s) = 0;
   virtual int get_variant() const = 0;
@@ -122,6 +124,70 @@ __global__ void bonds_out_kernel(Params<T> P, Bufs<T> B, int* pairs, int* state,
     state[2 * e] = (w & kBondBroken) ? (int)((w >> kBondModeShift) & 3u) : 0;  // 0 intact, else mode
     state[2 * e + 1] = B.bfail[lp][k];
   }
+}
+
+// Fragments: connected components of the intact bond graph. Every root
+// points to itself; a hook links the larger of two roots under the smaller
+// one (parents only ever decrease), so the final root of a component is its
+// smallest sorted index. Path halving during finds is a benign race for the
+// same reason.
+__device__ __forceinline__ int cc_find(int* parent, int x) {
+  int p = parent[x];
+  while (p != x) {
+    const int gp = parent[p];
+    if (gp != p) parent[x] = gp;
+    x = p;
+    p = gp;
+  }
+  return x;
+}
+
+template <class T>
+__global__ void cc_init_kernel(Params<T> P, int* parent, int* label) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  parent[i] = i;
+  label[i] = INT_MAX;
+}
+
+template <class T>
+__global__ void cc_hook_kernel(Params<T> P, Bufs<T> B, int* parent, int* changed) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const int lp = B.ctl->lp;
+  const int bc = B.bcnt[lp][i];
+  for (int s = 0; s < bc; ++s) {
+    const unsigned w = B.bpart[lp][(size_t)s * P.n + i];
+    if (w & kBondBroken) continue;
+    const int j = (int)(w & kBondIdx);
+    if (j <= i) continue;  // each bond once
+    const int ri = cc_find(parent, i), rj = cc_find(parent, j);
+    if (ri != rj) {
+      atomicMin(&parent[max(ri, rj)], min(ri, rj));
+      *changed = 1;
+    }
+  }
+}
+
+template <class T>
+__global__ void cc_compress_kernel(Params<T> P, int* parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < P.n) parent[i] = cc_find(parent, i);
+}
+
+// Label of a component: its smallest original id; count the roots.
+template <class T>
+__global__ void cc_label_kernel(Params<T> P, Bufs<T> B, const int* parent, int* label, unsigned long long* roots) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  atomicMin(&label[parent[i]], B.orig[B.ctl->lp][i]);
+  if (parent[i] == i) atomicAdd(roots, 1ull);
+}
+
+template <class T>
+__global__ void cc_out_kernel(Params<T> P, Bufs<T> B, const int* parent, const int* label, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < P.n) out[B.orig[B.ctl->lp][i]] = label[parent[i]];
 }
 
 // The rebuild pipeline (every kernel a no-op unless ctl->rebuild_pending).
@@ -671,6 +737,51 @@ struct Engine final : EngineBase {
     return TDEM_OK;
   }
 
+  // Fragment label (smallest original id of the fragment) of every disc, in
+  // original order, and the number of fragments (isolated discs included).
+  int fragments(int* labels, long long* count, cudaStream_t s) override {
+    if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "fragments before set_state");
+    const size_t n = (size_t)P.n;
+    int *parent = nullptr, *label = nullptr, *out = nullptr, *changed = nullptr;
+    unsigned long long* roots = nullptr;
+    TDEM_CUDA_TRY(&err, cudaMallocAsync(&parent, n * sizeof(int), s));
+    TDEM_CUDA_TRY(&err, cudaMallocAsync(&label, n * sizeof(int), s));
+    TDEM_CUDA_TRY(&err, cudaMallocAsync(&out, n * sizeof(int), s));
+    TDEM_CUDA_TRY(&err, cudaMallocAsync(&changed, sizeof(int), s));
+    TDEM_CUDA_TRY(&err, cudaMallocAsync(&roots, sizeof(unsigned long long), s));
+    cc_init_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, parent, label);
+    int rc = TDEM_OK;
+    bool done = P.BMAX == 0;
+    // hooking with pointer jumping converges in a few rounds; the bound only
+    // guards the host loop
+    for (int it = 0; it < 256 && !done; ++it) {
+      int h_changed = 0;
+      TDEM_CUDA_TRY(&err, cudaMemsetAsync(changed, 0, sizeof(int), s));
+      cc_hook_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, parent, changed);
+      cc_compress_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, parent);
+      TDEM_CUDA_TRY(&err, cudaMemcpyAsync(&h_changed, changed, sizeof(int), cudaMemcpyDeviceToHost, s));
+      TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
+      done = h_changed == 0;
+    }
+    if (!done) rc = tdem::fail(&err, TDEM_ERR_CUDA, "fragment labelling did not converge");
+    unsigned long long h_roots = 0;
+    if (!rc) {
+      TDEM_CUDA_TRY(&err, cudaMemsetAsync(roots, 0, sizeof(unsigned long long), s));
+      cc_label_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, parent, label, roots);
+      cc_out_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, parent, label, out);
+      TDEM_CUDA_TRY(&err, cudaMemcpyAsync(labels, out, n * sizeof(int), cudaMemcpyDeviceToHost, s));
+      TDEM_CUDA_TRY(&err, cudaMemcpyAsync(&h_roots, roots, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    }
+    cudaFreeAsync(parent, s);
+    cudaFreeAsync(label, s);
+    cudaFreeAsync(out, s);
+    cudaFreeAsync(changed, s);
+    cudaFreeAsync(roots, s);
+    TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
+    if (count) *count = (long long)h_roots;
+    return rc;
+  }
+
   int read_bonds(int* pairs, int* state, long long capacity, long long* count, cudaStream_t s) override {
     if (P.BMAX <= 0) {
       *count = 0;
@@ -901,6 +1012,14 @@ int tdem_hm_read_bonds(tdem_hm* h, int32_t* pairs, int32_t* state, int64_t capac
   long long c = 0;
   const int rc = h->e->read_bonds(pairs, state, (long long)capacity, &c, reinterpret_cast<cudaStream_t>(stream));
   *count = (int64_t)c;
+  return rc;
+}
+
+int tdem_hm_fragments(tdem_hm* h, int32_t* labels, int64_t* count, void* stream) {
+  if (!h || !labels) return TDEM_ERR_BADARG;
+  long long c = 0;
+  const int rc = h->e->fragments(labels, &c, reinterpret_cast<cudaStream_t>(stream));
+  if (count) *count = (int64_t)c;
   return rc;
 }
 

@@ -307,29 +307,33 @@ __global__ void strain_kernel(Params<T> P, Bufs<T> B) {
       const V4<T>* pos = B.pos[sp];
       const V4<T> p = pos[i];
       T g00 = 0, g01 = 0, g10 = 0, g11 = 0;
-      // all slot words, then all partner positions, then the sums (in slot order)
-      unsigned w[kMaxBondSlots];
+      // four slots at a time: their slot words, then their partner positions,
+      // then the sums (in slot order)
+      constexpr int KS = 4;
+      for (int s0 = 0; s0 < bc; s0 += KS) {
+        unsigned w[KS];
 #pragma unroll
-      for (int s = 0; s < kMaxBondSlots; ++s)
-        if (s < bc) w[s] = B.bpart[lp][(size_t)s * P.n + i];
-      V4<T> q[kMaxBondSlots];
-      V2<T> r[kMaxBondSlots];
+        for (int u = 0; u < KS; ++u)
+          if (s0 + u < bc) w[u] = B.bpart[lp][(size_t)(s0 + u) * P.n + i];
+        V4<T> q[KS];
+        V2<T> r[KS];
 #pragma unroll
-      for (int s = 0; s < kMaxBondSlots; ++s) {
-        if (s < bc) {
-          q[s] = pos[(int)(w[s] & kBondIdx)];
-          r[s] = B.bref[lp][(size_t)s * P.n + i];
+        for (int u = 0; u < KS; ++u) {
+          if (s0 + u < bc) {
+            q[u] = pos[(int)(w[u] & kBondIdx)];
+            r[u] = B.bref[lp][(size_t)(s0 + u) * P.n + i];
+          }
         }
-      }
 #pragma unroll
-      for (int s = 0; s < kMaxBondSlots; ++s) {
-        if (s < bc) {
-          const V2<T> cur = cell_delta<T>(Q, p, q[s]);
-          const T ux = cur.x - r[s].x, uy = cur.y - r[s].y;
-          g00 += ux * r[s].x;
-          g01 += ux * r[s].y;
-          g10 += uy * r[s].x;
-          g11 += uy * r[s].y;
+        for (int u = 0; u < KS; ++u) {
+          if (s0 + u < bc) {
+            const V2<T> cur = cell_delta<T>(Q, p, q[u]);
+            const T ux = cur.x - r[u].x, uy = cur.y - r[u].y;
+            g00 += ux * r[u].x;
+            g01 += ux * r[u].y;
+            g10 += uy * r[u].x;
+            g11 += uy * r[u].y;
+          }
         }
       }
       const V4<T> pi = B.bpinv[lp][i];
@@ -597,7 +601,7 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
     const int bc = B.bcnt[lp][i];
     if (bc > 0) {
       const T si = B.strain[i];
-      constexpr int KB = 3;  // bond slots whose loads are in flight together
+      constexpr int KB = 2;  // bond slots whose loads are in flight together
       for (int s0 = 0; s0 < bc; s0 += KB) {
         BondIn<T> in[KB];
 #pragma unroll

@@ -25,6 +25,7 @@ import json
 import math
 from dataclasses import asdict, dataclass
 
+import numpy as np
 import torch
 
 from . import _lib, ops
@@ -432,27 +433,23 @@ class IceDEM:
         return events
 
     def fragments(self) -> list[dict]:
-        """Connected components of surviving bonds, including isolated disks (dem.py:462-484)."""
+        """Connected components of the surviving bonds, isolated discs included,
+        ordered by their smallest particle id (the output of dem.py:462-484):
+        particle ids, mass, centroid and mean velocity per fragment."""
+        from scipy.sparse import coo_matrix
+        from scipy.sparse.csgraph import connected_components
+
         n = len(self.positions)
-        neighbors = [set() for _ in range(n)]
-        for i, j in self.pairs[self.alive].tolist():
-            neighbors[i].add(j)
-            neighbors[j].add(i)
+        ij = self.pairs[self.alive].cpu().numpy().reshape(-1, 2)
+        graph = coo_matrix((np.ones(len(ij)), (ij[:, 0], ij[:, 1])), shape=(n, n))
+        _, label = connected_components(graph, directed=False)
         pos = self.positions.cpu()
         vel = self.velocities.cpu()
-        unseen = set(range(n))
+        members: dict[int, list[int]] = {}
+        for i, c in enumerate(label.tolist()):  # ascending i: member lists come out sorted
+            members.setdefault(c, []).append(i)
         result = []
-        while unseen:
-            todo = [min(unseen)]
-            component = []
-            unseen.remove(todo[0])
-            while todo:
-                i = todo.pop()
-                component.append(i)
-                for j in sorted(neighbors[i] & unseen):
-                    unseen.remove(j)
-                    todo.append(j)
-            ids = sorted(component)
+        for ids in sorted(members.values(), key=lambda m: m[0]):
             result.append(dict(particle_ids=ids, mass_kg=len(ids) * self.config.mass,
                                centroid_m=pos[ids].mean(0).tolist(),
                                mean_velocity_m_s=vel[ids].mean(0).tolist()))

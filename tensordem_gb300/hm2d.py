@@ -347,6 +347,19 @@ class HM2D:
         return dict(pairs=pairs[:m][order].astype(np.int64), mode=state[:m, 0][order],
                     fail_eval=state[:m, 1][order])
 
+    def fragments(self) -> dict:
+        """Connected components of the intact bonds, computed on the device:
+        per-disc labels (the smallest original id of its fragment, original
+        order), the fragment count, and each fragment's size."""
+        n = self.config.n
+        labels = np.empty(n, dtype=np.int32)
+        count = C.c_int64()
+        with torch.cuda.device(self.device):
+            rc = self._lib.tdem_hm_fragments(self._h, labels.ctypes.data, C.byref(count), self._stream())
+        _lib.check(rc, self._h, "tdem_hm_fragments")
+        ids, sizes = np.unique(labels, return_counts=True)
+        return {"labels": labels, "count": int(count.value), "fragment_ids": ids, "sizes": sizes}
+
     def load_curve(self) -> np.ndarray:
         """Indenter reaction (ice on indenter) per committed evaluation, (E, 2)."""
         cap = max(self.config.load_capacity, 1)

@@ -137,3 +137,42 @@ def test_full_size_ice_sheet_builds_and_steps(hm):
     led = e.ledger()
     assert led["status"] == 0 and led["evals"] == 20
     assert len(e.bonds()["pairs"]) == len(bonds)
+
+
+def _components(n, pairs):
+    """Union-find over bond pairs, labels = smallest id of the component."""
+    parent = list(range(n))
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+    for a, b in pairs:
+        ra, rb = find(int(a)), find(int(b))
+        if ra != rb:
+            parent[max(ra, rb)] = min(ra, rb)
+    roots = [find(i) for i in range(n)]
+    low = {}
+    for i, r in enumerate(roots):
+        low[r] = min(low.get(r, i), i)
+    return np.array([low[r] for r in roots])
+
+
+def test_device_fragments_match_the_surviving_bond_graph(hm):
+    cfg, st, bonds, strength = small_sheet(24, 8, precision=64, steps=400, speed=20.0)
+    e = _engine(hm, cfg, st, bonds, strength)
+    o = bonded_oracle_for(cfg, st, bonds, strength)
+    before = e.fragments()
+    assert before["count"] == 1 and (before["labels"] == 0).all()
+    e.step(300)
+    o.step(299)
+    got = e.fragments()
+    table = e.bonds()
+    intact = table["pairs"][table["mode"] == 0]
+    want = _components(cfg.n, intact)
+    assert np.array_equal(got["labels"], want)
+    assert got["count"] == len(np.unique(want)) and got["count"] > 1
+    # and the oracle's surviving bonds give the same fragments
+    opairs = np.stack((o.bi, o.bj), axis=1)[o.alive]
+    assert np.array_equal(_components(cfg.n, opairs), want)

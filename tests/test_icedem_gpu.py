@@ -180,3 +180,23 @@ def test_snapshot_round_trip(tdem):
     assert torch.equal(sim.alive, other.alive)
     assert sim.accounting_vector() == other.accounting_vector()
     assert other.exchange_state()["schema"] == "tensordem.exchange/1"
+
+
+def test_fragments_partition_the_surviving_bond_graph():
+    """fragments() (dem.py:462-484 output): components of the surviving bonds,
+    isolated discs included, ordered by their smallest particle id."""
+    import tensordem_gb300 as tdem
+    sim = tdem.IceDEM(tdem.DEMConfig(nx=21, ny=5, breaking_strain=0.01, shear_breaking_strain=0.02))
+    sim.run(2000)
+    frags = sim.fragments()
+    n = len(sim.positions)
+    seen = sorted(i for f in frags for i in f["particle_ids"])
+    assert seen == list(range(n))
+    assert [f["particle_ids"][0] for f in frags] == sorted(f["particle_ids"][0] for f in frags)
+    label = np.empty(n, dtype=int)
+    for k, f in enumerate(frags):
+        label[f["particle_ids"]] = k
+        assert abs(f["mass_kg"] - len(f["particle_ids"]) * sim.config.mass) < 1e-12
+    pairs = sim.pairs[sim.alive].cpu().numpy()
+    assert (label[pairs[:, 0]] == label[pairs[:, 1]]).all()  # no surviving bond crosses fragments
+    assert len(frags) > 1
