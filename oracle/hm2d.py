@@ -37,13 +37,21 @@ slip loss ``mu F_n (|xi_trial| - |xi|)`` per contact and step
 (granular2d/engine.py:489-496, 576-588); elastic energies ``0.4 F_el delta``
 (Hertz) and ``0.5 S_t |xi|^2`` (scale_ceiling/kernel.py:461-487).
 
-Parity is pinned by known-answer tests on the reference's own anchors
-(tests/test_oracle_hm2d.py): k_t/k_n ratios (tests/test_hertz_mindlin.py), the
-restitution-to-damping map (tests/test_contact_tangential.py:73-83), the
-Coulomb stick/slip cycle area and brute-force pair sets
-(tests/test_scale_ceiling_dem.py:41-80). The full 2-D assembled step has no
-reference implementation to run, so beyond those anchors its parity is
-"unpinned" against a reference executable.
+Parity is pinned two ways.
+* Known-answer tests on the reference's own anchors (tests/test_oracle_hm2d.py):
+  k_t/k_n ratios (tests/test_hertz_mindlin.py), the restitution-to-damping map
+  (tests/test_contact_tangential.py:73-83), the Coulomb stick/slip cycle area
+  and brute-force pair sets (tests/test_scale_ceiling_dem.py:41-80).
+* A trajectory of the reference's own FP64 engine, FloeBed
+  (scale_ceiling/kernel.py:155-455), on a planar frictionless bed
+  (tests/golden/floebed_planar.npz, tests/test_floebed_golden.py). This oracle
+  reproduces it to 1e-14 (positions) after 200 steps: the Hertz normal law,
+  the dashpot on the half-step velocity, walls, gravity and velocity-Verlet
+  of the assembled step are pinned against a reference executable.
+The tangential history has no reference engine with this module's
+conventions: FloeBed keeps an unprojected history for separated pairs still in
+its list, and it has no rotation. Friction and rotation are pinned only by
+the anchors above.
 """
 
 from __future__ import annotations
