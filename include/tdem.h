@@ -131,6 +131,13 @@ void tdem_icedem_destroy(tdem_icedem* h);
 int tdem_icedem_num_bonds(const tdem_icedem* h);
 int tdem_icedem_bond_pairs(const tdem_icedem* h, int64_t* out_pair_index_host);
 
+/* Per-bond central-spring stiffness (host, one value per bond in bond order,
+ * each finite, > 0 and <= cfg.bond_stiffness). Every later evaluation adds,
+ * after the base force, (k_b - k) (d - L0) n on each surviving bond and books
+ * the actual spring energy of a bond when it breaks. Replaces the force and
+ * energy overrides of CalibratedIceDEM (src/tensordem/calibrated_dem.py:11-93). */
+int tdem_icedem_set_bond_stiffness(tdem_icedem* h, const double* k_host, int count);
+
 /* One force evaluation at `time`: commits breaks and their ledger entries and
  * writes the total force (n,2) and the ice-on-tool reaction (2) to device
  * buffers. `loads` is an optional (n,2) device array of external nodal

@@ -109,7 +109,7 @@ class IceDEMOracle:
                     "tool_impulse_on_ice_Ns")
 
     def __init__(self, config: OracleConfig = OracleConfig(), *, hull_profile=None,
-                 hull_start=(0.0, 0.0), hull_velocity=(0.0, 0.0)):
+                 hull_start=(0.0, 0.0), hull_velocity=(0.0, 0.0), bond_stiffness=None):
         cfg = config
         self.config = cfg
         # dem.py:100-104
@@ -159,6 +159,15 @@ class IceDEMOracle:
         self.hull_profile = None if hull_profile is None else np.asarray(hull_profile, np.float64)
         self.hull_start = np.asarray(hull_start, np.float64)
         self.hull_velocity = np.asarray(hull_velocity, np.float64)
+        # per-bond stiffness (calibrated_dem.py:20-42): None = the config's for every bond
+        self.pair_coefficients = None
+        if bond_stiffness is not None:
+            k = np.asarray(bond_stiffness, np.float64)
+            if k.shape != (len(self.bond_indices),) or not np.isfinite(k).all() or (k <= 0).any() \
+                    or (k > cfg.bond_stiffness).any():
+                raise ValueError("per-bond stiffness shape/finite/positive/conservative upper bound mismatch")
+            self.pair_coefficients = np.zeros(len(self.pairs))
+            self.pair_coefficients[self.bonded] = k
 
     # dem.py:171-176
     @property
@@ -266,6 +275,17 @@ class IceDEMOracle:
         force = force + tool_force
         if external_forces is not None:
             force = force + external_forces
+        if self.pair_coefficients is not None:
+            # calibrated_dem.py:62-84: (k_b - k) (d - L0) n on the surviving
+            # bonds, added after the base force (i side, then j side), and the
+            # actual spring energy of the bonds broken in this evaluation
+            difference = self.pair_coefficients - cfg.bond_stiffness
+            correction = (difference * extension * self.alive)[:, None] * normal
+            np.add.at(force, i, correction)
+            np.add.at(force, j, -correction)
+            energy_correction = 0.5 * difference[newly] * extension[newly] ** 2
+            self.accounting["fracture_release_J"] += float(energy_correction.sum())
+            self.failure_energy_J[newly] += energy_correction
         return force, tool_reaction
 
     def step(self, external_forces=None, *, load_time=None):
@@ -309,7 +329,10 @@ class IceDEMOracle:
         dist = np.sqrt((delta * delta).sum(axis=1))
         ext = dist - self.rest_lengths
         overlap = np.maximum(2 * cfg.radius - dist, 0.0)
-        bond = 0.5 * cfg.bond_stiffness * (ext[self.alive] ** 2).sum()
+        if self.pair_coefficients is None:
+            bond = 0.5 * cfg.bond_stiffness * (ext[self.alive] ** 2).sum()
+        else:  # calibrated_dem.py:86-93
+            bond = 0.5 * (self.pair_coefficients[self.alive] * ext[self.alive] ** 2).sum()
         contact = 0.5 * cfg.contact_stiffness * (overlap[~self.alive] ** 2).sum()
         d = np.sqrt(((self.positions - self.tool_position) ** 2).sum(axis=1))
         tool_ov = np.maximum(cfg.radius + cfg.tool_radius - d, 0.0)

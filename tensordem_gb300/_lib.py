@@ -112,6 +112,7 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_icedem_destroy": (None, [vp]),
         "tdem_icedem_num_bonds": (i32, [vp]),
         "tdem_icedem_bond_pairs": (i32, [vp, C.POINTER(C.c_int64)]),
+        "tdem_icedem_set_bond_stiffness": (i32, [vp, C.POINTER(C.c_double), i32]),
         "tdem_icedem_forces": (i32, [vp, C.POINTER(IceDEMStateC), vp, dbl, vp, vp, vp]),
         "tdem_icedem_step": (i32, [vp, C.POINTER(IceDEMStateC), vp, i32, dbl, vp]),
         "tdem_icedem_steps_done": (i32, [vp]),

@@ -56,6 +56,7 @@ struct Topo {
   const int* inc_other;   // (2B) partner disc of that bond
   const Mat2* pinv;       // (n) pseudo-inverse of the bond covariance (row major)
   const double2* hull;    // (hull_m) local hull vertices
+  const double* kcoef;    // (B) per-bond stiffness (N/m), or null: the config's stiffness for every bond
 };
 
 struct Mailbox {
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
     __syncthreads();
 
     // ---- phase 2: break test and irreversible commit (dem.py:243-277)
-    double brk[2] = {0.0, 0.0};  // released, acquired
+    double brk[3] = {0.0, 0.0, 0.0};  // released, acquired, per-bond stiffness correction
     int any_break = 0;
     for (int b = tid; b < P.nbond; b += nt) {
       const long long p = T.bpair[b];
@@ -238,6 +239,13 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
         S.failure_extension_m[p] = ext;
         const double energy = (0.5 * P.kb) * (ext * ext);
         S.failure_energy_J[p] = energy;
+        if (T.kcoef) {
+          // per-bond stiffness: the released energy of the actual spring law
+          // (calibrated_dem.py:80-84), booked after the base energy
+          const double corr = (0.5 * (T.kcoef[b] - P.kb)) * (ext * ext);
+          S.failure_energy_J[p] = energy + corr;
+          brk[2] += corr;
+        }
         const double ov = fmax(two_r - d, 0.0);
         brk[0] += energy;
         brk[1] += (0.5 * P.kc) * (ov * ov);
@@ -247,11 +255,12 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
       }
     }
     if (__syncthreads_or(any_break)) {
-      double tot[2];
-      block_sum_f64<2>(brk, red, tot);
+      double tot[3];
+      block_sum_f64<3>(brk, red, tot);
       if (tid == 0) {
         ledger[TDEM_L_FRACTURE_RELEASE] += tot[0];
         ledger[TDEM_L_CONTACT_ACQUIRED] += tot[1];
+        if (T.kcoef) ledger[TDEM_L_FRACTURE_RELEASE] += tot[2];
       }
     }
     __syncthreads();
@@ -333,6 +342,41 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
         acc[6] += L.x;
         acc[7] += L.y;
         acc[11] += pk.x * L.y - pk.y * L.x;
+      }
+      if (T.kcoef) {
+        // per-bond stiffness (calibrated_dem.py:70-79): after the base force,
+        // (k_b - k) * extension * n on each surviving bond, first the bonds
+        // where this disc is i (ascending j), then those where it is j
+        // (ascending i), which is the order of the incidence list
+        for (int e = T.inc_off[k]; e < T.inc_off[k + 1]; ++e) {
+          const int b = T.inc_bond[e];
+          if (!S.alive[T.bpair[b]]) continue;
+          const int j = T.inc_other[e];
+          const int lo = k < j ? k : j;
+          const int hi = k < j ? j : k;
+          const double dx = spos[hi].x - spos[lo].x;
+          const double dy = spos[hi].y - spos[lo].y;
+          const double d = sqrt(dx * dx + dy * dy);
+          double nx, ny;
+          if (d > 0.0) {
+            const double dcl = fmax(d, eps);
+            nx = dx / dcl;
+            ny = dy / dcl;
+          } else {
+            const double ix = gpos0[hi].x - gpos0[lo].x, iy = gpos0[hi].y - gpos0[lo].y;
+            const double id = sqrt(ix * ix + iy * iy);
+            nx = ix / id;
+            ny = iy / id;
+          }
+          const double m = (T.kcoef[b] - P.kb) * (d - T.rest[b]);
+          if (k == lo) {
+            fx += m * nx;
+            fy += m * ny;
+          } else {
+            fx += -(m * nx);
+            fy += -(m * ny);
+          }
+        }
       }
       sforce[k] = make_double2(fx, fy);
       if (S.fixed[k]) {
@@ -464,6 +508,7 @@ struct tdem_icedem {
   double2* ref = nullptr;
   tdem::icedem::Mat2* pinv = nullptr;
   double2* hull = nullptr;
+  double* kcoef = nullptr;  // per-bond stiffness, null unless set
   double* ledger = nullptr;
   tdem::icedem::Mailbox* mbox = nullptr;
   tdem::icedem::Mailbox* mbox_host = nullptr;
@@ -548,6 +593,7 @@ void tdem_icedem_destroy(tdem_icedem* h) {
   cudaFree(h->ref);
   cudaFree(h->pinv);
   cudaFree(h->hull);
+  cudaFree(h->kcoef);
   cudaFree(h->ledger);
   cudaFree(h->mbox);
   cudaFreeHost(h->mbox_host);
@@ -689,6 +735,22 @@ int tdem_icedem_create(const tdem_icedem_config* cfg, const double* x0, tdem_ice
 
 int tdem_icedem_num_bonds(const tdem_icedem* h) { return h ? h->nbond : -1; }
 
+int tdem_icedem_set_bond_stiffness(tdem_icedem* h, const double* k_host, int count) {
+  if (!h || !k_host) return TDEM_ERR_BADARG;
+  if (count != h->nbond)
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "per-bond stiffness count must equal the number of bonds");
+  for (int b = 0; b < count; ++b)
+    if (!(std::isfinite(k_host[b]) && k_host[b] > 0.0 && k_host[b] <= h->P.kb))
+      return tdem::fail(&h->err, TDEM_ERR_BADARG,
+                        "per-bond stiffness must be finite, positive and at most the config's bond stiffness");
+  std::vector<double> k(k_host, k_host + count);
+  if (h->kcoef) {
+    cudaFree(h->kcoef);
+    h->kcoef = nullptr;
+  }
+  return upload(&h->err, &h->kcoef, k);
+}
+
 int tdem_icedem_bond_pairs(const tdem_icedem* h, int64_t* out) {
   if (!h || !out) return TDEM_ERR_BADARG;
   std::memcpy(out, h->bpair_host.data(), h->bpair_host.size() * sizeof(int64_t));
@@ -702,7 +764,8 @@ static int launch(tdem_icedem* h, const tdem_icedem_state* st, const double* loa
       !st->alive || !st->failure_mode || !st->failure_time_s || !st->failure_extension_m ||
       !st->failure_energy_J)
     return tdem::fail(&h->err, TDEM_ERR_BADARG, "state pointer missing");
-  Topo T{h->bi, h->bj, h->bpair, h->rest, h->ref, h->inc_off, h->inc_bond, h->inc_other, h->pinv, h->hull};
+  Topo T{h->bi, h->bj, h->bpair, h->rest, h->ref, h->inc_off, h->inc_bond, h->inc_other, h->pinv, h->hull,
+         h->kcoef};
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   icedem_kernel<<<1, h->threads, h->smem, s>>>(h->P, T, *st, reinterpret_cast<const double2*>(loads),
                                                mode, n_steps, time,

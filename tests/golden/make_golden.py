@@ -18,6 +18,8 @@ Cases:
 * ``loads_5x3``: seeded external nodal loads, stepped with ``load_time``.
 * ``unit_*``: single ``forces()`` evaluations on hand-edited states taken from
   ``tests/test_dem.py`` (shear, tension, compression, coincident discs).
+* ``calibrated_21x5``: the demo at 0.01/0.02 with per-bond stiffness
+  (``src/tensordem/calibrated_dem.py``), seeded U[0.5, 1] x the config's.
 """
 
 from __future__ import annotations
@@ -152,6 +154,22 @@ def loads() -> None:
     print("loads broken", sim.broken_bonds)
 
 
+def calibrated() -> None:
+    """Per-bond stiffness (src/tensordem/calibrated_dem.py): the 21x5 demo at
+    0.01/0.02 with seeded bond stiffness U[0.5, 1] x the config's."""
+    from tensordem.calibrated_dem import CalibratedIceDEM
+    cfg = DEMConfig(breaking_strain=0.01, shear_breaking_strain=0.02)
+    probe = IceDEM(cfg)
+    rng = np.random.default_rng(21)
+    k = cfg.bond_stiffness * rng.uniform(0.5, 1.0, len(probe.bond_indices))
+    sim = CalibratedIceDEM(cfg, bond_stiffness=torch.tensor(k))
+    out = _record_run(sim, 2000, FRAMES)
+    out["config"] = _config_array(cfg)
+    out["bond_stiffness"] = k
+    np.savez_compressed(OUT / "calibrated_21x5.npz", **out)
+    print(f"calibrated: broken {sim.broken_bonds}/{int(sim.bonded.sum())} digest {out['break_digest']}")
+
+
 def unit_cases() -> None:
     """Single forces() calls on edited states (tests/test_dem.py:21-139)."""
     out = {}
@@ -219,7 +237,7 @@ def unit_cases() -> None:
 
 if __name__ == "__main__":
     torch.set_num_threads(1)
-    which = sys.argv[1:] or ["demo", "repro", "hull", "loads", "unit"]
+    which = sys.argv[1:] or ["demo", "repro", "hull", "loads", "unit", "calibrated"]
     if "demo" in which:
         demo(0.01, 0.02)
         demo(0.015, 0.03)
@@ -231,3 +249,5 @@ if __name__ == "__main__":
         loads()
     if "unit" in which:
         unit_cases()
+    if "calibrated" in which:
+        calibrated()

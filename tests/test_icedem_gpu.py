@@ -200,3 +200,39 @@ def test_fragments_partition_the_surviving_bond_graph():
     pairs = sim.pairs[sim.alive].cpu().numpy()
     assert (label[pairs[:, 0]] == label[pairs[:, 1]]).all()  # no surviving bond crosses fragments
     assert len(frags) > 1
+
+
+def test_per_bond_stiffness_parity(tdem):
+    """CalibratedIceDEM on the GPU against the reference's calibrated run."""
+    from tensordem_gb300.calibrated import CalibratedIceDEM
+    g = P.load("calibrated_21x5")
+    sim = CalibratedIceDEM(tdem.DEMConfig(**P.config_dict(g)), bond_stiffness=g["bond_stiffness"])
+    worst = P.replay(g, sim, to_np=_np)
+    me = sim.mechanical_energy()
+    got = [me[k] for k in ("kinetic_J", "bond_J", "pair_contact_J", "tool_contact_J", "mechanical_J")]
+    assert P.normwise(got, g["final_mech"]) <= P.RTOL
+    print("calibrated worst normwise errors", worst)
+
+
+def test_per_bond_stiffness_validation_and_restart(tdem):
+    from tensordem_gb300.calibrated import CalibratedIceDEM
+    cfg = tdem.DEMConfig(nx=7, ny=3, tool_speed=0.2, breaking_strain=0.008, shear_breaking_strain=0.02)
+    nb = int(tdem.IceDEM(cfg).bonded.sum())
+    k = np.linspace(0.6, 1.0, nb) * cfg.bond_stiffness
+    with pytest.raises(ValueError):
+        CalibratedIceDEM(cfg)
+    with pytest.raises(ValueError):
+        CalibratedIceDEM(cfg, bond_stiffness=k[:-1])
+    with pytest.raises(ValueError):
+        CalibratedIceDEM(cfg, bond_stiffness=k * 1.5)
+    sim = CalibratedIceDEM(cfg, bond_stiffness=k)
+    sim.run(40)
+    snap = sim.snapshot()
+    again = CalibratedIceDEM.from_snapshot(snap)
+    sim.run(40)
+    again.run(40)
+    assert torch.equal(sim.positions, again.positions)
+    assert torch.equal(sim.alive, again.alive)
+    sim.coefficients[0] *= 0.5  # a mutated host copy no longer matches the kernel's
+    with pytest.raises(ValueError):
+        sim.step()

@@ -81,3 +81,15 @@ def test_recommended_dt_matches_reference_value():
     g = P.load("demo_b0.01_s0.02")
     assert OracleConfig().recommended_dt == float(g["dt"])
     assert math.isclose(float(g["dt"]), 6.8788e-05, rel_tol=1e-4)
+
+
+def test_per_bond_stiffness_case():
+    """CalibratedIceDEM (src/tensordem/calibrated_dem.py) golden run."""
+    g = P.load("calibrated_21x5")
+    sim = _oracle_from(g, bond_stiffness=g["bond_stiffness"])
+    P.replay(g, sim, to_np=np.asarray)
+    me = sim.mechanical_energy()
+    got = [me[k] for k in ("kinetic_J", "bond_J", "pair_contact_J", "tool_contact_J", "mechanical_J")]
+    assert P.normwise(got, g["final_mech"]) <= P.RTOL
+    # the calibrated run is a different run: its break record differs from the plain demo's
+    assert not np.array_equal(g["failure_time_s"], P.load("demo_b0.01_s0.02")["failure_time_s"])
