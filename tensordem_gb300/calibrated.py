@@ -54,11 +54,11 @@ class CalibratedIceDEM(IceDEM):
                 or bool((self.pair_coefficients[~self.bonded] != 0).any())):
             raise ValueError("per-bond stiffness mutated after construction")
 
-    def forces(self, external_forces=None):
+    def forces(self, external_forces: torch.Tensor | None = None) -> tuple[torch.Tensor, torch.Tensor]:
         self._check()
         return super().forces(external_forces)
 
-    def step(self, external_forces=None, *, load_time=None) -> None:
+    def step(self, external_forces: torch.Tensor | None = None, *, load_time: float | None = None) -> None:
         self._check()
         super().step(external_forces, load_time=load_time)
 
