@@ -216,13 +216,6 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 constexpr int kVariants = 6;
 
 template <class T>
-struct StepKernel {
-  void* func;
-  int block;
-  int grid;
-};
-
-template <class T>
 using StepFn = void (*)(Params<T>, Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int);
 
 template <class T, bool F>

@@ -169,18 +169,6 @@ __device__ __forceinline__ void wall_contact(const Params<T>& P, T nwx, T nwy, T
   if (COMMIT) *slot = V2<T>{xx, xy};
 }
 
-template <class T>
-__device__ __forceinline__ float block_max_f(float x) {
-  __shared__ float s[kThreads / 32];
-  for (int off = 16; off > 0; off >>= 1) x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, off));
-  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = x;
-  __syncthreads();
-  float m = s[0];
-  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, s[w]);
-  __syncthreads();
-  return m;
-}
-
 __device__ __forceinline__ double block_sum_d(double x) {
   __shared__ double s[kThreads / 32];
   for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
