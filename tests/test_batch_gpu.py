@@ -228,3 +228,32 @@ def test_batch_capacity_and_argument_errors(bt):
         b.admit(_inst(bt, *_gas(6, 4), bonds=bad, strength=np.ones(1)))
     b.step(2)
     assert b.info()["status"] == 0
+
+
+def test_failed_instance_is_quarantined_and_others_continue(bt):
+    """An instance whose state blows up (dt far above its stability limit) is
+    reported and frozen; an instance sharing the batch keeps stepping and stays
+    within the FP32 tolerance of its solo run (the blow-up can only move the
+    shared rebuild times)."""
+    from dataclasses import replace
+    good_cfg, good_st = _gas(7)
+    bad_cfg, bad_st = dense_gas(16, seed=8, precision=32)  # fast, colliding discs
+    bad_cfg = replace(bad_cfg, dt=bad_cfg.dt * 200.0)
+    solo = _batch(bt, precision=32)
+    k0 = solo.admit(_inst(bt, good_cfg, good_st))
+    solo.step(80)
+    ref = solo.read(k0)
+    mix = _batch(bt, precision=32)
+    kg = mix.admit(_inst(bt, good_cfg, good_st))
+    kb = mix.admit(_inst(bt, bad_cfg, bad_st))
+    mix.step(80)
+    bad = mix.read(kb, state=False)["ledger"]
+    good = mix.read(kg)
+    assert bad["status"] != 0  # non-finite or escaped, reported on the instance
+    assert good["ledger"]["status"] == 0
+    assert np.isfinite(good["pos"]).all()
+    assert _rel(good["pos"], ref["pos"]) <= 1e-5
+    assert _rel(good["vel"], ref["vel"]) <= 1e-2
+    mix.retire(kb)
+    mix.step(10)  # the compaction rebuild drops the failed instance
+    assert mix.info()["live_particles"] == good_cfg.n
