@@ -10,7 +10,7 @@ step, outside its CUDA-event bracket.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Multi-GPU: the path does not shard in this build ("replicas only"): under
+Multi-GPU: the path does not shard ("replicas only"): under
 torchrun every rank runs its own replica (seeded by rank) and the line reports
 the aggregate particle-steps/s over the slowest rank's time (weak scaling).
 ``--impl reference`` times the CPU oracle (the FP64 restatement of the

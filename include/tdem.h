@@ -20,7 +20,7 @@
  *     ledger. The state arrays are owned by the caller (the Python drop-in
  *     keeps them as torch tensors) and passed on every call.
  *
- *  2. "hm": the spec mode, a 2-D Hertz-Mindlin disc engine: cell-list
+ *  2. "hm": the Hertz-Mindlin mode, a 2-D disc engine: cell-list
  *     contact detection with a Verlet skin, Hertz normal + Tsuji dashpot,
  *     Mindlin tangential spring with Coulomb cap and per-contact history,
  *     bonded-particle normal/shear springs with irreversible tensile and
@@ -165,7 +165,7 @@ int tdem_icedem_write_ledger(tdem_icedem* h, const double* in_host, int count, v
 int tdem_icedem_last_error(const tdem_icedem* h, char* buf, size_t len);
 
 /* ========================================================================
- * 2. North-star mode ("hm"): 2-D Hertz-Mindlin discs
+ * 2. Hertz-Mindlin mode ("hm"): 2-D Hertz-Mindlin discs
  * ====================================================================== */
 
 typedef struct tdem_hm tdem_hm;
@@ -352,7 +352,7 @@ int tdem_hm_use_graph(tdem_hm* h, int on);
 int tdem_hm_last_error(const tdem_hm* h, char* buf, size_t len);
 
 /* ========================================================================
- * 3. Batched ragged engine ("batch"): many independent spec solves
+ * 3. Batched ragged engine ("batch"): many independent Hertz-Mindlin solves
  * ====================================================================== */
 
 /* Many independent solves of uneven sizes (each described by a

@@ -1,4 +1,4 @@
-"""CPU FP64 restatement of the 2-D Hertz-Mindlin disc step (spec mode).
+"""CPU FP64 restatement of the 2-D Hertz-Mindlin disc step (Hertz-Mindlin mode).
 
 TEST INFRASTRUCTURE ONLY: the parity oracle and the timed CPU baseline for the
 CUDA engine in ``tensordem_gb300/csrc/hm2d.cu``. Only ``tests/``,

@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY. This module is the parity oracle for the CUDA
 reference-mode path in ``tensordem_gb300``. Only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` leg of ``bench.py`` may
-import it, and only as the checker or the timed CPU baseline; the product path
+import it, and only to check results or as the timed CPU baseline; the product path
 never calls it.
 
 It restates, in numpy float64, the algorithm of ``src/tensordem/dem.py`` of

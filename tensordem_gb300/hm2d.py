@@ -1,4 +1,4 @@
-"""Hertz-Mindlin 2-D disc engine (spec mode) on the GB300 CUDA path.
+"""Hertz-Mindlin 2-D disc engine (Hertz-Mindlin mode) on the GB300 CUDA path.
 
 :class:`HM2D` owns one engine of ``libtdem_sm103.so`` (include/tdem.h,
 ``tdem_hm_*``): device-resident particle state sorted by cell, a Verlet
