@@ -132,6 +132,10 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   const int sp = ctl->sp, lp = ctl->lp;
   const long long eval = ctl->evals;
   const int ntiles = ctl->ntiles;
+  // written only by the last warp of this kernel, after every block read them
+  const float disp0 = ctl->disp;
+  const int since0 = ctl->since;
+  const long long target = ctl->target;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int nwarps = gridDim.x * NW;
   if (threadIdx.x == 0) s_warps_done = 0u;
@@ -338,20 +342,21 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     if (mine != NW - 1) return;
     const unsigned tk = atomicAdd(&ctl->ticket, 1u);
     if (tk != gridDim.x - 1) return;
-    // last warp of the grid: step bookkeeping and the graph's conditions
-    __threadfence();
+    // last warp of the grid: step bookkeeping and the graph's conditions. The
+    // speed bound is read by an atomic at L2, issued only after the ticket's
+    // value was tested, so no fence is needed here.
     const float vm = sqrtf(__uint_as_float(atomicExch(&ctl->vmax2_bits, 0u)));
     ctl->ticket = 0;
     ctl->tile_next = 0;
     ctl->sp = sp ^ 1;
-    ctl->evals += 1;
-    const float disp = ctl->disp + vm;  // in units of each instance's allowed displacement
+    ctl->evals = eval + 1;
+    const float disp = disp0 + vm;  // in units of each instance's allowed displacement
     ctl->disp = disp;
-    const int since = ctl->since + 1;
+    const int since = since0 + 1;
     ctl->since = since;
     const int rebuild = (disp > 1.0f || (rebuild_every > 0 && since >= rebuild_every)) ? 1 : 0;
     ctl->rebuild_pending = rebuild;
-    const int keep_going = ctl->evals < ctl->target;
+    const int keep_going = eval + 1 < target;
     if (use_cond & 1) cudaGraphSetConditional(h_rebuild, (unsigned)rebuild);
     if (use_cond & 2) cudaGraphSetConditional(h_loop, (unsigned)keep_going);
   }

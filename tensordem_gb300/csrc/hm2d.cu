@@ -212,7 +212,7 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 
 // Step-kernel variants the autotuner chooses from: 0 = one thread per
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
-// block shapes.
+// block shapes; 4..5 = bulk-copy staging of own state.
 constexpr int kVariants = 6;
 
 template <class T>

@@ -566,10 +566,22 @@ __device__ __forceinline__ void indenter_contact(const Params<T>& P, long long e
 // Everything one particle does in one evaluation: its candidate slots, the
 // walls, and (committing modes) the velocity-Verlet update into the other
 // buffers. p, v, hd are the particle's own loads (already issued).
+// Positions of the first three partners of a list head, issued together.
+template <class T>
+__device__ __forceinline__ void load_head_partners(const V4<T>* __restrict__ pos, const uint4& hd, V4<T>& q0,
+                                                   V4<T>& q1, V4<T>& q2) {
+  const int cnt = (int)(hd.x & 0xFFu);
+  if (cnt > 0) q0 = pos[hd.y];
+  if (cnt > 1) q1 = pos[hd.z];
+  if (cnt > 2) q2 = pos[hd.w];
+}
+
+// process_particle with the first three partners' positions already loaded.
 template <class T, int MODE, bool FEAT>
-__device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i,
-                                                 const V4<T>& p, const V4<T>& v, const uint4& hd, int primed,
-                                                 long long eval, ThreadLedger<T>& L) {
+__device__ __forceinline__ void process_particle_q(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i,
+                                                   const V4<T>& p, const V4<T>& v, const uint4& hd,
+                                                   const V4<T>& q0, const V4<T>& q1, const V4<T>& q2, int primed,
+                                                   long long eval, ThreadLedger<T>& L) {
   constexpr bool COMMIT = MODE != kPeek;
   const int n = P.n;
   const V4<T>* __restrict__ pos = B.pos[sp];
@@ -578,11 +590,6 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
   V2<T>* __restrict__ hist = B.hist[lp];
   const int cnt = (int)(hd.x & 0xFFu);
   const unsigned mask = hd.x >> 8;
-  // positions of the first three partners, issued together
-  V4<T> q0{}, q1{}, q2{};
-  if (cnt > 0) q0 = pos[hd.y];
-  if (cnt > 1) q1 = pos[hd.z];
-  if (cnt > 2) q2 = pos[hd.w];
   unsigned nmask = 0u;
   Acc<T> fx, fy, tq;
   if (FEAT && P.BMAX > 0) {
@@ -692,14 +699,43 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
   }
 }
 
+template <class T, int MODE, bool FEAT>
+__device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i,
+                                                 const V4<T>& p, const V4<T>& v, const uint4& hd, int primed,
+                                                 long long eval, ThreadLedger<T>& L) {
+  V4<T> q0{}, q1{}, q2{};
+  load_head_partners<T>(B.pos[sp], hd, q0, q1, q2);
+  process_particle_q<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, q0, q1, q2, primed, eval, L);
+}
+
+// Control fields a step kernel reads once at its start. disp and target are
+// written only by the last warp of the kernel, after every block has read
+// them, so the epilogue needs no second round trip for them.
+struct StepCtl {
+  int sp, lp;
+  long long evals, target;
+  float disp;
+};
+
+__device__ __forceinline__ StepCtl load_step_ctl(const Ctl* ctl) {
+  StepCtl c;
+  c.sp = ctl->sp;
+  c.lp = ctl->lp;
+  c.evals = ctl->evals;
+  c.target = ctl->target;
+  c.disp = ctl->disp;
+  return c;
+}
+
 // Commit epilogue: per-warp ledger partials and the speed bound, then the
 // last warp of the last block does the step bookkeeping (indenter reaction,
 // rebuild trigger) and sets the graph's conditions. No block-wide barrier:
 // warps retire as soon as they are done.
 template <class T, bool FEAT>
-__device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T>& B, int sp,
+__device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T>& B, const StepCtl& c,
                                                 const ThreadLedger<T>& L, cudaGraphConditionalHandle h_rebuild,
                                                 cudaGraphConditionalHandle h_loop, int use_cond) {
+  const int sp = c.sp;
   Ctl* ctl = B.ctl;
   float wm = L.vmax2;
   T wd = L.diss, wf = L.frac, wix = L.ifx, wiy = L.ify;
@@ -738,8 +774,10 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
   // last warp of this block
   const unsigned t = atomicAdd(&ctl->ticket, 1u);
   if (t != gridDim.x - 1) return;
-  // last block of the grid
-  __threadfence();
+  // last block of the grid. The speed bound is read by an atomic at L2,
+  // issued only after the ticket's value was tested; the indenter partials
+  // are read with plain loads and need the fence.
+  if (FEAT) __threadfence();
   if (FEAT && P.irad > T(0)) {
     // sum the indenter partials in warp order (deterministic)
     const unsigned m = *reinterpret_cast<volatile unsigned*>(&ctl->load_entries);
@@ -765,21 +803,24 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
     ctl->reaction_x = -sx;
     ctl->reaction_y = -sy;
     ctl->tool_work += (double)P.dt * (sx * P.ind_vx + sy * P.ind_vy);
-    if (ctl->evals < (long long)P.load_cap) {
-      B.load[2 * ctl->evals] = -sx;
-      B.load[2 * ctl->evals + 1] = -sy;
+    if (c.evals < (long long)P.load_cap) {
+      B.load[2 * c.evals] = -sx;
+      B.load[2 * c.evals + 1] = -sy;
     }
     ctl->load_entries = 0u;
   }
-  const float vmax = sqrtf(__uint_as_float(atomicExch(&ctl->vmax2_bits, 0u)));
+  const unsigned vbits = atomicExch(&ctl->vmax2_bits, 0u);
+  const int status = *reinterpret_cast<volatile int*>(&ctl->status);
+  const float vmax = sqrtf(__uint_as_float(vbits));
   ctl->ticket = 0;
   ctl->sp = sp ^ 1;
-  ctl->evals += 1;
-  const float disp = ctl->disp + vmax * (float)P.dt;
+  const long long evals = c.evals + 1;
+  ctl->evals = evals;
+  const float disp = c.disp + vmax * (float)P.dt;
   ctl->disp = disp;
   const int rebuild = (disp > P.rebuild_disp) ? 1 : 0;
   ctl->rebuild_pending = rebuild;
-  const int keep_going = (ctl->evals < ctl->target) && !(ctl->status & kStatusNonfinite);
+  const int keep_going = (evals < c.target) && !(status & kStatusNonfinite);
   // use_cond bit 0: this launch sits in a graph with a rebuild IF node;
   // bit 1: it also sits in the step loop's WHILE body
   if (use_cond & 1) cudaGraphSetConditional(h_rebuild, (unsigned)rebuild);
@@ -792,14 +833,15 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel
                                                             cudaGraphConditionalHandle h_rebuild,
                                                             cudaGraphConditionalHandle h_loop, int use_cond,
                                                             int primed) {
-  const int sp = B.ctl->sp, lp = B.ctl->lp;
+  const StepCtl c = load_step_ctl(B.ctl);
+  const int sp = c.sp, lp = c.lp;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   ThreadLedger<T> L;
   if (i < P.n) {
     const V4<T> p = B.pos[sp][i];
     const V4<T> v = B.vel[sp][i];
     const uint4 hd = B.head[lp][i];
-    process_particle<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, primed, B.ctl->evals, L);
+    process_particle<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, primed, c.evals, L);
   }
   if (MODE == kPeek) {
     const double k = block_sum_d(L.ke);
@@ -825,7 +867,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel
     }
     return;
   }
-  commit_epilogue<T, FEAT>(P, B, sp, L, h_rebuild, h_loop, use_cond);
+  commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
 // Persistent grid-stride variant: while a thread works on particle i it has
@@ -837,8 +879,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
                                                                cudaGraphConditionalHandle h_loop, int use_cond,
                                                                int primed) {
   static_assert(MODE != kPeek, "read-back uses force_kernel");
-  const int sp = B.ctl->sp, lp = B.ctl->lp;
-  const long long eval = B.ctl->evals;
+  const StepCtl c = load_step_ctl(B.ctl);
+  const int sp = c.sp, lp = c.lp;
+  const long long eval = c.evals;
   const int stride = gridDim.x * BLOCK;
   int i = blockIdx.x * BLOCK + threadIdx.x;
   ThreadLedger<T> L;
@@ -864,7 +907,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
     v = vn;
     hd = hn;
   }
-  commit_epilogue<T, FEAT>(P, B, sp, L, h_rebuild, h_loop, use_cond);
+  commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
 // Bulk-copy variant: each block streams its tiles of own-particle state
@@ -884,8 +927,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bu
   __shared__ alignas(128) V4<T> s_vel[2][BLOCK];
   __shared__ alignas(128) uint4 s_head[2][BLOCK];
   __shared__ alignas(8) uint64_t s_bar[2];
-  const int sp = B.ctl->sp, lp = B.ctl->lp;
-  const long long eval = B.ctl->evals;
+  const StepCtl c = load_step_ctl(B.ctl);
+  const int sp = c.sp, lp = c.lp;
+  const long long eval = c.evals;
   const int n = P.n;
   const int ntiles = (n + BLOCK - 1) / BLOCK;
   ThreadLedger<T> L;
@@ -926,7 +970,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bu
     }
     __syncthreads();
   }
-  commit_epilogue<T, FEAT>(P, B, sp, L, h_rebuild, h_loop, use_cond);
+  commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
 // ---------------------------------------------------------------------------
