@@ -49,55 +49,72 @@ static __global__ void batch_count_kernel(Ctl* ctl, const int* cell_start) {
   if (ctl->rebuild_pending) ctl->n_live = cell_start[ctl->key_hi];
 }
 
-// Sorted range and first tile of every live instance slot (one block).
+// Sorted range and first tile of every live instance slot (one block). Tiles
+// are numbered kind-major: first the instances without bonds or indenter (run
+// by the granular kernel build), then the others. ifirst[pass * slots + s] is
+// slot s's first tile in its pass (non-decreasing over the whole array).
 template <class T>
 __global__ void batch_tiles_count_kernel(Bufs<T> B, int slots) {
   Ctl* ctl = B.ctl;
   if (!ctl->rebuild_pending) return;
   int carry = 0;
-  for (int c0 = 0; c0 < slots; c0 += kScanChunk) {
-    const int base = c0 + threadIdx.x * kScanItems;
-    int st[kScanItems], en[kScanItems], nt[kScanItems];
-    int local = 0;
-    for (int k = 0; k < kScanItems; ++k) {
-      const int s = base + k;
-      st[k] = en[k] = nt[k] = 0;
-      if (s < slots && (B.istate[s] & kInstAlive)) {
-        const Params<T>& Q = B.iparams[s];
-        st[k] = B.cell_start[Q.key_off];
-        en[k] = B.cell_start[Q.key_off + Q.ncx * Q.ncy];
-        nt[k] = (en[k] - st[k] + kTile - 1) / kTile;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int c0 = 0; c0 < slots; c0 += kScanChunk) {
+      const int base = c0 + threadIdx.x * kScanItems;
+      int st[kScanItems], en[kScanItems], nt[kScanItems];
+      bool mine[kScanItems];
+      int local = 0;
+      for (int k = 0; k < kScanItems; ++k) {
+        const int s = base + k;
+        st[k] = en[k] = nt[k] = 0;
+        mine[k] = false;
+        if (s < slots && (B.istate[s] & kInstAlive)) {
+          const Params<T>& Q = B.iparams[s];
+          mine[k] = (Q.feat != 0) == (pass == 1);
+          if (mine[k]) {
+            st[k] = B.cell_start[Q.key_off];
+            en[k] = B.cell_start[Q.key_off + Q.ncx * Q.ncy];
+            nt[k] = (en[k] - st[k] + kTile - 1) / kTile;
+          }
+        } else if (s < slots && pass == 0) {
+          mine[k] = true;  // dead or free slot: an empty range
+        }
+        local += nt[k];
       }
-      local += nt[k];
+      int total;
+      int run = carry + block_exclusive_scan(local, &total);
+      for (int k = 0; k < kScanItems; ++k) {
+        const int s = base + k;
+        if (s < slots) {
+          B.ifirst[pass * slots + s] = run;
+          if (mine[k]) B.irange[s] = make_int4(st[k], en[k], run, nt[k]);
+        }
+        run += nt[k];
+      }
+      carry += total;
     }
-    int total;
-    int run = carry + block_exclusive_scan(local, &total);
-    for (int k = 0; k < kScanItems; ++k) {
-      const int s = base + k;
-      if (s < slots) B.irange[s] = make_int4(st[k], en[k], run, nt[k]);
-      run += nt[k];
-    }
-    carry += total;
+    if (pass == 0 && threadIdx.x == 0) ctl->ntiles_plain = carry;
   }
   if (threadIdx.x == 0) ctl->ntiles = carry;
 }
 
-// Tile table: tile t belongs to the last slot whose first tile is <= t.
+// Tile table: tile t belongs to the last entry of ifirst that is <= t.
 template <class T>
 __global__ void batch_tiles_fill_kernel(Bufs<T> B, int slots) {
   const Ctl* ctl = B.ctl;
   if (!ctl->rebuild_pending) return;
   const int nt = ctl->ntiles;
+  const int m = 2 * slots;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
-    int lo = 0, hi = slots;
+    int lo = 0, hi = m;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (B.irange[mid].z <= t)
+      if (B.ifirst[mid] <= t)
         lo = mid + 1;
       else
         hi = mid;
     }
-    const int s = lo - 1;  // irange[0].z == 0 <= t, so s >= 0
+    const int s = (lo - 1) % slots;  // ifirst[0] == 0 <= t, so lo >= 1
     const int4 r = B.irange[s];
     const int first = r.x + (t - r.z) * kTile;
     B.tiles[t] = make_int4(s, first, min(kTile, r.y - first), 0);
@@ -118,11 +135,16 @@ __device__ __forceinline__ T warp_sum(T x) {
   return x;
 }
 
-template <class T, int MODE, int BLOCK, int MINB>
+// PART 0: every tile (read-back); 1: the granular instances' tiles, granular
+// code, no step bookkeeping; 2: the other tiles, full code, and the step
+// bookkeeping (it runs after part 1 in the same stream).
+template <class T, int MODE, int BLOCK, int MINB, int PART>
 __global__ void __launch_bounds__(BLOCK, MINB)
     batch_kernel(Bufs<T> B, cudaGraphConditionalHandle h_rebuild, cudaGraphConditionalHandle h_loop,
                  int use_cond, int rebuild_every) {
   static_assert(MODE == kBatch || MODE == kPeek, "batched modes only");
+  static_assert((MODE == kPeek) == (PART == 0), "read-back covers every tile; steps run in two parts");
+  constexpr bool FEAT = PART != 1;
   constexpr int NW = BLOCK / 32;
   constexpr int PW = (int)(sizeof(Params<T>) / 4);
   static_assert(sizeof(Params<T>) % 4 == 0, "Params copied as 32-bit words");
@@ -131,7 +153,8 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   Ctl* ctl = B.ctl;
   const int sp = ctl->sp, lp = ctl->lp;
   const long long eval = ctl->evals;
-  const int ntiles = ctl->ntiles;
+  const int tbeg = PART == 2 ? ctl->ntiles_plain : 0;
+  const int ntiles = PART == 1 ? ctl->ntiles_plain : ctl->ntiles;
   // written only by the last warp of this kernel, after every block read them
   const float disp0 = ctl->disp;
   const int since0 = ctl->since;
@@ -158,7 +181,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   auto grab = [&]() -> int {
     if (MODE == kPeek) return (grabs++ == 0) ? (int)min((long long)gw * per, (long long)ntiles) : ntiles;
     int b = 0;
-    if (lane == 0) b = atomicAdd(&ctl->tile_next, kChunk);
+    if (lane == 0) b = tbeg + atomicAdd(PART == 1 ? &ctl->tile_next : &ctl->tile_next2, kChunk);
     return __shfl_sync(kFull, b, 0);
   };
   int t = grab();
@@ -278,7 +301,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
       }
     } else if (run) {
       ThreadLedger<T> L;
-      if (lane < d.z) process_particle<T, MODE, true>(Q, B, sp, lp, d.y + lane, p, v, hd, primed, le, L);
+      if (lane < d.z) process_particle<T, MODE, FEAT>(Q, B, sp, lp, d.y + lane, p, v, hd, primed, le, L);
       double* row = B.tpart + (size_t)t * kTileVals;
       if (MODE == kBatch) {
         const float f = (float)Q.dt / Q.rebuild_disp;
@@ -337,6 +360,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     if (lane != 0) return;
     const unsigned bits = __float_as_uint(vmax);
     if (bits > *reinterpret_cast<volatile unsigned*>(&ctl->vmax2_bits)) atomicMax(&ctl->vmax2_bits, bits);
+    if (PART == 1) return;  // the second launch does the step bookkeeping
     __threadfence();
     const unsigned mine = atomicAdd(&s_warps_done, 1u);
     if (mine != NW - 1) return;
@@ -348,6 +372,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     const float vm = sqrtf(__uint_as_float(atomicExch(&ctl->vmax2_bits, 0u)));
     ctl->ticket = 0;
     ctl->tile_next = 0;
+    ctl->tile_next2 = 0;
     ctl->sp = sp ^ 1;
     ctl->evals = eval + 1;
     const float disp = disp0 + vm;  // in units of each instance's allowed displacement
@@ -534,15 +559,21 @@ inline int bvariant_block(int v) { return (v == 1 || v == 3) ? 128 : 256; }
 template <class T>
 using BatchFn = void (*)(Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int);
 
-template <class T>
-BatchFn<T> batch_fn(int variant, bool peek) {
-  if (peek) return &batch_kernel<T, kPeek, 256, 2>;
+template <class T, int PART>
+BatchFn<T> batch_fn_part(int variant) {
   switch (variant) {
-    case 1: return &batch_kernel<T, kBatch, 128, 4>;
-    case 2: return &batch_kernel<T, kBatch, 256, 3>;
-    case 3: return &batch_kernel<T, kBatch, 128, 6>;
-    default: return &batch_kernel<T, kBatch, 256, 2>;
+    case 1: return &batch_kernel<T, kBatch, 128, 4, PART>;
+    case 2: return &batch_kernel<T, kBatch, 256, 3, PART>;
+    case 3: return &batch_kernel<T, kBatch, 128, 6, PART>;
+    default: return &batch_kernel<T, kBatch, 256, 2, PART>;
   }
+}
+
+// part 0: read-back over every tile; 1 / 2: the two launches of a step
+template <class T>
+BatchFn<T> batch_fn(int variant, int part) {
+  if (part == 0) return &batch_kernel<T, kPeek, 256, 2, 0>;
+  return part == 1 ? batch_fn_part<T, 1>(variant) : batch_fn_part<T, 2>(variant);
 }
 
 inline int bvariant_minb(int v) { return v == 0 ? 2 : v == 1 ? 4 : v == 2 ? 3 : 6; }
@@ -708,6 +739,7 @@ struct Batch final : BatchBase {
     B.iparams = iparams;
     B.istate = a.take<int>((size_t)slots);
     B.irange = a.take<int4>((size_t)slots);
+    B.ifirst = a.take<int>(2 * (size_t)slots);
     B.iticket = a.take<unsigned>((size_t)slots);
     B.iled = a.take<double>((size_t)slots * kInstLedger);
     B.tiles = a.take<int4>(tiles_cap);
@@ -801,6 +833,15 @@ struct Batch final : BatchBase {
 
   unsigned vgrid(int v) const { return (unsigned)(sms * bvariant_minb(v)); }
 
+  // One step as plain launches: strain, the granular tiles, the other tiles
+  // (with the step bookkeeping), the rebuild if it was triggered.
+  void launch_step(int v, cudaStream_t s) {
+    launch_strain(s);
+    batch_fn<T>(v, 1)<<<vgrid(v), bvariant_block(v), 0, s>>>(B, 0, 0, 0, cfg.rebuild_every);
+    batch_fn<T>(v, 2)<<<vgrid(v), bvariant_block(v), 0, s>>>(B, 0, 0, 0, cfg.rebuild_every);
+    launch_rebuild(s);
+  }
+
   int add_step_and_rebuild(cudaGraph_t g, cudaGraphConditionalHandle h, cudaGraphConditionalHandle hl) {
     int cond_bits = 3, every = cfg.rebuild_every;
     void* args[] = {&B, &h, &hl, &cond_bits, &every};
@@ -819,12 +860,15 @@ struct Batch final : BatchBase {
       ndep = 1;
     }
     cudaKernelNodeParams kp = {};
-    kp.func = reinterpret_cast<void*>(batch_fn<T>(variant, false));
+    kp.func = reinterpret_cast<void*>(batch_fn<T>(variant, 1));
     kp.gridDim = dim3(vgrid(variant));
     kp.blockDim = dim3((unsigned)bvariant_block(variant));
     kp.kernelParams = args;
+    cudaGraphNode_t pnode;
+    TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&pnode, g, dep, ndep, &kp));
+    kp.func = reinterpret_cast<void*>(batch_fn<T>(variant, 2));
     cudaGraphNode_t knode;
-    TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&knode, g, dep, ndep, &kp));
+    TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&knode, g, &pnode, 1, &kp));
     cudaGraphNodeParams ip = {};
     ip.type = cudaGraphNodeTypeConditional;
     ip.conditional.handle = h;
@@ -841,7 +885,7 @@ struct Batch final : BatchBase {
     return TDEM_OK;
   }
 
-  // set target -> WHILE { [strain] -> batch kernel -> IF rebuild { ... } }
+  // set target -> WHILE { [strain] -> granular tiles -> other tiles -> IF rebuild { ... } }
   int build_graph() {
     TDEM_CUDA_TRY(&err, cudaGraphCreate(&graph, 0));
     TDEM_CUDA_TRY(&err, cudaGraphConditionalHandleCreate(&h_loop, graph, 1, cudaGraphCondAssignDefault));
@@ -1019,6 +1063,7 @@ struct Batch final : BatchBase {
     I.par.key_off = key_off;
     I.par.eval0 = evals;
     I.par.stop = LLONG_MAX;
+    I.par.feat = (nb > 0 || c.indenter_radius > 0.0) ? 1 : 0;
     // stage and append
     double* h = stage_host;
     std::memcpy(h, pos, 2 * (size_t)m * sizeof(double));
@@ -1087,10 +1132,7 @@ struct Batch final : BatchBase {
       TDEM_CUDA_TRY(&err, cudaGraphLaunch(exec, s));
     } else {
       for (long long k = 0; k < n; ++k) {
-        launch_strain(s);
-        batch_fn<T>(variant, false)<<<vgrid(variant), bvariant_block(variant), 0, s>>>(B, 0, 0, 0,
-                                                                                         cfg.rebuild_every);
-        launch_rebuild(s);
+        launch_step(variant, s);
       }
       TDEM_CUDA_TRY(&err, cudaGetLastError());
     }
@@ -1110,7 +1152,7 @@ struct Batch final : BatchBase {
     if (rc) return rc;
     launch_strain(s);
     batch_state_kernel<<<1, 1, 0, s>>>(B.istate, id, kInstPeek, 0);
-    batch_fn<T>(0, true)<<<(unsigned)(sms * 2), 256, 0, s>>>(B, 0, 0, 0, 0);
+    batch_fn<T>(0, 0)<<<(unsigned)(sms * 2), 256, 0, s>>>(B, 0, 0, 0, 0);
     batch_state_kernel<<<1, 1, 0, s>>>(B.istate, id, 0, kInstPeek);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     return TDEM_OK;
@@ -1209,7 +1251,7 @@ struct Batch final : BatchBase {
     launch_strain(s);
     const unsigned g = grid_items(count);
     batch_state_list_kernel<<<g, kThreads, 0, s>>>(B.istate, list_dev, count, kInstPeek, 0);
-    batch_fn<T>(0, true)<<<(unsigned)(sms * 2), 256, 0, s>>>(B, 0, 0, 0, 0);
+    batch_fn<T>(0, 0)<<<(unsigned)(sms * 2), 256, 0, s>>>(B, 0, 0, 0, 0);
     batch_state_list_kernel<<<g, kThreads, 0, s>>>(B.istate, list_dev, count, 0, kInstPeek);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     TDEM_CUDA_TRY(&err, cudaMemcpyAsync(all_led_host, B.iled, (size_t)slots * kInstLedger * sizeof(double),
@@ -1329,9 +1371,7 @@ struct Batch final : BatchBase {
     for (int v = 0; v < kBatchVariants; ++v) {
       TDEM_CUDA_TRY(&err, cudaEventRecord(e0, s));
       for (int k = 0; k < steps; ++k) {
-        launch_strain(s);
-        batch_fn<T>(v, false)<<<vgrid(v), bvariant_block(v), 0, s>>>(B, 0, 0, 0, cfg.rebuild_every);
-        launch_rebuild(s);
+        launch_step(v, s);
       }
       TDEM_CUDA_TRY(&err, cudaEventRecord(e1, s));
       TDEM_CUDA_TRY(&err, cudaEventSynchronize(e1));

@@ -93,6 +93,7 @@ struct Params {
   int key_off;       // first cell key of the instance (key = key_off + cy * ncx + cx)
   long long eval0;   // batch evaluation index of the instance's first step
   long long stop;    // the instance's own step limit: frozen once it has taken `stop` steps
+  int feat;          // 1: the instance has bonds or an indenter (stepped by the bonded kernel build)
   // FP32 screens that keep FP64 off the common path (decisions unchanged):
   // float brackets of the break strains (largest float <= eps, smallest >= eps)
   float eps_t_lo, eps_t_hi, eps_s_lo, eps_s_hi;
@@ -116,7 +117,7 @@ struct Ctl {
   int status;              // Status bits
   int rebuilds;
   int max_cnt;             // largest candidate count of the last rebuild
-  int pad;
+  int tile_next2;          // batched engine: chunk counter of the second step launch
   long long evals;         // force evaluations committed (prime + steps)
   long long target;        // stop the step loop at this many evaluations
   double tool_work;        // work done by the indenter on the discs (J)
@@ -127,9 +128,10 @@ struct Ctl {
   int n_live;              // particles in the sorted arrays [0, n_live)
   int n_old;               // n_live when the running rebuild started
   int ntiles;              // 32-particle tiles of the live instances
+  int ntiles_plain;        // of which the first ones belong to instances without bonds or indenter
   int since;               // steps since the last rebuild
   int key_hi;              // dead-particle key: one past the highest allocated cell key
-  int tile_next;           // next tile chunk handed out by the running step kernel
+  int tile_next;           // next tile chunk handed out by the (first) step launch
 };
 
 // Batched engine: per-instance state word (low byte: Status bits of the
@@ -189,6 +191,7 @@ struct Bufs {
   unsigned* iticket;   // per instance slot: tiles finished in the running kernel
   double* iled;        // [slots * kInstLedger] per-instance ledger
   int* tmp_key;        // rebuild: cell key of each old particle
+  int* ifirst;         // [2 * slots]: first tile of each slot, plain instances then the others
 };
 
 // The cell id rides in the last lane of the position vector: bit-cast for
