@@ -462,6 +462,159 @@ int tdem_batch_autotune(tdem_batch* h, int steps, float* ms_out, void* stream);
 int tdem_batch_use_graph(tdem_batch* h, int on);
 int tdem_batch_last_error(const tdem_batch* h, char* buf, size_t len);
 
+/* ========================================================================
+ * 4. 3-D reference mode ("icedem3d"): the reference's IceDEM3D
+ * ====================================================================== */
+
+/* FP64 step of the reference's bonded-sphere engine
+ * (src/tensordem/dem3d.py:564-1663): central-force bonds of the cubic
+ * lattice (linear or Maxwell-Wiechert), tensile / objective-shear / creep
+ * breakage, cell-list sphere contacts (linear penalty or Hertz, restitution
+ * or absolute dashpot, Cundall-Strack friction with a pair-keyed history that
+ * is never dropped, rolling-resistance couple), a spherical indenter, top /
+ * bottom / lateral plane platens (with Coulomb friction), gravity, buoyancy,
+ * wet drag and semi-implicit Euler. One CTA runs one instance for many steps
+ * per launch; each particle's force is summed in the reference's index_add_
+ * order. Derived constants are computed by the caller exactly as the
+ * reference computes them (Python floats), so the kernel sees the same bits. */
+typedef struct tdem_icedem3d tdem_icedem3d;
+
+enum { TDEM_ICE3D_MAX_BRANCHES = 4 };
+
+/* Friction-cone laws (DEM3DConfig.friction_cone_limit, dem3d.py:453-498). */
+enum {
+  TDEM_CONE_OFF = 0,   /* no tangential spring */
+  TDEM_CONE_SINGLE,    /* limit = c0 N */
+  TDEM_CONE_TANH,      /* limit = (c0 + c1 (1 - tanh(|v_t| / c2)) / 2) N */
+  TDEM_CONE_DUAL       /* limit = |F_t| > c0 N ? c1 N : c0 N */
+};
+
+typedef struct {
+  int32_t n;                 /* particles, 2 <= n <= tdem_icedem3d_max_particles() */
+  int32_t nbond;             /* bonds (pairs i < j sorted by i * n + j) */
+  int32_t hertz;             /* 0: linear penalty k_n; 1: Hertz (contact_model="hertz") */
+  int32_t damping;           /* 0 none, 1 restitution-derived, 2 absolute (contact_damping) */
+  int32_t hertz_tangential;  /* 1: k_t = hertz_kt sqrt(overlap); 0: constant tangential_k */
+  int32_t rolling;           /* rolling-resistance couple on */
+  int32_t platens;           /* bit0 top, bit1 bottom, bit2 lateral */
+  int32_t body;              /* bit0 body forces on, bit1 water present, bit2 wet drag */
+  int32_t n_branches;        /* Maxwell branches (0: linear bond) */
+  int32_t creep;             /* Kachanov damage clock on */
+  int32_t any_fixed;         /* some particle is fixed (pinned-pair effective mass) */
+  double radius, mass, dt, drag;
+  double bond_k;             /* linear k_b, or the equilibrium spring k0 */
+  double branch_k[TDEM_ICE3D_MAX_BRANCHES];
+  double branch_tau[TDEM_ICE3D_MAX_BRANCHES];
+  double branch_decay[TDEM_ICE3D_MAX_BRANCHES];      /* exp(-dt / tau) */
+  double branch_one_minus[TDEM_ICE3D_MAX_BRANCHES];  /* -expm1(-dt / tau) */
+  double breaking_strain, shear_breaking_strain;
+  double creep_exponent, creep_dt_over_time;         /* m, dt / t_ref */
+  double contact_k;          /* linear penalty stiffness */
+  double hertz_kn;           /* (4/3) E* sqrt(R*), particle pair */
+  double hertz_kn_rigid;     /* (4/3) E* sqrt(R*), rigid counterpart */
+  double hertz_pot;          /* (8/15) E* sqrt(R*), particle pair (contact energy) */
+  double tangential_k, hertz_kt;
+  double damping_c;          /* absolute: contact_damping; restitution, Hertz: 2 zeta */
+  double gamma_mobile, gamma_pinned; /* restitution, linear: 2 zeta sqrt(k_n m_eff) */
+  double mass_mobile, mass_pinned;   /* m / 2 and m */
+  int32_t cone, platen_cone;         /* TDEM_CONE_* of particle and platen friction */
+  double cone_c[3], platen_cone_c[3];
+  double roll_mu;
+  double tool_radius, tool_damping;
+  double tool_start[3], tool_velocity[3];
+  double platen_k, platen_c, platen_kt;
+  double top_start_z, top_velocity, bottom_start_z, bottom_velocity;
+  double lateral_k, lateral_c;
+  double gravity_force;      /* m g */
+  double buoyancy_force;     /* rho_w g (4/3) pi r^3 */
+  double wet_drag;           /* C_wet */
+  double water_level;
+  double cap_denominator;    /* 4 r**3, the spherical-cap volume fraction's denominator */
+} tdem_icedem3d_config;
+
+/* Constant topology, host arrays, copied at create time. */
+typedef struct {
+  const int32_t* bond_i;       /* (B) */
+  const int32_t* bond_j;       /* (B) */
+  const double* rest_length;   /* (B) */
+  const double* reference;     /* (B,3) x0[j] - x0[i] */
+  const double* initial_normal;/* (B,3) */
+  const double* threshold;     /* (B) per-bond tensile threshold, or NULL */
+  const double* creep_reference; /* (B) Kachanov reference force, or NULL */
+  const double* pinv;          /* (n,3,3) pseudo-inverse of each particle's bond covariance */
+  const uint8_t* full_rank;    /* (n) covariance of rank 3 */
+} tdem_icedem3d_topology;
+
+/* Caller-owned state, device pointers, passed on every call. */
+typedef struct {
+  double* positions;           /* (n,3) */
+  double* velocities;          /* (n,3) */
+  const double* initial_positions; /* (n,3) */
+  const uint8_t* fixed;        /* (n) */
+  uint8_t* alive;              /* (B) */
+  uint8_t* failure_mode;       /* (B) 1 tensile, 2 shear, 3 both, 4 creep */
+  double* failure_time_s;      /* (B) */
+  double* failure_extension_m; /* (B) */
+  double* failure_energy_J;    /* (B) */
+  double* branch_offsets;      /* (B, n_branches) or NULL */
+  double* elongation_prev;     /* (B) or NULL */
+  double* damage;              /* (B) or NULL */
+  double* bond_dissipation;    /* (1) cumulative dashpot dissipation, or NULL */
+  double* top_tangential;      /* (n,3) top platen spring offsets, or NULL */
+  double* bottom_tangential;   /* (n,3) */
+  double* lateral_position;    /* (4) x_min, x_max, y_min, y_max planes, or NULL */
+  const double* lateral_velocity; /* (4) */
+} tdem_icedem3d_state;
+
+enum {
+  TDEM_L3_REACTION_X = 0, TDEM_L3_REACTION_Y, TDEM_L3_REACTION_Z,
+  TDEM_L3_TOP_REACTION_Z, TDEM_L3_BOTTOM_REACTION_Z,
+  TDEM_L3_LATERAL_0, TDEM_L3_LATERAL_1, TDEM_L3_LATERAL_2, TDEM_L3_LATERAL_3,
+  TDEM_L3_FRICTION_POWER, TDEM_L3_ROLLING_POWER,
+  TDEM_L3_CONTACT_ENERGY,     /* contact potential of the evaluated configuration */
+  TDEM_L3_CONTACTS,           /* overlapping pairs of the last evaluation */
+  TDEM_L3_HISTORY_MAX,        /* largest friction-history table of a particle */
+  TDEM_L3_STEPS_DONE, TDEM_L3_STATUS,
+  TDEM_L3_MIN_BREAK_MARGIN,
+  TDEM_L3_COUNT = 20
+};
+
+int tdem_icedem3d_max_particles(void);
+int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_topology* topo,
+                         tdem_icedem3d** out);
+void tdem_icedem3d_destroy(tdem_icedem3d* h);
+
+/* One force evaluation at `time` (IceDEM3D.forces, dem3d.py:1301-1642):
+ * update_fracture commits breaks, update_history advances the friction and
+ * Maxwell histories. Writes the total force (n,3) to `out_force` (device).
+ * `loads`: optional (n,3) device array. */
+int tdem_icedem3d_forces(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads,
+                         double time, int update_fracture, int update_history, double* out_force,
+                         void* stream);
+
+/* `n_steps` steps from `time` (IceDEM3D.step, dem3d.py:1644-1663), loads held
+ * over all of them. Synchronizes `stream`; TDEM_ERR_NONFINITE after the step
+ * whose state stopped being finite, TDEM_ERR_CAPACITY when a contact list or
+ * friction history of a particle overflowed. */
+int tdem_icedem3d_step(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads,
+                       int64_t n_steps, double time, void* stream);
+
+/* Ledger of the last call (TDEM_L3_COUNT doubles). Synchronizes `stream`. */
+int tdem_icedem3d_read_ledger(tdem_icedem3d* h, double* out_host, int count, void* stream);
+
+/* Overlapping pairs (i < j) of the last evaluation, host int32 (count, 2). */
+int tdem_icedem3d_read_contacts(tdem_icedem3d* h, int32_t* pairs_host, int64_t capacity, int64_t* count,
+                                void* stream);
+/* The pair friction history (the reference's IceDEM3D._tangential_state,
+ * dem3d.py:1152-1185): `count` entries of pair (i < j, host int32 (count,2))
+ * and stored tangential displacement (host double (count,3)). Set replaces
+ * the whole table; read returns it in (i, then insertion) order. */
+int tdem_icedem3d_set_history(tdem_icedem3d* h, const int32_t* pairs_host, const double* disp_host, int64_t count,
+                              void* stream);
+int tdem_icedem3d_read_history(tdem_icedem3d* h, int32_t* pairs_host, double* disp_host, int64_t capacity,
+                               int64_t* count, void* stream);
+int tdem_icedem3d_last_error(const tdem_icedem3d* h, char* buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,55 @@ class BatchConfigC(C.Structure):
     ]
 
 
+class IceDEM3DConfigC(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32), ("nbond", C.c_int32), ("hertz", C.c_int32), ("damping", C.c_int32),
+        ("hertz_tangential", C.c_int32), ("rolling", C.c_int32), ("platens", C.c_int32),
+        ("body", C.c_int32), ("n_branches", C.c_int32), ("creep", C.c_int32), ("any_fixed", C.c_int32),
+        ("radius", C.c_double), ("mass", C.c_double), ("dt", C.c_double), ("drag", C.c_double),
+        ("bond_k", C.c_double), ("branch_k", C.c_double * 4), ("branch_tau", C.c_double * 4),
+        ("branch_decay", C.c_double * 4), ("branch_one_minus", C.c_double * 4),
+        ("breaking_strain", C.c_double), ("shear_breaking_strain", C.c_double),
+        ("creep_exponent", C.c_double), ("creep_dt_over_time", C.c_double),
+        ("contact_k", C.c_double), ("hertz_kn", C.c_double), ("hertz_kn_rigid", C.c_double),
+        ("hertz_pot", C.c_double), ("tangential_k", C.c_double), ("hertz_kt", C.c_double),
+        ("damping_c", C.c_double), ("gamma_mobile", C.c_double), ("gamma_pinned", C.c_double),
+        ("mass_mobile", C.c_double), ("mass_pinned", C.c_double),
+        ("cone", C.c_int32), ("platen_cone", C.c_int32),
+        ("cone_c", C.c_double * 3), ("platen_cone_c", C.c_double * 3),
+        ("roll_mu", C.c_double), ("tool_radius", C.c_double), ("tool_damping", C.c_double),
+        ("tool_start", C.c_double * 3), ("tool_velocity", C.c_double * 3),
+        ("platen_k", C.c_double), ("platen_c", C.c_double), ("platen_kt", C.c_double),
+        ("top_start_z", C.c_double), ("top_velocity", C.c_double),
+        ("bottom_start_z", C.c_double), ("bottom_velocity", C.c_double),
+        ("lateral_k", C.c_double), ("lateral_c", C.c_double),
+        ("gravity_force", C.c_double), ("buoyancy_force", C.c_double), ("wet_drag", C.c_double),
+        ("water_level", C.c_double), ("cap_denominator", C.c_double),
+    ]
+
+
+class IceDEM3DTopologyC(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "bond_i", "bond_j", "rest_length", "reference", "initial_normal", "threshold",
+        "creep_reference", "pinv", "full_rank")]
+
+
+class IceDEM3DStateC(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "positions", "velocities", "initial_positions", "fixed", "alive", "failure_mode",
+        "failure_time_s", "failure_extension_m", "failure_energy_J", "branch_offsets",
+        "elongation_prev", "damage", "bond_dissipation", "top_tangential", "bottom_tangential",
+        "lateral_position", "lateral_velocity")]
+
+
+# 3-D reference-mode ledger slots (TDEM_L3_*)
+L3_REACTION, L3_TOP, L3_BOTTOM, L3_LATERAL = 0, 3, 4, 5
+L3_FRICTION_POWER, L3_ROLLING_POWER, L3_CONTACT_ENERGY, L3_CONTACTS = 9, 10, 11, 12
+L3_HISTORY_MAX, L3_STEPS_DONE, L3_STATUS, L3_MIN_BREAK_MARGIN = 13, 14, 15, 16
+L3_COUNT = 20
+CONE_OFF, CONE_SINGLE, CONE_TANH, CONE_DUAL = 0, 1, 2, 3
+
+
 # Batched engine: extra ledger slots (TDEM_BATCH_L_*) and info slots (TDEM_BATCH_I_*)
 BATCH_PEAK_LOAD, BATCH_PEAK_EVAL, BATCH_REACTION_X, BATCH_REACTION_Y = 16, 17, 18, 19
 BATCH_L_COUNT = 20
@@ -119,6 +168,17 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_icedem_read_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
         "tdem_icedem_write_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
         "tdem_icedem_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "tdem_icedem3d_max_particles": (i32, []),
+        "tdem_icedem3d_create": (i32, [C.POINTER(IceDEM3DConfigC), C.POINTER(IceDEM3DTopologyC),
+                                       C.POINTER(vp)]),
+        "tdem_icedem3d_destroy": (None, [vp]),
+        "tdem_icedem3d_forces": (i32, [vp, C.POINTER(IceDEM3DStateC), vp, dbl, i32, i32, vp, vp]),
+        "tdem_icedem3d_step": (i32, [vp, C.POINTER(IceDEM3DStateC), vp, C.c_int64, dbl, vp]),
+        "tdem_icedem3d_read_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
+        "tdem_icedem3d_read_contacts": (i32, [vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
+        "tdem_icedem3d_set_history": (i32, [vp, vp, vp, C.c_int64, vp]),
+        "tdem_icedem3d_read_history": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
+        "tdem_icedem3d_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
         "tdem_hm_create": (i32, [C.POINTER(HMConfigC), C.POINTER(vp)]),
         "tdem_hm_destroy": (None, [vp]),
         "tdem_hm_set_state": (i32, [vp, vp, vp, vp, vp, vp, vp, i32, vp]),
@@ -188,6 +248,8 @@ def last_error(fn_name: str, handle) -> str:
         lib().tdem_hm_last_error(handle, buf, len(buf))
     elif fn_name.startswith("tdem_batch"):
         lib().tdem_batch_last_error(handle, buf, len(buf))
+    elif fn_name.startswith("tdem_icedem3d"):
+        lib().tdem_icedem3d_last_error(handle, buf, len(buf))
     else:
         lib().tdem_icedem_last_error(handle, buf, len(buf))
     return buf.value.decode(errors="replace")

@@ -22,9 +22,9 @@ LIB = BUILD / "libtdem_sm103.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "--std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I", str(PKG.parent / "include")]
-# Per-unit extra flags. The reference-mode unit reproduces torch's one-op-per-
-# rounding FP64 arithmetic, so it forbids fused multiply-adds.
-EXTRA = {"icedem.cu": ["--fmad=false"]}
+# Per-unit extra flags. The reference-mode units reproduce torch's one-op-per-
+# rounding FP64 arithmetic, so they forbid fused multiply-adds.
+EXTRA = {"icedem.cu": ["--fmad=false"], "icedem3d.cu": ["--fmad=false"]}
 
 
 def _nvcc() -> str:

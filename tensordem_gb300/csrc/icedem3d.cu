@@ -1,0 +1,1172 @@
+// 3-D reference mode: the FP64 bonded-sphere step of the reference's IceDEM3D
+// (src/tensordem/dem3d.py:564-1663), on sm_103a.
+//
+// Design. One CTA owns one instance and runs many steps per launch; phases of
+// a step are separated by block barriers and every scratch array lives in the
+// handle (L1/L2 resident at reference-mode sizes). A step is:
+//   1. objective shear strain per particle (dem3d.py:875-901),
+//   2. bond force, break test and commit, Maxwell branches, creep clock, one
+//      thread per bond (dem3d.py:984-1100, 1342-1360),
+//   3. cell hash of the positions: cell = floor(x / 2r) keyed into an open-
+//      addressing table, members of each cell in ascending particle order
+//      (dem3d.py:825-856 builds the same cells in a Python dict),
+//   4. contacts: each particle evaluates its pairs with higher ids over the 27
+//      neighbour cells, in the reference's pair-list order, and lists its
+//      pairs with lower ids in that order too (dem3d.py:1374-1514),
+//   5. assembly and semi-implicit Euler: each particle sums its force in the
+//      order of the reference's index_add_ calls (bond i-side then j-side,
+//      then per contact term the i-side then the j-side), then tool, platens
+//      and integration (dem3d.py:1516-1663).
+// Pair forces that the reference adds as exact zeros are skipped. Block
+// reductions run in a fixed order, so reruns are bitwise identical.
+//
+// This translation unit is compiled with --fmad=false: the reference runs
+// one torch op per arithmetic step, each rounded separately.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.h"
+
+namespace tdem {
+namespace icedem3d {
+
+constexpr int kMaxParticles = 65536;
+constexpr int kThreads = 512;
+constexpr int kContacts = 32;  // overlapping partners of one particle, per side
+constexpr int kHistory = 64;   // friction-history entries of one particle (as the pair's lower id)
+constexpr long long kCoordHalf = 1ll << 20;  // |cell coordinate| bound of the 21-bit packing
+constexpr unsigned long long kEmpty = ~0ull;
+constexpr double kEps = 2.220446049250313e-16;
+
+constexpr int kStatusNonfinite = 1;
+constexpr int kStatusContacts = 2;
+constexpr int kStatusHistory = 4;
+constexpr int kStatusEscaped = 8;
+
+static_assert(16 * (kThreads / 32) * 2 >= kThreads, "the count scan borrows the reduction scratch as ints");
+
+struct Dev {
+  // topology (constant)
+  const int* bi;
+  const int* bj;
+  const double* rest;
+  const double* ref;    // (B,3)
+  const double* inorm;  // (B,3)
+  const double* thr;    // (B) or null
+  const double* cref;   // (B) or null
+  const double* pinv;   // (n,9)
+  const unsigned char* frank;
+  const int* inc_off;    // (n+1)
+  const int* inc_split;  // (n) i-side entries of each particle
+  const int* inc_bond;   // (2B)
+  const int* inc_other;  // (2B)
+  // scratch
+  double* shear;             // (n)
+  double* abf;               // (B,3) active bond force
+  unsigned long long* pkey;  // (n) packed cell
+  int* pslot;                // (n) hash slot, -1: not hashed
+  unsigned long long* hkey;  // (H)
+  int* hcnt;
+  int* hstart;
+  int* hfill;
+  int* hmin;
+  int* members;   // (n)
+  int* ci_cnt;    // (n)
+  int* ci_j;      // (n, kContacts)
+  double* ci_v;   // (n, kContacts, 9): friction force, rolling force on j, contact force
+  int* cj_cnt;    // (n)
+  int* cj_i;      // (n, kContacts)
+  int* hist_cnt;  // (n)
+  int* hist_j;    // (n, kHistory)
+  double* hist_d; // (n, kHistory, 3)
+  double* ledger; // TDEM_L3_COUNT
+  int* status;
+  unsigned hmask;
+};
+
+// torch.linalg.vector_norm of a 3-vector on the CPU: one fused multiply-add
+// per component after the first square, then the square root.
+__device__ __forceinline__ double norm3(double x, double y, double z) { return sqrt(fma(z, z, fma(y, y, x * x))); }
+
+__device__ __forceinline__ unsigned hash_slot(unsigned long long key, unsigned mask) {
+  unsigned long long z = key * 0x9E3779B97F4A7C15ull;
+  z ^= z >> 31;
+  z *= 0xBF58476D1CE4E5B9ull;
+  z ^= z >> 29;
+  return (unsigned)z & mask;
+}
+
+__device__ __forceinline__ unsigned long long pack_cell(long long cx, long long cy, long long cz) {
+  return ((unsigned long long)(cx + kCoordHalf) << 42) | ((unsigned long long)(cy + kCoordHalf) << 21) |
+         (unsigned long long)(cz + kCoordHalf);
+}
+
+__device__ __forceinline__ int find_cell(const Dev& D, unsigned long long key) {
+  unsigned s = hash_slot(key, D.hmask);
+  for (unsigned probe = 0; probe <= D.hmask; ++probe) {
+    const unsigned long long k = D.hkey[s];
+    if (k == key) return (int)s;
+    if (k == kEmpty) return -1;
+    s = (s + 1) & D.hmask;
+  }
+  return -1;
+}
+
+// DEM3DConfig.friction_cone_limit (dem3d.py:453-498).
+__device__ __forceinline__ double cone_limit(int mode, const double* c, double ft_mag, double normal, double slip) {
+  if (mode == TDEM_CONE_TANH) {
+    const double blend = 0.5 * (1.0 - tanh(slip / c[2]));
+    return (c[0] + c[1] * blend) * normal;
+  }
+  if (mode == TDEM_CONE_DUAL) {
+    const double st = c[0] * normal;
+    return ft_mag > st ? c[1] * normal : st;
+  }
+  return c[0] * normal;
+}
+
+// x ** m as torch evaluates a scalar power (its special cases 1, 2, 3).
+__device__ __forceinline__ double torch_pow(double x, double m) {
+  if (m == 1.0) return x;
+  if (m == 2.0) return x * x;
+  if (m == 3.0) return x * x * x;
+  return pow(x, m);
+}
+
+// Spherical-cap submerged fraction (buoyancy_wet3d.py:134-155).
+__device__ __forceinline__ double submerged(const tdem_icedem3d_config& P, double z) {
+  const double r = P.radius;
+  const double h = z - P.water_level;
+  const double hc = fmin(fmax(h, -r), r);
+  const double a = r - hc;
+  double f = ((a * a) * (2.0 * r + hc)) / P.cap_denominator;
+  f = fmin(fmax(f, 0.0), 1.0);
+  if (h >= r) f = 0.0;
+  if (h <= -r) f = 1.0;
+  return f;
+}
+
+struct Out {
+  double* force;      // (n,3) or null
+  int mode;           // 0: steps; 1: one evaluation
+  int uf, uh;         // update_fracture, update_history
+  long long n_steps;
+  double time;
+};
+
+__global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config P, Dev D, tdem_icedem3d_state S,
+                                                             const double* __restrict__ loads, Out O) {
+  __shared__ double red[16 * (kThreads / 32)];
+  __shared__ int s_flags;
+  const int n = P.n, nb = P.nbond;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int M = P.n_branches;
+  const double two_r = 2.0 * P.radius;
+  const double width = 2.0 * P.radius;
+  const bool friction = P.cone != TDEM_CONE_OFF;
+  const bool platen_friction = P.platen_cone != TDEM_CONE_OFF;
+  double* pos = S.positions;
+  double* vel = S.velocities;
+  double time = O.time;
+  double min_margin = 1e300;
+  int hist_max = 0;
+  long long done = 0;
+  const long long total = O.mode == 1 ? 1 : O.n_steps;
+
+  if (tid == 0) s_flags = 0;
+  for (long long step = 0; step < total; ++step) {
+    const int uf = O.mode == 1 ? O.uf : 1;
+    const int uh = O.mode == 1 ? O.uh : 1;
+    int flags = 0;
+    // ---- clear the cell table; shear strain (dem3d.py:875-901)
+    for (unsigned s = tid; s <= D.hmask; s += nt) {
+      D.hkey[s] = kEmpty;
+      D.hcnt[s] = 0;
+      D.hfill[s] = 0;
+    }
+    if (uf && nb > 0) {
+      for (int k = tid; k < n; k += nt) {
+        double c[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) c[q] = 0.0;
+        for (int e = D.inc_off[k]; e < D.inc_off[k + 1]; ++e) {
+          const int b = D.inc_bond[e];
+          const int i = D.bi[b], j = D.bj[b];
+          const double qx = pos[3 * j] - pos[3 * i];
+          const double qy = pos[3 * j + 1] - pos[3 * i + 1];
+          const double qz = pos[3 * j + 2] - pos[3 * i + 2];
+          const double rx = D.ref[3 * b], ry = D.ref[3 * b + 1], rz = D.ref[3 * b + 2];
+          c[0] += qx * rx; c[1] += qx * ry; c[2] += qx * rz;
+          c[3] += qy * rx; c[4] += qy * ry; c[5] += qy * rz;
+          c[6] += qz * rx; c[7] += qz * ry; c[8] += qz * rz;
+        }
+        double shear = 0.0;
+        if (D.frank[k]) {
+          const double* p = D.pinv + 9 * (size_t)k;
+          double f[9];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+              f[3 * a + b] = (c[3 * a] * p[b] + c[3 * a + 1] * p[3 + b]) + c[3 * a + 2] * p[6 + b];
+          double e[9];
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              const double g = (f[a] * f[b] + f[3 + a] * f[3 + b]) + f[6 + a] * f[6 + b];
+              e[3 * a + b] = 0.5 * (g - (a == b ? 1.0 : 0.0));
+            }
+          const double mean = ((e[0] + e[4]) + e[8]) / 3.0;
+          e[0] = e[0] - mean;
+          e[4] = e[4] - mean;
+          e[8] = e[8] - mean;
+          // dev.square().sum(dim=(1, 2)): torch's contiguous inner sum of 9
+          // values: the tail element, then the four lanes of two 4-wide loads
+          double sq[9];
+#pragma unroll
+          for (int q = 0; q < 9; ++q) sq[q] = e[q] * e[q];
+          double s2 = sq[8];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) s2 = s2 + (sq[q] + sq[q + 4]);
+          shear = sqrt((2.0 / 3.0) * fmax(s2, 0.0));
+        }
+        D.shear[k] = shear;
+      }
+    }
+    __syncthreads();
+
+    // ---- bonds: force, break commit, Maxwell branches, creep (dem3d.py:1018-1100, 1342-1360)
+    double diss = 0.0;
+    for (int b = tid; b < nb; b += nt) {
+      const int i = D.bi[b], j = D.bj[b];
+      const double dx = pos[3 * j] - pos[3 * i];
+      const double dy = pos[3 * j + 1] - pos[3 * i + 1];
+      const double dz = pos[3 * j + 2] - pos[3 * i + 2];
+      const double dist = norm3(dx, dy, dz);
+      double nx, ny, nz;
+      if (dist > kEps) {
+        const double dc = fmax(dist, kEps);
+        nx = dx / dc;
+        ny = dy / dc;
+        nz = dz / dc;
+      } else {
+        nx = D.inorm[3 * b];
+        ny = D.inorm[3 * b + 1];
+        nz = D.inorm[3 * b + 2];
+      }
+      const double ext = dist - D.rest[b];
+      bool alive = S.alive[b] != 0;
+      double mag;
+      if (M == 0) {
+        mag = P.bond_k * ext;
+      } else {
+        double* off = S.branch_offsets + (size_t)b * M;
+        if (uh) {
+          // advance_branches (ice_bond_viscoelastic.py:186-253), exact over the increment
+          const double d_old = S.elongation_prev[b];
+          const double d_dot = (ext - d_old) / P.dt;
+          double dis = 0.0;
+          for (int a = 0; a < M; ++a) {
+            const double tau = P.branch_tau[a];
+            const double s0 = d_old - off[a];
+            const double amp = d_dot * tau;
+            const double om = P.branch_one_minus[a], dec = P.branch_decay[a];
+            const double s_new = amp * om + s0 * dec;
+            const double sa = s0 - amp;
+            const double i2 = ((amp * amp) * P.dt + (((2.0 * amp) * sa) * tau) * om) +
+                              ((0.5 * (sa * sa)) * tau) * (om * (1.0 + dec));
+            dis = dis + (P.branch_k[a] / tau) * i2;
+            off[a] = alive ? ext - s_new : ext;
+          }
+          if (alive) diss += dis;
+          S.elongation_prev[b] = ext;
+        }
+        mag = P.bond_k * ext;
+        for (int a = 0; a < M; ++a) mag = mag + P.branch_k[a] * (ext - off[a]);
+      }
+      if (uf && alive) {
+        const double strain = ext / D.rest[b];
+        const double sb = 0.5 * (D.shear[i] + D.shear[j]);
+        const double thr = D.thr ? D.thr[b] : P.breaking_strain;
+        const bool tf = strain > thr;
+        const bool sf = sb > P.shear_breaking_strain;
+        int mode = 0;
+        if (tf || sf) {
+          mode = (tf ? 1 : 0) + 2 * (sf ? 1 : 0);
+        } else {
+          min_margin = fmin(min_margin, fmin((thr - strain) / thr,
+                                             (P.shear_breaking_strain - sb) / P.shear_breaking_strain));
+          if (P.creep) {
+            // Kachanov clock (ice_bond_viscoelastic.py:284-297, dem3d.py:1079-1100)
+            const double ratio = fabs(mag) / fmax(D.cref[b], 1e-30);
+            const double dmg = S.damage[b] + torch_pow(ratio, P.creep_exponent) * P.creep_dt_over_time;
+            S.damage[b] = dmg;
+            if (dmg >= 1.0) mode = 4;
+          }
+        }
+        if (mode) {
+          alive = false;
+          S.alive[b] = 0;
+          S.failure_mode[b] = (unsigned char)mode;
+          S.failure_time_s[b] = time;
+          S.failure_extension_m[b] = ext;
+          double energy;
+          if (M == 0) {
+            energy = (0.5 * P.bond_k) * (ext * ext);
+          } else {
+            const double* off = S.branch_offsets + (size_t)b * M;
+            energy = (0.5 * P.bond_k) * (ext * ext);
+            for (int a = 0; a < M; ++a) {
+              const double s = ext - off[a];
+              energy = energy + (0.5 * P.branch_k[a]) * (s * s);
+            }
+          }
+          S.failure_energy_J[b] = energy;
+        }
+      }
+      D.abf[3 * b] = alive ? mag * nx : 0.0;
+      D.abf[3 * b + 1] = alive ? mag * ny : 0.0;
+      D.abf[3 * b + 2] = alive ? mag * nz : 0.0;
+    }
+    if (M > 0 && uh) {
+      // cumulative dashpot dissipation of the bonds alive before the commit
+      double v[1] = {diss}, tot[1];
+      block_sum_f64<1>(v, red, tot);
+      if (tid == 0 && S.bond_dissipation) S.bond_dissipation[0] = S.bond_dissipation[0] + tot[0];
+    }
+
+    // ---- cell hash (dem3d.py:825-856)
+    for (int k = tid; k < n; k += nt) {
+      const double fx = floor(pos[3 * k] / width);
+      const double fy = floor(pos[3 * k + 1] / width);
+      const double fz = floor(pos[3 * k + 2] / width);
+      const double lim = (double)kCoordHalf - 2.0;
+      int slot = -1;
+      if (fabs(fx) < lim && fabs(fy) < lim && fabs(fz) < lim) {
+        const unsigned long long key = pack_cell((long long)fx, (long long)fy, (long long)fz);
+        unsigned s = hash_slot(key, D.hmask);
+        for (unsigned probe = 0; probe <= D.hmask; ++probe) {
+          const unsigned long long prev = atomicCAS(&D.hkey[s], kEmpty, key);
+          if (prev == kEmpty || prev == key) {
+            slot = (int)s;
+            break;
+          }
+          s = (s + 1) & D.hmask;
+        }
+        if (slot >= 0) {  // always: the table has at least 2n slots
+          D.pkey[k] = key;
+          atomicAdd(&D.hcnt[slot], 1);
+        }
+      } else {
+        flags |= (fx == fx && fy == fy && fz == fz) ? kStatusEscaped : kStatusNonfinite;
+      }
+      D.pslot[k] = slot;
+    }
+    __syncthreads();
+    // exclusive scan of the cell counts (each thread a contiguous chunk)
+    {
+      const unsigned H = D.hmask + 1;
+      const unsigned per = (H + nt - 1) / nt;
+      const unsigned lo = min(H, tid * per), hi = min(H, lo + per);
+      int local = 0;
+      for (unsigned s = lo; s < hi; ++s) local += D.hcnt[s];
+      int* sc = reinterpret_cast<int*>(red);
+      sc[tid] = local;
+      __syncthreads();
+      if (tid == 0) {
+        int run = 0;
+        for (int t = 0; t < nt; ++t) {
+          const int c = sc[t];
+          sc[t] = run;
+          run += c;
+        }
+      }
+      __syncthreads();
+      int run = sc[tid];
+      for (unsigned s = lo; s < hi; ++s) {
+        D.hstart[s] = run;
+        run += D.hcnt[s];
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < n; k += nt) {
+      const int s = D.pslot[k];
+      if (s >= 0) D.members[D.hstart[s] + atomicAdd(&D.hfill[s], 1)] = k;
+    }
+    __syncthreads();
+    for (unsigned s = tid; s <= D.hmask; s += nt) {
+      const int c = D.hcnt[s];
+      if (c == 0) continue;
+      int* m = D.members + D.hstart[s];
+      for (int a = 1; a < c; ++a) {  // members in ascending particle order
+        const int x = m[a];
+        int b = a - 1;
+        while (b >= 0 && m[b] > x) {
+          m[b + 1] = m[b];
+          --b;
+        }
+        m[b + 1] = x;
+      }
+      D.hmin[s] = m[0];
+    }
+    __syncthreads();
+
+    // ---- contacts (dem3d.py:1374-1514)
+    double acc_fp = 0.0, acc_rp = 0.0, acc_en = 0.0, acc_nc = 0.0;
+    for (int k = tid; k < n; k += nt) {
+      int nci = 0, ncj = 0;
+      if (D.pslot[k] >= 0) {
+        const unsigned long long kk = D.pkey[k];
+        const long long cx = (long long)(kk >> 42) - kCoordHalf;
+        const long long cy = (long long)((kk >> 21) & ((1ull << 21) - 1)) - kCoordHalf;
+        const long long cz = (long long)(kk & ((1ull << 21) - 1)) - kCoordHalf;
+        const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
+        const double vkx = vel[3 * k], vky = vel[3 * k + 1], vkz = vel[3 * k + 2];
+        const bool fk = S.fixed[k] != 0;
+        unsigned long long cj_key[kContacts];
+        int* hj = D.hist_j + (size_t)k * kHistory;
+        double* hd = D.hist_d + (size_t)k * kHistory * 3;
+        int hc = friction ? D.hist_cnt[k] : 0;
+        const int ib0 = D.inc_off[k], ib1 = ib0 + D.inc_split[k];
+        for (int dx = -1; dx <= 1; ++dx)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+              const int s = find_cell(D, pack_cell(cx + dx, cy + dy, cz + dz));
+              if (s < 0) continue;
+              const int m0 = D.hstart[s], m1 = m0 + D.hcnt[s];
+              for (int m = m0; m < m1; ++m) {
+                const int j = D.members[m];
+                if (j == k) continue;
+                if (j < k) {
+                  // pair (j, k): k is its second particle; same arithmetic as j's side
+                  const double ex = pkx - pos[3 * j], ey = pky - pos[3 * j + 1], ez = pkz - pos[3 * j + 2];
+                  const double ov = fmax(two_r - norm3(ex, ey, ez), 0.0);
+                  if (!(ov > 0.0)) continue;
+                  if (ncj == kContacts) {
+                    flags |= kStatusContacts;
+                    continue;
+                  }
+                  // reference order of this side: by the cell's first particle, then id
+                  const unsigned long long key = ((unsigned long long)D.hmin[s] << 32) | (unsigned)j;
+                  int a = ncj - 1;
+                  while (a >= 0 && cj_key[a] > key) {
+                    cj_key[a + 1] = cj_key[a];
+                    --a;
+                  }
+                  cj_key[a + 1] = key;
+                  ++ncj;
+                  continue;
+                }
+                const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
+                const double dist = norm3(ex, ey, ez);
+                const double ov = fmax(two_r - dist, 0.0);
+                if (!(ov > 0.0)) continue;
+                if (nci == kContacts) {
+                  flags |= kStatusContacts;
+                  continue;
+                }
+                bool balive = false;
+                for (int e = ib0; e < ib1; ++e)
+                  if (D.inc_other[e] == j) {
+                    balive = S.alive[D.inc_bond[e]] != 0;
+                    break;
+                  }
+                const double dc = fmax(dist, kEps);
+                const double nx = ex / dc, ny = ey / dc, nz = ez / dc;
+                const double vjx = vel[3 * j], vjy = vel[3 * j + 1], vjz = vel[3 * j + 2];
+                const double rvx = vjx - vkx, rvy = vjy - vky, rvz = vjz - vkz;
+                const double vn = (rvx * nx + rvy * ny) + rvz * nz;
+                const bool pinned = P.any_fixed && (fk != (S.fixed[j] != 0));
+                const double k_local = P.hertz ? P.hertz_kn * sqrt(ov) : P.contact_k;
+                double gamma = 0.0;
+                if (P.damping == 2) {
+                  gamma = P.damping_c;
+                } else if (P.damping == 1) {
+                  gamma = P.hertz ? P.damping_c * sqrt(k_local * (pinned ? P.mass_pinned : P.mass_mobile))
+                                  : (pinned ? P.gamma_pinned : P.gamma_mobile);
+                }
+                double mag = fmax(k_local * ov - gamma * vn, 0.0);
+                if (balive) mag = 0.0;
+                else acc_en += P.hertz ? P.hertz_pot * pow(ov, 2.5) : (0.5 * P.contact_k) * (ov * ov);
+                double* out = D.ci_v + ((size_t)k * kContacts + nci) * 9;
+                const double vtx = rvx - vn * nx, vty = rvy - vn * ny, vtz = rvz - vn * nz;
+                if (friction) {
+                  // Cundall-Strack spring with the pair's stored displacement
+                  int h = -1;
+                  for (int q = 0; q < hc; ++q)
+                    if (hj[q] == j) {
+                      h = q;
+                      break;
+                    }
+                  double tx = 0.0, ty = 0.0, tz = 0.0;
+                  if (h >= 0) {
+                    tx = hd[3 * h];
+                    ty = hd[3 * h + 1];
+                    tz = hd[3 * h + 2];
+                  }
+                  if (uh) {
+                    tx = tx + vtx * P.dt;
+                    ty = ty + vty * P.dt;
+                    tz = tz + vtz * P.dt;
+                  }
+                  const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
+                  const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
+                  const double fm = norm3(fx, fy, fz);
+                  const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
+                  const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
+                  const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
+                  out[0] = Fx;
+                  out[1] = Fy;
+                  out[2] = Fz;
+                  acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
+                  if (uh) {
+                    const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
+                    if (h >= 0) {
+                      hd[3 * h] = sx;
+                      hd[3 * h + 1] = sy;
+                      hd[3 * h + 2] = sz;
+                    } else if (sx != 0.0 || sy != 0.0 || sz != 0.0) {
+                      // an absent entry reads as zero, so only non-zero values need a slot
+                      if (hc == kHistory) {
+                        flags |= kStatusHistory;
+                      } else {
+                        hj[hc] = j;
+                        hd[3 * hc] = sx;
+                        hd[3 * hc + 1] = sy;
+                        hd[3 * hc + 2] = sz;
+                        ++hc;
+                      }
+                    }
+                  }
+                }
+                if (P.rolling) {
+                  // rolling-resistance couple (dem3d.py:1242-1299)
+                  const double vtm = norm3(vtx, vty, vtz);
+                  double hx = 0.0, hy = 0.0, hz = 0.0;
+                  if (vtm > 1e-15) {
+                    const double vc = fmax(vtm, kEps);
+                    hx = vtx / vc;
+                    hy = vty / vc;
+                    hz = vtz / vc;
+                  }
+                  const double fm = -(P.roll_mu * mag);
+                  const double jx = fm * hx, jy = fm * hy, jz = fm * hz;
+                  out[3] = jx;
+                  out[4] = jy;
+                  out[5] = jz;
+                  acc_rp += ((-jx) * (vkx - vjx) + (-jy) * (vky - vjy)) + (-jz) * (vkz - vjz);
+                }
+                const double cm = -mag;
+                out[6] = cm * nx;
+                out[7] = cm * ny;
+                out[8] = cm * nz;
+                D.ci_j[(size_t)k * kContacts + nci] = j;
+                ++nci;
+              }
+            }
+        if (friction) {
+          D.hist_cnt[k] = hc;
+          hist_max = max(hist_max, hc);
+        }
+        for (int a = 0; a < ncj; ++a) D.cj_i[(size_t)k * kContacts + a] = (int)(cj_key[a] & 0xffffffffull);
+      }
+      D.ci_cnt[k] = nci;
+      D.cj_cnt[k] = ncj;
+      acc_nc += (double)nci;
+    }
+    __syncthreads();
+
+    // ---- assembly and semi-implicit Euler (dem3d.py:1326-1340, 1516-1663)
+    double acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = 0.0;
+    const double tpx = P.tool_start[0] + time * P.tool_velocity[0];
+    const double tpy = P.tool_start[1] + time * P.tool_velocity[1];
+    const double tpz = P.tool_start[2] + time * P.tool_velocity[2];
+    const double top_z = P.top_start_z + time * P.top_velocity;
+    const double bottom_z = P.bottom_start_z + time * P.bottom_velocity;
+    double lp[4] = {0.0, 0.0, 0.0, 0.0}, lvx = 0.0, lvy = 0.0;
+    if (P.platens & 4) {
+      for (int q = 0; q < 4; ++q) lp[q] = S.lateral_position[q];
+      lvx = S.lateral_velocity[0];
+      lvy = S.lateral_velocity[2];
+    }
+    for (int k = tid; k < n; k += nt) {
+      const double px = pos[3 * k], py = pos[3 * k + 1], pz = pos[3 * k + 2];
+      const double vx = vel[3 * k], vy = vel[3 * k + 1], vz = vel[3 * k + 2];
+      double fx = (-P.drag) * vx, fy = (-P.drag) * vy, fz = (-P.drag) * vz;
+      if (P.body & 1) {
+        double bx = 0.0, by = 0.0, bz = 0.0;
+        if (P.gravity_force > 0.0) bz = bz - P.gravity_force;
+        if (P.body & 2) {
+          const double fs = submerged(P, pz);
+          bz = bz + P.buoyancy_force * fs;
+          if (P.body & 4) {
+            const double c = P.wet_drag * fs;
+            bx = bx - c * vx;
+            by = by - c * vy;
+            bz = bz - c * vz;
+          }
+        }
+        fx = fx + bx;
+        fy = fy + by;
+        fz = fz + bz;
+      }
+      if (loads) {
+        fx = fx + loads[3 * k];
+        fy = fy + loads[3 * k + 1];
+        fz = fz + loads[3 * k + 2];
+      }
+      const int e0 = D.inc_off[k], es = e0 + D.inc_split[k], e1 = D.inc_off[k + 1];
+      for (int e = e0; e < e1; ++e) {
+        const int b = D.inc_bond[e];
+        if (!S.alive[b]) continue;
+        const double* a = D.abf + 3 * (size_t)b;
+        if (e < es) {
+          fx += a[0];
+          fy += a[1];
+          fz += a[2];
+        } else {
+          fx += -a[0];
+          fy += -a[1];
+          fz += -a[2];
+        }
+      }
+      const int nci = D.ci_cnt[k], ncj = D.cj_cnt[k];
+      const double* mine = D.ci_v + (size_t)k * kContacts * 9;
+      // value slot `o` of the pair (i, k) in i's contact list
+      auto theirs = [&](int c) -> const double* {
+        const int i = D.cj_i[(size_t)k * kContacts + c];
+        const int cnt = D.ci_cnt[i];
+        const int* js = D.ci_j + (size_t)i * kContacts;
+        for (int q = 0; q < cnt; ++q)
+          if (js[q] == k) return D.ci_v + ((size_t)i * kContacts + q) * 9;
+        return nullptr;
+      };
+      if (friction) {
+        for (int c = 0; c < nci; ++c) {
+          fx += mine[9 * c];
+          fy += mine[9 * c + 1];
+          fz += mine[9 * c + 2];
+        }
+        for (int c = 0; c < ncj; ++c) {
+          const double* t = theirs(c);
+          if (!t) continue;
+          fx += -t[0];
+          fy += -t[1];
+          fz += -t[2];
+        }
+      }
+      if (P.rolling) {
+        for (int c = 0; c < nci; ++c) {
+          fx += -mine[9 * c + 3];
+          fy += -mine[9 * c + 4];
+          fz += -mine[9 * c + 5];
+        }
+        for (int c = 0; c < ncj; ++c) {
+          const double* t = theirs(c);
+          if (!t) continue;
+          fx += t[3];
+          fy += t[4];
+          fz += t[5];
+        }
+      }
+      for (int c = 0; c < nci; ++c) {
+        fx += mine[9 * c + 6];
+        fy += mine[9 * c + 7];
+        fz += mine[9 * c + 8];
+      }
+      for (int c = 0; c < ncj; ++c) {
+        const double* t = theirs(c);
+        if (!t) continue;
+        fx += -t[6];
+        fy += -t[7];
+        fz += -t[8];
+      }
+      // spherical indenter (dem3d.py:1519-1532)
+      {
+        const double dx = px - tpx, dy = py - tpy, dz = pz - tpz;
+        const double dist = norm3(dx, dy, dz);
+        double nx = 0.0, ny = 0.0, nz = -1.0;
+        if (dist > kEps) {
+          const double dc = fmax(dist, kEps);
+          nx = dx / dc;
+          ny = dy / dc;
+          nz = dz / dc;
+        }
+        const double ov = fmax((P.radius + P.tool_radius) - dist, 0.0);
+        const double vn = ((vx - P.tool_velocity[0]) * nx + (vy - P.tool_velocity[1]) * ny) +
+                          (vz - P.tool_velocity[2]) * nz;
+        const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.contact_k * ov;
+        double mag = fmax(el - P.tool_damping * vn, 0.0);
+        if (!(ov > 0.0)) mag = 0.0;
+        const double tx = mag * nx, ty = mag * ny, tz = mag * nz;
+        acc[0] += tx;
+        acc[1] += ty;
+        acc[2] += tz;
+        fx += tx;
+        fy += ty;
+        fz += tz;
+      }
+      // plane platens (dem3d.py:1534-1580) with Coulomb friction (dem3d.py:1187-1240)
+      for (int side = 0; side < 2; ++side) {
+        if (!(P.platens & (1 << side))) continue;
+        double ov, mag;
+        if (side == 0) {
+          ov = fmax((pz + P.radius) - top_z, 0.0);
+          const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
+          mag = fmax(el + P.platen_c * (vz - P.top_velocity), 0.0);
+          if (!(ov > 0.0)) mag = 0.0;
+          fz += -mag;
+          acc[3] += mag;
+        } else {
+          ov = fmax((bottom_z + P.radius) - pz, 0.0);
+          const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
+          mag = fmax(el - P.platen_c * (vz - P.bottom_velocity), 0.0);
+          if (!(ov > 0.0)) mag = 0.0;
+          fz += mag;
+          acc[4] += -mag;
+        }
+        if (platen_friction) {
+          double* td = (side == 0 ? S.top_tangential : S.bottom_tangential) + 3 * (size_t)k;
+          const bool touch = ov > 0.0;
+          const double ux = touch ? vx : 0.0, uy = touch ? vy : 0.0;
+          const double slip = norm3(ux, uy, 0.0);
+          double tx = td[0], ty = td[1], tz = td[2];
+          if (uh) {
+            tx = tx + ux * P.dt;
+            ty = ty + uy * P.dt;
+            tz = tz + 0.0 * P.dt;
+            if (!touch) tx = ty = tz = 0.0;
+            td[0] = tx;
+            td[1] = ty;
+            td[2] = tz;
+          }
+          const double kk = -P.platen_kt;
+          const double sx = kk * tx, sy = kk * ty, sz = kk * tz;
+          const double sm = norm3(sx, sy, sz);
+          const double lim = cone_limit(P.platen_cone, P.platen_cone_c, sm, mag, slip);
+          const double sc = sm > lim ? lim / fmax(sm, kEps) : 1.0;
+          fx += sx * sc;
+          fy += sy * sc;
+          fz += sz * sc;
+        }
+      }
+      if (P.platens & 4) {
+        // lateral servo platens (dem3d.py:1582-1623)
+        const double r = P.radius;
+        double ov = fmax((lp[0] - px) + r, 0.0);
+        double mg = fmax(P.lateral_k * ov - P.lateral_c * (vx - lvx), 0.0);
+        if (!(ov > 0.0)) mg = 0.0;
+        fx += mg;
+        acc[5] += -mg;
+        ov = fmax((px + r) - lp[1], 0.0);
+        mg = fmax(P.lateral_k * ov + P.lateral_c * (vx - lvx), 0.0);
+        if (!(ov > 0.0)) mg = 0.0;
+        fx -= mg;
+        acc[6] += mg;
+        ov = fmax((lp[2] - py) + r, 0.0);
+        mg = fmax(P.lateral_k * ov - P.lateral_c * (vy - lvy), 0.0);
+        if (!(ov > 0.0)) mg = 0.0;
+        fy += mg;
+        acc[7] += -mg;
+        ov = fmax((py + r) - lp[3], 0.0);
+        mg = fmax(P.lateral_k * ov + P.lateral_c * (vy - lvy), 0.0);
+        if (!(ov > 0.0)) mg = 0.0;
+        fy -= mg;
+        acc[8] += mg;
+      }
+      if (O.mode == 1) {
+        O.force[3 * k] = fx;
+        O.force[3 * k + 1] = fy;
+        O.force[3 * k + 2] = fz;
+        continue;
+      }
+      double ax = fx / P.mass, ay = fy / P.mass, az = fz / P.mass;
+      const bool fixed = S.fixed[k] != 0;
+      if (fixed) ax = ay = az = 0.0;
+      double nvx = vx + ax * P.dt, nvy = vy + ay * P.dt, nvz = vz + az * P.dt;
+      if (fixed) nvx = nvy = nvz = 0.0;
+      double npx = px + nvx * P.dt, npy = py + nvy * P.dt, npz = pz + nvz * P.dt;
+      if (fixed) {
+        npx = S.initial_positions[3 * k];
+        npy = S.initial_positions[3 * k + 1];
+        npz = S.initial_positions[3 * k + 2];
+      }
+      vel[3 * k] = nvx;
+      vel[3 * k + 1] = nvy;
+      vel[3 * k + 2] = nvz;
+      pos[3 * k] = npx;
+      pos[3 * k + 1] = npy;
+      pos[3 * k + 2] = npz;
+      if (!(isfinite(npx) && isfinite(npy) && isfinite(npz) && isfinite(nvx) && isfinite(nvy) && isfinite(nvz)))
+        flags |= kStatusNonfinite;
+    }
+    acc[9] = acc_fp;
+    acc[10] = acc_rp;
+    acc[11] = acc_en;
+    acc[12] = acc_nc;
+    if (flags) atomicOr(&s_flags, flags);
+    double tot[16];
+    block_sum_f64<16>(acc, red, tot);
+    const double mm = block_min_f64(min_margin, red);
+    const double hm = -block_min_f64(-(double)hist_max, red);
+    if (tid == 0) {
+      double* L = D.ledger;
+      L[TDEM_L3_REACTION_X] = -tot[0];
+      L[TDEM_L3_REACTION_Y] = -tot[1];
+      L[TDEM_L3_REACTION_Z] = -tot[2];
+      L[TDEM_L3_TOP_REACTION_Z] = tot[3];
+      L[TDEM_L3_BOTTOM_REACTION_Z] = tot[4];
+      for (int q = 0; q < 4; ++q) L[TDEM_L3_LATERAL_0 + q] = tot[5 + q];
+      if (uh) {
+        L[TDEM_L3_FRICTION_POWER] = tot[9];
+        L[TDEM_L3_ROLLING_POWER] = tot[10];
+      }
+      L[TDEM_L3_CONTACT_ENERGY] = tot[11];
+      L[TDEM_L3_CONTACTS] = tot[12];
+      L[TDEM_L3_HISTORY_MAX] = hm;
+      L[TDEM_L3_MIN_BREAK_MARGIN] = fmin(L[TDEM_L3_MIN_BREAK_MARGIN], mm);
+    }
+    // every thread takes the same exit decision: the flags were OR-ed in before
+    // the reductions' barriers, and s_flags is never cleared inside the loop
+    const int f = s_flags;
+    if (O.mode == 1) {
+      done = 1;
+      if (tid == 0 && f) *D.status = f;
+      break;
+    }
+    if ((P.platens & 4) && tid < 4) S.lateral_position[tid] = lp[tid] + S.lateral_velocity[tid] * P.dt;
+    time = time + P.dt;
+    done = step + 1;
+    if (f) {
+      if (tid == 0) *D.status = f;
+      break;
+    }
+  }
+  if (tid == 0) D.ledger[TDEM_L3_STEPS_DONE] = (double)done;
+}
+
+}  // namespace icedem3d
+}  // namespace tdem
+
+using namespace tdem::icedem3d;
+
+struct tdem_icedem3d {
+  tdem_icedem3d_config cfg{};
+  Dev dev{};
+  std::vector<void*> allocs;
+  double* ledger_host = nullptr;
+  int* status_host = nullptr;
+  std::string err;
+  int n = 0, nb = 0;
+};
+
+namespace {
+
+std::string g_create_error3;
+
+template <class T>
+int dalloc(tdem_icedem3d* h, T** p, size_t count) {
+  void* q = nullptr;
+  TDEM_CUDA_TRY(&h->err, cudaMalloc(&q, std::max<size_t>(1, count) * sizeof(T)));
+  h->allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return TDEM_OK;
+}
+
+template <class T>
+int dupload(tdem_icedem3d* h, const T** dst, const T* src, size_t count) {
+  T* p = nullptr;
+  int rc = dalloc(h, &p, count);
+  if (rc) return rc;
+  if (count) TDEM_CUDA_TRY(&h->err, cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  *dst = p;
+  return TDEM_OK;
+}
+
+void destroy(tdem_icedem3d* h) {
+  if (!h) return;
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->ledger_host) cudaFreeHost(h->ledger_host);
+  if (h->status_host) cudaFreeHost(h->status_host);
+  delete h;
+}
+
+int check_state(tdem_icedem3d* h, const tdem_icedem3d_state* st) {
+  const tdem_icedem3d_config& c = h->cfg;
+  if (!st || !st->positions || !st->velocities || !st->initial_positions || !st->fixed)
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "state needs positions, velocities, initial positions and fixed");
+  if (h->nb > 0 && (!st->alive || !st->failure_mode || !st->failure_time_s || !st->failure_extension_m ||
+                    !st->failure_energy_J))
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "state needs the bond arrays");
+  if (c.n_branches > 0 && (!st->branch_offsets || !st->elongation_prev))
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "Maxwell bonds need branch offsets and elongations");
+  if (c.creep && !st->damage) return tdem::fail(&h->err, TDEM_ERR_BADARG, "creep needs the damage array");
+  if (c.platen_cone != TDEM_CONE_OFF && (!st->top_tangential || !st->bottom_tangential))
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "platen friction needs the platen spring offsets");
+  if ((c.platens & 4) && (!st->lateral_position || !st->lateral_velocity))
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "lateral platens need their positions and velocities");
+  return TDEM_OK;
+}
+
+int launch(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads, Out o, cudaStream_t s) {
+  int rc = check_state(h, st);
+  if (rc) return rc;
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(h->dev.status, 0, sizeof(int), s));
+  icedem3d_kernel<<<1, kThreads, 0, s>>>(h->cfg, h->dev, *st, loads, o);
+  TDEM_CUDA_TRY(&h->err, cudaGetLastError());
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(h->status_host, h->dev.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
+  const int f = *h->status_host;
+  if (f & kStatusNonfinite)
+    return tdem::fail(&h->err, TDEM_ERR_NONFINITE, "non-finite DEM3D state; reduce dt or contact stiffness");
+  if (f & kStatusContacts)
+    return tdem::fail(&h->err, TDEM_ERR_CAPACITY,
+                      "a particle overlaps more than " + std::to_string(kContacts) + " others");
+  if (f & kStatusHistory)
+    return tdem::fail(&h->err, TDEM_ERR_CAPACITY,
+                      "a particle's friction history exceeds " + std::to_string(kHistory) + " partners");
+  if (f & kStatusEscaped)
+    return tdem::fail(&h->err, TDEM_ERR_CAPACITY, "a particle left the 2^20-cell hash range");
+  return TDEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tdem_icedem3d_max_particles(void) { return kMaxParticles; }
+
+int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_topology* topo,
+                         tdem_icedem3d** out) {
+  if (!out) return TDEM_ERR_BADARG;
+  *out = nullptr;
+  if (!cfg || !topo) return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "null config or topology");
+  const int n = cfg->n, nb = cfg->nbond;
+  if (n < 2 || n > kMaxParticles)
+    return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "n must be in 2.." + std::to_string(kMaxParticles));
+  if (nb < 0) return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "nbond must be >= 0");
+  if (cfg->n_branches < 0 || cfg->n_branches > TDEM_ICE3D_MAX_BRANCHES)
+    return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "n_branches must be in 0..4");
+  if (!(cfg->dt > 0.0) || !(cfg->mass > 0.0) || !(cfg->radius > 0.0))
+    return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "dt, mass and radius must be positive");
+  if (nb > 0 && (!topo->bond_i || !topo->bond_j || !topo->rest_length || !topo->reference ||
+                 !topo->initial_normal))
+    return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "bond topology arrays missing");
+  if (!topo->pinv || !topo->full_rank)
+    return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "per-particle pseudo-inverses missing");
+  if (cfg->creep && !topo->creep_reference)
+    return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "creep needs the per-bond reference force");
+  // per-particle incidence: i side (ascending j), then j side (ascending i)
+  std::vector<int> cnt_i(n, 0), cnt_j(n, 0);
+  long long prev = -1;
+  for (int b = 0; b < nb; ++b) {
+    const int i = topo->bond_i[b], j = topo->bond_j[b];
+    if (i < 0 || j <= i || j >= n)
+      return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "bond " + std::to_string(b) + " is not 0 <= i < j < n");
+    const long long key = (long long)i * n + j;
+    if (key <= prev) return tdem::fail(&g_create_error3, TDEM_ERR_BADARG, "bonds must be sorted by i * n + j");
+    prev = key;
+    ++cnt_i[i];
+    ++cnt_j[j];
+  }
+  std::vector<int> off(n + 1, 0), split(n), inc_bond(2 * (size_t)nb), inc_other(2 * (size_t)nb);
+  for (int k = 0; k < n; ++k) {
+    off[k + 1] = off[k] + cnt_i[k] + cnt_j[k];
+    split[k] = cnt_i[k];
+  }
+  std::vector<int> fi(n), fj(n);
+  for (int k = 0; k < n; ++k) {
+    fi[k] = off[k];
+    fj[k] = off[k] + cnt_i[k];
+  }
+  for (int b = 0; b < nb; ++b) {
+    const int i = topo->bond_i[b], j = topo->bond_j[b];
+    inc_bond[fi[i]] = b;
+    inc_other[fi[i]++] = j;
+    inc_bond[fj[j]] = b;
+    inc_other[fj[j]++] = i;
+  }
+  tdem_icedem3d* h = new tdem_icedem3d();
+  h->cfg = *cfg;
+  h->n = n;
+  h->nb = nb;
+  Dev& D = h->dev;
+  unsigned H = 64;
+  while (H < 2u * (unsigned)n) H <<= 1;
+  D.hmask = H - 1;
+  int rc = 0;
+  auto fail_out = [&](int code) {
+    g_create_error3 = h->err;
+    destroy(h);
+    return code;
+  };
+  if ((rc = dupload(h, &D.bi, topo->bond_i, nb)) || (rc = dupload(h, &D.bj, topo->bond_j, nb)) ||
+      (rc = dupload(h, &D.rest, topo->rest_length, nb)) || (rc = dupload(h, &D.ref, topo->reference, 3 * (size_t)nb)) ||
+      (rc = dupload(h, &D.inorm, topo->initial_normal, 3 * (size_t)nb)) ||
+      (rc = dupload(h, &D.pinv, topo->pinv, 9 * (size_t)n)) ||
+      (rc = dupload(h, &D.frank, topo->full_rank, (size_t)n)))
+    return fail_out(rc);
+  D.thr = nullptr;
+  D.cref = nullptr;
+  if (topo->threshold && (rc = dupload(h, &D.thr, topo->threshold, nb))) return fail_out(rc);
+  if (topo->creep_reference && (rc = dupload(h, &D.cref, topo->creep_reference, nb))) return fail_out(rc);
+  const int* p_off = nullptr;
+  const int* p_split = nullptr;
+  const int* p_bond = nullptr;
+  const int* p_other = nullptr;
+  if ((rc = dupload(h, &p_off, off.data(), off.size())) || (rc = dupload(h, &p_split, split.data(), split.size())) ||
+      (rc = dupload(h, &p_bond, inc_bond.data(), inc_bond.size())) ||
+      (rc = dupload(h, &p_other, inc_other.data(), inc_other.size())))
+    return fail_out(rc);
+  D.inc_off = p_off;
+  D.inc_split = p_split;
+  D.inc_bond = p_bond;
+  D.inc_other = p_other;
+  if ((rc = dalloc(h, &D.shear, n)) || (rc = dalloc(h, &D.abf, 3 * (size_t)nb)) || (rc = dalloc(h, &D.pkey, n)) ||
+      (rc = dalloc(h, &D.pslot, n)) || (rc = dalloc(h, &D.hkey, H)) || (rc = dalloc(h, &D.hcnt, H)) ||
+      (rc = dalloc(h, &D.hstart, H)) || (rc = dalloc(h, &D.hfill, H)) || (rc = dalloc(h, &D.hmin, H)) ||
+      (rc = dalloc(h, &D.members, n)) || (rc = dalloc(h, &D.ci_cnt, n)) ||
+      (rc = dalloc(h, &D.ci_j, (size_t)n * kContacts)) || (rc = dalloc(h, &D.ci_v, (size_t)n * kContacts * 9)) ||
+      (rc = dalloc(h, &D.cj_cnt, n)) || (rc = dalloc(h, &D.cj_i, (size_t)n * kContacts)) ||
+      (rc = dalloc(h, &D.hist_cnt, n)) || (rc = dalloc(h, &D.hist_j, (size_t)n * kHistory)) ||
+      (rc = dalloc(h, &D.hist_d, (size_t)n * kHistory * 3)) || (rc = dalloc(h, &D.ledger, TDEM_L3_COUNT)) ||
+      (rc = dalloc(h, &D.status, 1)))
+    return fail_out(rc);
+  std::vector<double> led(TDEM_L3_COUNT, 0.0);
+  led[TDEM_L3_MIN_BREAK_MARGIN] = 1e300;
+  if (cudaMemcpy(D.ledger, led.data(), led.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(D.hist_cnt, 0, (size_t)n * sizeof(int)) != cudaSuccess ||
+      cudaMemset(D.ci_cnt, 0, (size_t)n * sizeof(int)) != cudaSuccess ||
+      cudaMallocHost(&h->ledger_host, TDEM_L3_COUNT * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&h->status_host, sizeof(int)) != cudaSuccess) {
+    h->err = "device initialisation failed";
+    return fail_out(TDEM_ERR_CUDA);
+  }
+  *out = h;
+  return TDEM_OK;
+}
+
+void tdem_icedem3d_destroy(tdem_icedem3d* h) { destroy(h); }
+
+int tdem_icedem3d_forces(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads, double time,
+                         int update_fracture, int update_history, double* out_force, void* stream) {
+  if (!h) return TDEM_ERR_BADARG;
+  if (!out_force) return tdem::fail(&h->err, TDEM_ERR_BADARG, "out_force is required");
+  Out o{out_force, 1, update_fracture ? 1 : 0, update_history ? 1 : 0, 1, time};
+  return launch(h, st, loads, o, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int tdem_icedem3d_step(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads, int64_t n_steps,
+                       double time, void* stream) {
+  if (!h) return TDEM_ERR_BADARG;
+  if (n_steps < 1) return tdem::fail(&h->err, TDEM_ERR_BADARG, "n_steps must be >= 1");
+  Out o{nullptr, 0, 1, 1, (long long)n_steps, time};
+  return launch(h, st, loads, o, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int tdem_icedem3d_read_ledger(tdem_icedem3d* h, double* out, int count, void* stream) {
+  if (!h || !out || count < 0 || count > TDEM_L3_COUNT) return TDEM_ERR_BADARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(h->ledger_host, h->dev.ledger, TDEM_L3_COUNT * sizeof(double),
+                                         cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
+  h->ledger_host[TDEM_L3_STATUS] = (double)*h->status_host;
+  std::memcpy(out, h->ledger_host, count * sizeof(double));
+  return TDEM_OK;
+}
+
+int tdem_icedem3d_read_contacts(tdem_icedem3d* h, int32_t* pairs, int64_t capacity, int64_t* count, void* stream) {
+  if (!h || !count || capacity < 0 || (capacity > 0 && !pairs)) return TDEM_ERR_BADARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  std::vector<int> cnt(h->n), js((size_t)h->n * kContacts);
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(cnt.data(), h->dev.ci_cnt, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(js.data(), h->dev.ci_j, js.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
+  int64_t m = 0;
+  for (int k = 0; k < h->n; ++k)
+    for (int c = 0; c < cnt[k]; ++c) {
+      if (m < capacity) {
+        pairs[2 * m] = k;
+        pairs[2 * m + 1] = js[(size_t)k * kContacts + c];
+      }
+      ++m;
+    }
+  *count = m;
+  if (m > capacity) return tdem::fail(&h->err, TDEM_ERR_CAPACITY, "contact buffer too small");
+  return TDEM_OK;
+}
+
+int tdem_icedem3d_set_history(tdem_icedem3d* h, const int32_t* pairs, const double* disp, int64_t count,
+                              void* stream) {
+  if (!h || count < 0 || (count > 0 && (!pairs || !disp))) return TDEM_ERR_BADARG;
+  const int n = h->n;
+  std::vector<int> cnt(n, 0), js((size_t)n * kHistory, 0);
+  std::vector<double> ds((size_t)n * kHistory * 3, 0.0);
+  for (int64_t e = 0; e < count; ++e) {
+    const int i = pairs[2 * e], j = pairs[2 * e + 1];
+    if (i < 0 || j <= i || j >= n)
+      return tdem::fail(&h->err, TDEM_ERR_BADARG, "history pair " + std::to_string(e) + " is not 0 <= i < j < n");
+    if (cnt[i] == kHistory)
+      return tdem::fail(&h->err, TDEM_ERR_CAPACITY,
+                        "particle " + std::to_string(i) + " has more than " + std::to_string(kHistory) + " partners");
+    for (int q = 0; q < cnt[i]; ++q)
+      if (js[(size_t)i * kHistory + q] == j)
+        return tdem::fail(&h->err, TDEM_ERR_BADARG, "duplicate history pair");
+    const size_t slot = (size_t)i * kHistory + cnt[i]++;
+    js[slot] = j;
+    for (int c = 0; c < 3; ++c) ds[3 * slot + c] = disp[3 * e + c];
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
+  TDEM_CUDA_TRY(&h->err, cudaMemcpy(h->dev.hist_cnt, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice));
+  TDEM_CUDA_TRY(&h->err, cudaMemcpy(h->dev.hist_j, js.data(), js.size() * sizeof(int), cudaMemcpyHostToDevice));
+  TDEM_CUDA_TRY(&h->err, cudaMemcpy(h->dev.hist_d, ds.data(), ds.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return TDEM_OK;
+}
+
+int tdem_icedem3d_read_history(tdem_icedem3d* h, int32_t* pairs, double* disp, int64_t capacity, int64_t* count,
+                               void* stream) {
+  if (!h || !count || capacity < 0 || (capacity > 0 && (!pairs || !disp))) return TDEM_ERR_BADARG;
+  const int n = h->n;
+  std::vector<int> cnt(n), js((size_t)n * kHistory);
+  std::vector<double> ds((size_t)n * kHistory * 3);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(cnt.data(), h->dev.hist_cnt, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(js.data(), h->dev.hist_j, js.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(ds.data(), h->dev.hist_d, ds.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
+  int64_t m = 0;
+  for (int i = 0; i < n; ++i)
+    for (int q = 0; q < cnt[i]; ++q) {
+      const size_t slot = (size_t)i * kHistory + q;
+      if (m < capacity) {
+        pairs[2 * m] = i;
+        pairs[2 * m + 1] = js[slot];
+        for (int c = 0; c < 3; ++c) disp[3 * m + c] = ds[3 * slot + c];
+      }
+      ++m;
+    }
+  *count = m;
+  if (m > capacity) return tdem::fail(&h->err, TDEM_ERR_CAPACITY, "history buffer too small");
+  return TDEM_OK;
+}
+
+int tdem_icedem3d_last_error(const tdem_icedem3d* h, char* buf, size_t len) {
+  if (!buf || len == 0) return TDEM_ERR_BADARG;
+  const std::string& e = h ? h->err : g_create_error3;
+  const size_t m = std::min(len - 1, e.size());
+  std::memcpy(buf, e.data(), m);
+  buf[m] = '\0';
+  return TDEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,186 @@
+"""Replay of the golden IceDEM3D runs against any implementation of the 3-D step.
+
+The same replay drives the numpy oracle (CPU tests) and the CUDA path (GPU
+tests) against the reference's own outputs (tests/golden/dem3d_*.npz, made by
+tests/golden/make_golden3d.py), with one set of tolerances:
+
+* bond states at every frame and ``failure_mode`` / ``failure_time_s`` at the
+  end: bit-exact;
+* positions, velocities, the side-effect-free force probe, reactions and the
+  diagnostics scalars at every frame: within ``RTOL`` relative to the largest
+  magnitude of that quantity (normwise);
+* ``failure_extension_m`` / ``failure_energy_J``, ``energy()`` and the bond-law
+  state at the end: within ``RTOL`` normwise.
+"""
+
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+RTOL = 1e-12
+DIAG_KEYS = ("reaction_x", "reaction_y", "reaction_z", "top_platen_reaction_z_N",
+             "bottom_platen_reaction_z_N", "boundary_reaction_x", "boundary_reaction_y",
+             "boundary_reaction_z", "broken_bonds", "kinetic_energy_J", "bond_elastic_energy_J",
+             "particle_contact_energy_J", "tool_contact_energy_J", "platen_contact_energy_J",
+             "released_bond_energy_J", "lateral_platen_energy_J", "mechanical_energy_J",
+             "gravity_force_z_N", "buoyancy_force_z_N", "wet_drag_force_z_N", "net_body_force_z_N",
+             "submerged_volume_m3")
+ENERGY_KEYS = ("kinetic_energy_J", "bond_elastic_energy_J", "particle_contact_energy_J",
+               "tool_contact_energy_J", "platen_contact_energy_J", "released_bond_energy_J",
+               "mechanical_energy_J")
+CASES = ("dem3d_box", "dem3d_hertz_friction", "dem3d_cylinder", "dem3d_loads")
+# Cases whose arithmetic uses no transcendental library function (pow, tanh)
+# replay the whole trajectory to 1e-12 (they come out bit-identical). The
+# Hertz / tanh-cone case does not: torch's CPU pow and tanh are correctly
+# rounded in ~98.5% of calls only, so no other implementation matches them bit
+# for bit, and the fracturing friction contacts amplify those last-bit
+# differences over hundreds of steps. It is held to the one-step replay from
+# the reference's own state at every frame instead.
+FREE_RUN = ("dem3d_box", "dem3d_cylinder", "dem3d_loads")
+
+
+def load(name: str) -> dict:
+    with np.load(GOLDEN / f"{name}.npz", allow_pickle=False) as z:
+        return {k: z[k] for k in z.files}
+
+
+def config_dict(g: dict) -> dict:
+    cfg = json.loads(str(g["config"]))
+    for k in ("bond_delayed_elastic_fraction", "bond_relaxation_time_s"):
+        cfg[k] = tuple(cfg[k])
+    return cfg
+
+
+def normwise(a, b, floor: float = 0.0) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = max(np.abs(b).max(initial=0.0), floor)
+    if scale == 0.0:
+        return float(np.abs(a - b).max(initial=0.0))
+    return float(np.abs(a - b).max(initial=0.0) / scale)
+
+
+def _diag_scale(g: dict, k: int, c: int) -> float:
+    """Scale of one diagnostics scalar: energies against the largest energy of
+    the frame, forces against the largest force magnitude of the frame."""
+    row = g["frame_diag"][k]
+    name = DIAG_KEYS[c]
+    if name.endswith("_m3"):
+        return max(abs(row[c]), 1e-300)
+    if name.endswith("_J"):
+        idx = [i for i, n in enumerate(DIAG_KEYS) if n.endswith("_J")]
+        return max(np.abs(row[idx]).max(), 1e-300)
+    return max(np.abs(g["frame_force"][k]).max(), np.abs(row[:8]).max(), 1e-300)
+
+
+def replay(g: dict, sim, *, to_np, rtol: float = RTOL) -> dict:
+    """Drive ``sim`` through the golden protocol; assert and return the worst errors."""
+    frames = [int(s) for s in g["frame_step"]]
+    loads = g.get("loads")
+    worst = {"pos": 0.0, "vel": 0.0, "force": 0.0, "reaction": 0.0, "diag": 0.0}
+    s = 0
+    for k, target in enumerate(frames):
+        if loads is not None:
+            while s < target:
+                sim.step(loads[s])
+                s += 1
+        elif target > s:
+            sim.run(target - s)
+            s = target
+        f, r = sim.forces(update_fracture=False, update_history=False)
+        errs = {
+            "pos": normwise(to_np(sim.positions), g["frame_pos"][k]),
+            "vel": normwise(to_np(sim.velocities), g["frame_vel"][k]),
+            "force": normwise(to_np(f), g["frame_force"][k]),
+            "reaction": normwise(to_np(r), g["frame_reaction"][k], floor=np.abs(g["frame_force"][k]).max()),
+        }
+        diag = sim.diagnostics()
+        got = np.asarray([float(diag[n]) for n in DIAG_KEYS])
+        derr = [abs(got[c] - g["frame_diag"][k][c]) / _diag_scale(g, k, c) for c in range(len(DIAG_KEYS))]
+        errs["diag"] = max(derr)
+        assert errs["diag"] <= rtol, f"step {target}: {DIAG_KEYS[int(np.argmax(derr))]} error {errs['diag']:.3e}"
+        lat = np.asarray(diag["lateral_platen_reaction"], dtype=np.float64)
+        errs["diag"] = max(errs["diag"], normwise(lat, g["frame_lateral"][k],
+                                                  floor=np.abs(g["frame_force"][k]).max()))
+        for name, e in errs.items():
+            worst[name] = max(worst[name], e)
+            assert e <= rtol, f"step {target}: {name} error {e:.3e} > {rtol:.0e}"
+        alive = np.asarray(to_np(sim.alive), dtype=bool)
+        assert np.array_equal(alive, g["frame_alive"][k]), f"step {target}: bond states differ"
+        assert sim.time == float(g["frame_time"][k])
+    assert np.array_equal(to_np(sim.failure_mode), g["failure_mode"])
+    assert np.array_equal(to_np(sim.failure_time_s), g["failure_time_s"])
+    for name in ("failure_extension_m", "failure_energy_J"):
+        e = normwise(to_np(getattr(sim, name)), g[name])
+        assert e <= rtol, f"{name} error {e:.3e}"
+    en = sim.energy()
+    e = normwise([en[n] for n in ENERGY_KEYS], g["energy"])
+    assert e <= rtol, f"energy() error {e:.3e}"
+    if g["branch_offsets"].size:
+        e = normwise(to_np(sim.branch_offsets), g["branch_offsets"])
+        assert e <= rtol, f"branch offsets error {e:.3e}"
+    e = normwise(to_np(sim.bond_damage), g["bond_damage"])
+    assert e <= rtol, f"bond damage error {e:.3e}"
+    assert abs(sim.cumulative_bond_dissipation_J - float(g["bond_dissipation"])) <= \
+        rtol * max(abs(float(g["bond_dissipation"])), 1e-300)
+    return worst
+
+
+def set_frame_state(g: dict, k: int, sim, *, to_device) -> None:
+    """Load the reference's full state at frame ``k`` into ``sim``: positions,
+    velocities, bond states, the failure ledger up to that time, the Maxwell
+    branches, the platen springs, the lateral platens and the pair friction
+    history."""
+    t_k = float(g["frame_time"][k])
+    sim.positions = to_device(g["frame_pos"][k])
+    sim.velocities = to_device(g["frame_vel"][k])
+    sim.alive = to_device(g["frame_alive"][k])
+    before = (g["failure_time_s"] >= 0) & (g["failure_time_s"] < t_k)
+    sim.failure_mode = to_device(np.where(before, g["failure_mode"], 0).astype(np.uint8))
+    sim.failure_time_s = to_device(np.where(before, g["failure_time_s"], -1.0))
+    sim.failure_extension_m = to_device(np.where(before, g["failure_extension_m"], 0.0))
+    sim.failure_energy_J = to_device(np.where(before, g["failure_energy_J"], 0.0))
+    sim.branch_offsets = to_device(g["teach_offsets"][k])
+    sim._bond_elongation_prev = to_device(g["teach_elong_prev"][k])
+    sim.bond_damage = to_device(g["teach_damage"][k])
+    sim._top_platen_tang_disp = to_device(g["teach_top_tang"][k])
+    sim._bottom_platen_tang_disp = to_device(g["teach_bottom_tang"][k])
+    sim.lateral_platen_pos = to_device(g["teach_lateral_pos"][k])
+    sim.cumulative_bond_dissipation_J = float(g["teach_dissipation"][k])
+    lo = int(np.sum(g["teach_hist_count"][:k]))
+    hi = lo + int(g["teach_hist_count"][k])
+    sim.set_friction_history({(int(a), int(b)): tuple(d) for (a, b), d in
+                              zip(g["teach_hist_pairs"][lo:hi], g["teach_hist_disp"][lo:hi])})
+    sim.time = t_k
+    sim.step_count = int(g["frame_step"][k])
+
+
+def replay_one_step(g: dict, sim, *, to_np, to_device, rtol: float = RTOL) -> dict:
+    """From the reference's state at every frame: the force probe, then one
+    step (positions, velocities, bond states and the breaks of that step)."""
+    worst = {"force": 0.0, "pos": 0.0, "vel": 0.0}
+    loads = g.get("loads")
+    frames = [int(s) for s in g["frame_step"]]
+    for k, s in enumerate(frames[:-1]):
+        set_frame_state(g, k, sim, to_device=to_device)
+        f, _ = sim.forces(update_fracture=False, update_history=False)
+        e = normwise(to_np(f), g["frame_force"][k])
+        worst["force"] = max(worst["force"], e)
+        assert e <= rtol, f"step {s}: force probe error {e:.3e}"
+        sim.step(None if loads is None else loads[s])
+        for name, want in (("pos", g["teach_next_pos"][k]), ("vel", g["teach_next_vel"][k])):
+            e = normwise(to_np(getattr(sim, "positions" if name == "pos" else "velocities")), want)
+            worst[name] = max(worst[name], e)
+            assert e <= rtol, f"step {s} -> {s + 1}: {name} error {e:.3e}"
+        assert np.array_equal(np.asarray(to_np(sim.alive), dtype=bool), g["teach_next_alive"][k]), \
+            f"step {s} -> {s + 1}: bond states differ"
+        now = g["failure_time_s"] == float(g["frame_time"][k])
+        assert np.array_equal(to_np(sim.failure_mode)[now], g["failure_mode"][now])
+        for name in ("failure_extension_m", "failure_energy_J"):
+            e = normwise(to_np(getattr(sim, name))[now], g[name][now])
+            assert e <= rtol, f"step {s}: {name} error {e:.3e}"
+    return worst
