@@ -4,6 +4,11 @@
   (src/tensordem/cli.py:42-110, 254-285), same flags and the same outputs
   (history.csv, trajectory.pt, accounting.json), stepped by the FP64 CUDA
   reference-mode kernel.
+* ``dem-3d`` - the reference's 3-D bonded-sphere indentation
+  (src/tensordem/dem3d_cli.py:12-150), same flags and outputs (history.csv,
+  checkpoint_3d.pt, trajectory_3d.pt, restart from a checkpoint), stepped by
+  the FP64 CUDA 3-D reference-mode kernel.
+* ``bench-3d`` - step rate of the 3-D reference mode on indentation specimens.
 * ``hm2d`` - the Hertz-Mindlin disc settling case on the GB300 engine: run,
   time and report (used for profiling runs as well).
 * ``ensemble`` - a seeded mixed ensemble of independent runs in the batched
@@ -208,6 +213,104 @@ def _cmd_serve(args: argparse.Namespace) -> None:
         Path(args.output).write_text(json.dumps(out, indent=1))
 
 
+def _cmd_dem_3d(args: argparse.Namespace) -> None:
+    from .dem3d import DEM3DConfig, IceDEM3D
+
+    if args.steps < 1 or args.save_every < 1:
+        sys.exit("--steps and --save-every must be positive")
+    if args.stability_report:
+        sys.exit("--stability-report (src/tensordem/stability.py) is not built in tensordem_gb300")
+    try:
+        if args.restart is not None:
+            if not args.restart.is_file():
+                sys.exit(f"restart checkpoint not found: {args.restart}")
+            checkpoint = torch.load(args.restart, map_location="cpu", weights_only=False)
+            if not isinstance(checkpoint, dict) or "state" not in checkpoint:
+                sys.exit("restart file must be a TensorDEM 3-D checkpoint with a 'state' entry")
+            saved = checkpoint["state"].get("config")
+            if not isinstance(saved, dict):
+                sys.exit("restart checkpoint has no valid saved configuration")
+            saved = {k: tuple(v) if isinstance(v, list) else v for k, v in saved.items()}
+            sim = IceDEM3D(DEM3DConfig(**{**saved, "device": args.device}))
+            sim.load_state_dict(checkpoint["state"])
+        else:
+            sim = IceDEM3D(DEM3DConfig(
+                nx=args.nx, ny=args.ny, nz=args.nz, dt=args.dt, tool_speed=args.speed, radius=args.radius,
+                tool_radius=args.tool_radius, breaking_strain=args.breaking_strain,
+                shear_breaking_strain=args.shear_breaking_strain, device=args.device, geometry=args.geometry,
+                fix_bottom=args.fix_bottom, top_platen_enabled=args.top_platen,
+                bottom_platen_enabled=args.bottom_platen, platen_stiffness=args.platen_stiffness,
+                platen_damping=args.platen_damping, top_platen_gap=args.top_platen_gap,
+                bottom_platen_gap=args.bottom_platen_gap, top_platen_velocity=args.top_platen_velocity,
+                bottom_platen_velocity=args.bottom_platen_velocity))
+    except (ValueError, RuntimeError, TypeError, OSError, KeyError, NotImplementedError) as exc:
+        sys.exit(str(exc))
+    args.output.mkdir(parents=True, exist_ok=True)
+    frames, velocities, alive_frames, times, tool_positions = [], [], [], [], []
+    history = args.output / "history.csv"
+    append = args.restart is not None and history.exists()
+    with history.open("a" if append else "w", newline="", encoding="utf-8") as stream:
+        writer = None
+        step = 0
+        while step <= args.steps:
+            if (step % args.save_every == 0 or step == args.steps) and not (append and step == 0):
+                row = sim.diagnostics()
+                row.setdefault("time_s", row["time"])
+                if writer is None:
+                    writer = csv.DictWriter(stream, fieldnames=list(row))
+                    if not append:
+                        writer.writeheader()
+                writer.writerow(row)
+                frames.append(sim.positions.cpu().clone())
+                velocities.append(sim.velocities.cpu().clone())
+                alive_frames.append(sim.alive[sim.bonded].cpu().clone())
+                times.append(sim.time)
+                tool_positions.append(sim.tool_position.cpu().clone())
+                torch.save({"format": "tensordem-dem3d-checkpoint-v1",
+                            "state": {k: (v.cpu() if isinstance(v, torch.Tensor) else v)
+                                      for k, v in sim.state_dict().items()}},
+                           args.output / "checkpoint_3d.pt")
+            if step == args.steps:
+                break
+            nxt = min(args.steps, (step // args.save_every + 1) * args.save_every)
+            sim.run(nxt - step)  # one kernel launch to the next sample point
+            step = nxt
+    torch.save({
+        "dimension": 3, "config": asdict(sim.config), "dt": sim.dt,
+        "times": torch.tensor(times, dtype=torch.float64),
+        "positions": torch.stack(frames), "velocities": torch.stack(velocities),
+        "bond_pairs": sim.pairs[sim.bonded].cpu(), "bond_alive": torch.stack(alive_frames),
+        "fixed": sim.fixed.cpu(), "tool_positions": torch.stack(tool_positions),
+        "failure_mode": sim.failure_mode.cpu(), "failure_time_s": sim.failure_time_s.cpu(),
+        "failure_extension_m": sim.failure_extension_m.cpu(), "failure_energy_J": sim.failure_energy_J.cpu(),
+    }, args.output / "trajectory_3d.pt")
+    print(f"3-D done: t={sim.time:.6g} s, dt={sim.dt:.4g} s, particles={len(sim.positions)}, "
+          f"broken={sim.broken_bonds}, output={args.output}")
+
+
+def _cmd_bench_3d(args: argparse.Namespace) -> None:
+    """Steps per second of the 3-D reference mode on indentation specimens."""
+    from .dem3d import DEM3DConfig, IceDEM3D
+
+    rows = []
+    for size in args.sizes:
+        nx, ny, nz = (int(v) for v in size.split("x"))
+        sim = IceDEM3D(DEM3DConfig(nx=nx, ny=ny, nz=nz, breaking_strain=0.004, shear_breaking_strain=0.008,
+                                   friction_coefficient=args.friction, restitution_coefficient=0.7))
+        sim.run(args.warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.run(args.steps)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        n = len(sim.positions)
+        rows.append({"specimen": size, "particles": n, "bonds": len(sim.pairs), "steps": args.steps,
+                     "us_per_step": 1e6 * dt / args.steps, "particle_steps_per_s": n * args.steps / dt,
+                     "broken": sim.broken_bonds,
+                     "contacts": int(sim.read_ledger()[12])})
+        print(json.dumps(rows[-1]), flush=True)
+
+
 def main(argv: list[str] | None = None) -> None:
     parser = argparse.ArgumentParser(description="tensordem_gb300: GB300 2-D DEM step")
     sub = parser.add_subparsers(dest="command")
@@ -228,6 +331,39 @@ def main(argv: list[str] | None = None) -> None:
     d.add_argument("--output", type=Path, default=Path("results"))
     d.add_argument("--save-every", type=int, default=20)
     d.set_defaults(func=_cmd_dem_2d)
+    d3 = sub.add_parser("dem-3d", help="3-D bonded-sphere indentation (reference mode, FP64)")
+    d3.add_argument("--nx", type=int, default=9)
+    d3.add_argument("--ny", type=int, default=5)
+    d3.add_argument("--nz", type=int, default=3)
+    d3.add_argument("--steps", type=int, default=1000)
+    d3.add_argument("--dt", type=float, default=None)
+    d3.add_argument("--speed", type=float, default=0.5)
+    d3.add_argument("--radius", type=float, default=0.025)
+    d3.add_argument("--tool-radius", type=float, default=0.1)
+    d3.add_argument("--breaking-strain", type=float, default=0.015)
+    d3.add_argument("--shear-breaking-strain", type=float, default=0.03)
+    d3.add_argument("--device", default="cuda")
+    d3.add_argument("--geometry", choices=("box", "cylinder_xz"), default="box")
+    d3.add_argument("--save-every", type=int, default=20)
+    d3.add_argument("--output", type=Path, default=Path("results-3d"))
+    d3.add_argument("--restart", type=Path, default=None)
+    d3.add_argument("--fix-bottom", action="store_true")
+    d3.add_argument("--top-platen", action="store_true")
+    d3.add_argument("--bottom-platen", action="store_true")
+    d3.add_argument("--platen-stiffness", type=float, default=5000.0)
+    d3.add_argument("--platen-damping", type=float, default=0.0)
+    d3.add_argument("--top-platen-gap", type=float, default=0.0)
+    d3.add_argument("--bottom-platen-gap", type=float, default=0.0)
+    d3.add_argument("--top-platen-velocity", type=float, default=0.0)
+    d3.add_argument("--bottom-platen-velocity", type=float, default=0.0)
+    d3.add_argument("--stability-report", action="store_true")
+    d3.set_defaults(func=_cmd_dem_3d)
+    b3 = sub.add_parser("bench-3d", help="3-D reference-mode step rate on indentation specimens")
+    b3.add_argument("--sizes", nargs="+", default=["9x5x3", "20x10x6", "40x20x10", "60x30x15"])
+    b3.add_argument("--steps", type=int, default=2000)
+    b3.add_argument("--warmup", type=int, default=200)
+    b3.add_argument("--friction", type=float, default=0.3)
+    b3.set_defaults(func=_cmd_bench_3d)
     h = sub.add_parser("hm2d", help="Hertz-Mindlin disc settling case on the GPU engine")
     h.add_argument("--case", choices=("gas", "ice"), default="gas",
                    help="gas: n-side^2 disc settling case; ice: (2 n-side) x (n-side / 2) bonded hex sheet")

@@ -1,24 +1,29 @@
 // 3-D reference mode: the FP64 bonded-sphere step of the reference's IceDEM3D
 // (src/tensordem/dem3d.py:564-1663), on sm_103a.
 //
-// Design. One CTA owns one instance and runs many steps per launch; phases of
-// a step are separated by block barriers and every scratch array lives in the
-// handle (L1/L2 resident at reference-mode sizes). A step is:
-//   1. objective shear strain per particle (dem3d.py:875-901),
-//   2. bond force, break test and commit, Maxwell branches, creep clock, one
-//      thread per bond (dem3d.py:984-1100, 1342-1360),
-//   3. cell hash of the positions: cell = floor(x / 2r) keyed into an open-
-//      addressing table, members of each cell in ascending particle order
-//      (dem3d.py:825-856 builds the same cells in a Python dict),
-//   4. contacts: each particle evaluates its pairs with higher ids over the 27
+// Design. One cooperative launch runs many steps of one instance on all SMs
+// (FP64 throughput per SM is small on this part, so the work is spread as
+// wide as it goes). Phases of a step are separated by a grid barrier with a
+// bounded wait; every scratch array lives in the handle. A step is:
+//   A. objective shear strain per particle (dem3d.py:875-901), and the cell
+//      hash of the positions: cell = floor(x / 2r) keyed into an open-
+//      addressing table (dem3d.py:825-856 builds the same cells in a dict);
+//   B. bond force, break test and commit, Maxwell branches, creep clock, one
+//      thread per bond (dem3d.py:984-1100, 1342-1360); cell ranges taken
+//      from an atomic cursor;
+//   C. members scattered into their cells; D. each cell's members sorted
+//      ascending (so the placement order of C does not matter);
+//   E. contacts: each particle evaluates its pairs with higher ids over the 27
 //      neighbour cells, in the reference's pair-list order, and lists its
-//      pairs with lower ids in that order too (dem3d.py:1374-1514),
-//   5. assembly and semi-implicit Euler: each particle sums its force in the
+//      pairs with lower ids in that order too (dem3d.py:1374-1514);
+//   F. assembly and semi-implicit Euler: each particle sums its force in the
 //      order of the reference's index_add_ calls (bond i-side then j-side,
 //      then per contact term the i-side then the j-side), then tool, platens
-//      and integration (dem3d.py:1516-1663).
-// Pair forces that the reference adds as exact zeros are skipped. Block
-// reductions run in a fixed order, so reruns are bitwise identical.
+//      and integration (dem3d.py:1516-1663); the cell table is cleared.
+// Pair forces that the reference adds as exact zeros are skipped. Every value
+// a particle or bond gets is computed by one thread, independent of the grid,
+// so trajectories are bitwise reproducible; ledger sums combine per-block
+// partials in block order.
 //
 // This translation unit is compiled with --fmad=false: the reference runs
 // one torch op per arithmetic step, each rounded separately.
@@ -36,8 +41,10 @@
 namespace tdem {
 namespace icedem3d {
 
-constexpr int kMaxParticles = 65536;
-constexpr int kThreads = 512;
+constexpr int kMaxParticles = 1 << 20;
+constexpr int kBlock = 128;               // threads per block
+constexpr int kItemsPerBlock = 32;        // grid sizing: at most this many items per block
+constexpr unsigned long long kBarrierSpins = 1ull << 24;  // ~1 s of 64 ns naps
 constexpr int kContacts = 32;  // overlapping partners of one particle, per side
 constexpr int kHistory = 64;   // friction-history entries of one particle (as the pair's lower id)
 constexpr long long kCoordHalf = 1ll << 20;  // |cell coordinate| bound of the 21-bit packing
@@ -48,8 +55,8 @@ constexpr int kStatusNonfinite = 1;
 constexpr int kStatusContacts = 2;
 constexpr int kStatusHistory = 4;
 constexpr int kStatusEscaped = 8;
-
-static_assert(16 * (kThreads / 32) * 2 >= kThreads, "the count scan borrows the reduction scratch as ints");
+constexpr int kStatusBarrier = 16;
+constexpr int kPartials = 16;  // per-block ledger partial sums
 
 struct Dev {
   // topology (constant)
@@ -88,7 +95,52 @@ struct Dev {
   double* ledger; // TDEM_L3_COUNT
   int* status;
   unsigned hmask;
+  // grid coordination
+  unsigned* bar_count;
+  unsigned* bar_gen;
+  int* cursor;     // cell-range allocation cursor
+  int* gflags;     // [2] status bits of the step, by step parity
+  double* part;    // [grid, kPartials] per-block ledger partials
+  double* pmin;    // [grid, 2] per-block min break margin, max history size
+  double* pdiss;   // [grid] per-block dashpot dissipation of the launch
 };
+
+// Grid-wide barrier of a cooperative launch. The wait is bounded: when it
+// runs out the block records kStatusBarrier and the caller returns.
+__device__ __noinline__ bool grid_sync(const Dev& D) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* gen = D.bar_gen;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(D.bar_count, 1u) == gridDim.x - 1) {
+      atomicExch(D.bar_count, 0u);
+      __threadfence();
+      atomicAdd(D.bar_gen, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kBarrierSpins) {
+          ok = 0;
+          atomicOr(D.status, kStatusBarrier);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+#define TDEM_GRID_SYNC() \
+  do {                    \
+    if (!grid_sync(D)) return; \
+  } while (0)
 
 // torch.linalg.vector_norm of a 3-vector on the CPU: one fused multiply-add
 // per component after the first square, then the square root.
@@ -160,12 +212,12 @@ struct Out {
   double time;
 };
 
-__global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config P, Dev D, tdem_icedem3d_state S,
-                                                             const double* __restrict__ loads, Out O) {
-  __shared__ double red[16 * (kThreads / 32)];
-  __shared__ int s_flags;
+__global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_config P, Dev D, tdem_icedem3d_state S,
+                                                           const double* __restrict__ loads, Out O) {
+  __shared__ double red[kPartials * (kBlock / 32)];
   const int n = P.n, nb = P.nbond;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int M = P.n_branches;
   const double two_r = 2.0 * P.radius;
   const double width = 2.0 * P.radius;
@@ -177,21 +229,18 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
   double min_margin = 1e300;
   int hist_max = 0;
   long long done = 0;
+  double diss_launch = 0.0;  // this thread's dashpot dissipation over the launch
   const long long total = O.mode == 1 ? 1 : O.n_steps;
+  // the cell table starts cleared (by the host, then by phase F of each step)
 
-  if (tid == 0) s_flags = 0;
   for (long long step = 0; step < total; ++step) {
     const int uf = O.mode == 1 ? O.uf : 1;
     const int uh = O.mode == 1 ? O.uh : 1;
     int flags = 0;
-    // ---- clear the cell table; shear strain (dem3d.py:875-901)
-    for (unsigned s = tid; s <= D.hmask; s += nt) {
-      D.hkey[s] = kEmpty;
-      D.hcnt[s] = 0;
-      D.hfill[s] = 0;
-    }
+    if (gt == 0) *D.cursor = 0;  // its last use was phase B of the previous step
+    // ---- A: shear strain (dem3d.py:875-901)
     if (uf && nb > 0) {
-      for (int k = tid; k < n; k += nt) {
+      for (int k = gt; k < n; k += gs) {
         double c[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) c[q] = 0.0;
@@ -240,11 +289,40 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
         D.shear[k] = shear;
       }
     }
-    __syncthreads();
+    // ---- A: cell hash (dem3d.py:825-856)
+    for (int k = gt; k < n; k += gs) {
+      const double fx = floor(pos[3 * k] / width);
+      const double fy = floor(pos[3 * k + 1] / width);
+      const double fz = floor(pos[3 * k + 2] / width);
+      const double lim = (double)kCoordHalf - 2.0;
+      int slot = -1;
+      if (fabs(fx) < lim && fabs(fy) < lim && fabs(fz) < lim) {
+        const unsigned long long key = pack_cell((long long)fx, (long long)fy, (long long)fz);
+        unsigned s = hash_slot(key, D.hmask);
+        for (unsigned probe = 0; probe <= D.hmask; ++probe) {
+          const unsigned long long prev = atomicCAS(&D.hkey[s], kEmpty, key);
+          if (prev == kEmpty || prev == key) {
+            slot = (int)s;
+            break;
+          }
+          s = (s + 1) & D.hmask;
+        }
+        if (slot >= 0) {  // always: the table has at least 2n slots
+          D.pkey[k] = key;
+          atomicAdd(&D.hcnt[slot], 1);
+        }
+      } else {
+        flags |= (fx == fx && fy == fy && fz == fz) ? kStatusEscaped : kStatusNonfinite;
+      }
+      D.pslot[k] = slot;
+    }
+    TDEM_GRID_SYNC();
+    // every block has read the flags of the previous step (before the barrier
+    // above), so the other parity can be cleared for the next step
+    if (gt == 0) D.gflags[(step + 1) & 1] = 0;
 
-    // ---- bonds: force, break commit, Maxwell branches, creep (dem3d.py:1018-1100, 1342-1360)
-    double diss = 0.0;
-    for (int b = tid; b < nb; b += nt) {
+    // ---- B: bonds: force, break commit, Maxwell branches, creep (dem3d.py:1018-1100, 1342-1360)
+    for (int b = gt; b < nb; b += gs) {
       const int i = D.bi[b], j = D.bj[b];
       const double dx = pos[3 * j] - pos[3 * i];
       const double dy = pos[3 * j + 1] - pos[3 * i + 1];
@@ -285,7 +363,7 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
             dis = dis + (P.branch_k[a] / tau) * i2;
             off[a] = alive ? ext - s_new : ext;
           }
-          if (alive) diss += dis;
+          if (alive) diss_launch += dis;
           S.elongation_prev[b] = ext;
         }
         mag = P.bond_k * ext;
@@ -335,77 +413,24 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
       D.abf[3 * b + 1] = alive ? mag * ny : 0.0;
       D.abf[3 * b + 2] = alive ? mag * nz : 0.0;
     }
-    if (M > 0 && uh) {
-      // cumulative dashpot dissipation of the bonds alive before the commit
-      double v[1] = {diss}, tot[1];
-      block_sum_f64<1>(v, red, tot);
-      if (tid == 0 && S.bond_dissipation) S.bond_dissipation[0] = S.bond_dissipation[0] + tot[0];
+    // ---- B: cell ranges from the cursor
+    for (unsigned s = gt; s <= D.hmask; s += gs) {
+      const int c = D.hcnt[s];
+      if (c) D.hstart[s] = atomicAdd(D.cursor, c);
     }
-
-    // ---- cell hash (dem3d.py:825-856)
-    for (int k = tid; k < n; k += nt) {
-      const double fx = floor(pos[3 * k] / width);
-      const double fy = floor(pos[3 * k + 1] / width);
-      const double fz = floor(pos[3 * k + 2] / width);
-      const double lim = (double)kCoordHalf - 2.0;
-      int slot = -1;
-      if (fabs(fx) < lim && fabs(fy) < lim && fabs(fz) < lim) {
-        const unsigned long long key = pack_cell((long long)fx, (long long)fy, (long long)fz);
-        unsigned s = hash_slot(key, D.hmask);
-        for (unsigned probe = 0; probe <= D.hmask; ++probe) {
-          const unsigned long long prev = atomicCAS(&D.hkey[s], kEmpty, key);
-          if (prev == kEmpty || prev == key) {
-            slot = (int)s;
-            break;
-          }
-          s = (s + 1) & D.hmask;
-        }
-        if (slot >= 0) {  // always: the table has at least 2n slots
-          D.pkey[k] = key;
-          atomicAdd(&D.hcnt[slot], 1);
-        }
-      } else {
-        flags |= (fx == fx && fy == fy && fz == fz) ? kStatusEscaped : kStatusNonfinite;
-      }
-      D.pslot[k] = slot;
-    }
-    __syncthreads();
-    // exclusive scan of the cell counts (each thread a contiguous chunk)
-    {
-      const unsigned H = D.hmask + 1;
-      const unsigned per = (H + nt - 1) / nt;
-      const unsigned lo = min(H, tid * per), hi = min(H, lo + per);
-      int local = 0;
-      for (unsigned s = lo; s < hi; ++s) local += D.hcnt[s];
-      int* sc = reinterpret_cast<int*>(red);
-      sc[tid] = local;
-      __syncthreads();
-      if (tid == 0) {
-        int run = 0;
-        for (int t = 0; t < nt; ++t) {
-          const int c = sc[t];
-          sc[t] = run;
-          run += c;
-        }
-      }
-      __syncthreads();
-      int run = sc[tid];
-      for (unsigned s = lo; s < hi; ++s) {
-        D.hstart[s] = run;
-        run += D.hcnt[s];
-      }
-    }
-    __syncthreads();
-    for (int k = tid; k < n; k += nt) {
+    TDEM_GRID_SYNC();
+    // ---- C: members into their cells
+    for (int k = gt; k < n; k += gs) {
       const int s = D.pslot[k];
       if (s >= 0) D.members[D.hstart[s] + atomicAdd(&D.hfill[s], 1)] = k;
     }
-    __syncthreads();
-    for (unsigned s = tid; s <= D.hmask; s += nt) {
+    TDEM_GRID_SYNC();
+    // ---- D: each cell's members in ascending particle order
+    for (unsigned s = gt; s <= D.hmask; s += gs) {
       const int c = D.hcnt[s];
       if (c == 0) continue;
       int* m = D.members + D.hstart[s];
-      for (int a = 1; a < c; ++a) {  // members in ascending particle order
+      for (int a = 1; a < c; ++a) {
         const int x = m[a];
         int b = a - 1;
         while (b >= 0 && m[b] > x) {
@@ -416,11 +441,11 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
       }
       D.hmin[s] = m[0];
     }
-    __syncthreads();
+    TDEM_GRID_SYNC();
 
-    // ---- contacts (dem3d.py:1374-1514)
+    // ---- E: contacts (dem3d.py:1374-1514)
     double acc_fp = 0.0, acc_rp = 0.0, acc_en = 0.0, acc_nc = 0.0;
-    for (int k = tid; k < n; k += nt) {
+    for (int k = gt; k < n; k += gs) {
       int nci = 0, ncj = 0;
       if (D.pslot[k] >= 0) {
         const unsigned long long kk = D.pkey[k];
@@ -581,9 +606,9 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
       D.cj_cnt[k] = ncj;
       acc_nc += (double)nci;
     }
-    __syncthreads();
+    TDEM_GRID_SYNC();
 
-    // ---- assembly and semi-implicit Euler (dem3d.py:1326-1340, 1516-1663)
+    // ---- F: assembly and semi-implicit Euler (dem3d.py:1326-1340, 1516-1663)
     double acc[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q] = 0.0;
@@ -598,7 +623,7 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
       lvx = S.lateral_velocity[0];
       lvy = S.lateral_velocity[2];
     }
-    for (int k = tid; k < n; k += nt) {
+    for (int k = gt; k < n; k += gs) {
       const double px = pos[3 * k], py = pos[3 * k + 1], pz = pos[3 * k + 2];
       const double vx = vel[3 * k], vy = vel[3 * k + 1], vz = vel[3 * k + 2];
       double fx = (-P.drag) * vx, fy = (-P.drag) * vy, fz = (-P.drag) * vz;
@@ -809,49 +834,78 @@ __global__ void __launch_bounds__(kThreads) icedem3d_kernel(tdem_icedem3d_config
       if (!(isfinite(npx) && isfinite(npy) && isfinite(npz) && isfinite(nvx) && isfinite(nvy) && isfinite(nvz)))
         flags |= kStatusNonfinite;
     }
+    // clear the cell table for the next step (nobody reads it in this phase)
+    for (unsigned s = gt; s <= D.hmask; s += gs) {
+      D.hkey[s] = kEmpty;
+      D.hcnt[s] = 0;
+      D.hfill[s] = 0;
+    }
     acc[9] = acc_fp;
     acc[10] = acc_rp;
     acc[11] = acc_en;
     acc[12] = acc_nc;
-    if (flags) atomicOr(&s_flags, flags);
-    double tot[16];
-    block_sum_f64<16>(acc, red, tot);
+    if (flags) atomicOr(&D.gflags[step & 1], flags);
+    double tot[kPartials];
+    block_sum_f64<kPartials>(acc, red, tot);
     const double mm = block_min_f64(min_margin, red);
     const double hm = -block_min_f64(-(double)hist_max, red);
+    double dv[1] = {diss_launch}, dtot[1];
+    block_sum_f64<1>(dv, red, dtot);
     if (tid == 0) {
-      double* L = D.ledger;
-      L[TDEM_L3_REACTION_X] = -tot[0];
-      L[TDEM_L3_REACTION_Y] = -tot[1];
-      L[TDEM_L3_REACTION_Z] = -tot[2];
-      L[TDEM_L3_TOP_REACTION_Z] = tot[3];
-      L[TDEM_L3_BOTTOM_REACTION_Z] = tot[4];
-      for (int q = 0; q < 4; ++q) L[TDEM_L3_LATERAL_0 + q] = tot[5 + q];
-      if (uh) {
-        L[TDEM_L3_FRICTION_POWER] = tot[9];
-        L[TDEM_L3_ROLLING_POWER] = tot[10];
-      }
-      L[TDEM_L3_CONTACT_ENERGY] = tot[11];
-      L[TDEM_L3_CONTACTS] = tot[12];
-      L[TDEM_L3_HISTORY_MAX] = hm;
-      L[TDEM_L3_MIN_BREAK_MARGIN] = fmin(L[TDEM_L3_MIN_BREAK_MARGIN], mm);
+      for (int q = 0; q < kPartials; ++q) D.part[(size_t)blockIdx.x * kPartials + q] = tot[q];
+      D.pmin[2 * blockIdx.x] = mm;
+      D.pmin[2 * blockIdx.x + 1] = hm;
+      D.pdiss[blockIdx.x] = dtot[0];
     }
-    // every thread takes the same exit decision: the flags were OR-ed in before
-    // the reductions' barriers, and s_flags is never cleared inside the loop
-    const int f = s_flags;
-    if (O.mode == 1) {
-      done = 1;
-      if (tid == 0 && f) *D.status = f;
-      break;
+    TDEM_GRID_SYNC();
+    // every block takes the same exit decision: this parity's flags are final
+    // after the barrier and are cleared only two steps later
+    const int f = *reinterpret_cast<volatile int*>(&D.gflags[step & 1]);
+    const bool last = O.mode == 1 || f != 0 || step + 1 == total;
+    if (O.mode != 1) {
+      if (blockIdx.x == 0 && (P.platens & 4) && tid < 4)
+        S.lateral_position[tid] = lp[tid] + S.lateral_velocity[tid] * P.dt;
+      time = time + P.dt;
     }
-    if ((P.platens & 4) && tid < 4) S.lateral_position[tid] = lp[tid] + S.lateral_velocity[tid] * P.dt;
-    time = time + P.dt;
     done = step + 1;
-    if (f) {
-      if (tid == 0) *D.status = f;
-      break;
+    if (last) {
+      if (blockIdx.x == 0 && tid < kPartials + 3) {
+        // ledger of the last evaluation: per-block partials in block order
+        double* L = D.ledger;
+        const int q = tid;
+        if (q < kPartials) {
+          double s = 0.0;
+          for (unsigned bk = 0; bk < gridDim.x; ++bk) s += D.part[(size_t)bk * kPartials + q];
+          const double neg = -s;
+          if (q < 3) L[TDEM_L3_REACTION_X + q] = neg;
+          else if (q == 3) L[TDEM_L3_TOP_REACTION_Z] = s;
+          else if (q == 4) L[TDEM_L3_BOTTOM_REACTION_Z] = s;
+          else if (q < 9) L[TDEM_L3_LATERAL_0 + q - 5] = s;
+          else if (q == 9 && uh) L[TDEM_L3_FRICTION_POWER] = s;
+          else if (q == 10 && uh) L[TDEM_L3_ROLLING_POWER] = s;
+          else if (q == 11) L[TDEM_L3_CONTACT_ENERGY] = s;
+          else if (q == 12) L[TDEM_L3_CONTACTS] = s;
+        } else if (q == kPartials) {
+          double m = L[TDEM_L3_MIN_BREAK_MARGIN];
+          for (unsigned bk = 0; bk < gridDim.x; ++bk) m = fmin(m, D.pmin[2 * bk]);
+          L[TDEM_L3_MIN_BREAK_MARGIN] = m;
+        } else if (q == kPartials + 1) {
+          double m = 0.0;
+          for (unsigned bk = 0; bk < gridDim.x; ++bk) m = fmax(m, D.pmin[2 * bk + 1]);
+          L[TDEM_L3_HISTORY_MAX] = m;
+        } else if (S.bond_dissipation && M > 0) {
+          double s = 0.0;
+          for (unsigned bk = 0; bk < gridDim.x; ++bk) s += D.pdiss[bk];
+          S.bond_dissipation[0] = S.bond_dissipation[0] + s;
+        }
+      }
+      if (gt == 0) {
+        if (f) atomicOr(D.status, f);
+        D.ledger[TDEM_L3_STEPS_DONE] = (double)done;
+      }
+      return;
     }
   }
-  if (tid == 0) D.ledger[TDEM_L3_STEPS_DONE] = (double)done;
 }
 
 }  // namespace icedem3d
@@ -862,6 +916,7 @@ using namespace tdem::icedem3d;
 struct tdem_icedem3d {
   tdem_icedem3d_config cfg{};
   Dev dev{};
+  int max_grid = 1;  // co-resident blocks of the cooperative launch
   std::vector<void*> allocs;
   double* ledger_host = nullptr;
   int* status_host = nullptr;
@@ -920,9 +975,22 @@ int check_state(tdem_icedem3d* h, const tdem_icedem3d_state* st) {
 int launch(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads, Out o, cudaStream_t s) {
   int rc = check_state(h, st);
   if (rc) return rc;
-  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(h->dev.status, 0, sizeof(int), s));
-  icedem3d_kernel<<<1, kThreads, 0, s>>>(h->cfg, h->dev, *st, loads, o);
-  TDEM_CUDA_TRY(&h->err, cudaGetLastError());
+  Dev& D = h->dev;
+  const size_t H = (size_t)D.hmask + 1;
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.status, 0, sizeof(int), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.bar_count, 0, sizeof(unsigned), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.gflags, 0, 2 * sizeof(int), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hkey, 0xff, H * sizeof(unsigned long long), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hcnt, 0, H * sizeof(int), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hfill, 0, H * sizeof(int), s));
+  const long long items = std::max<long long>(h->n, h->nb);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(h->max_grid, (items + kItemsPerBlock - 1) /
+                                                                                  kItemsPerBlock));
+  tdem_icedem3d_config cfg = h->cfg;
+  tdem_icedem3d_state state = *st;
+  void* args[] = {&cfg, &D, &state, const_cast<double**>(&loads), &o};
+  TDEM_CUDA_TRY(&h->err, cudaLaunchCooperativeKernel(reinterpret_cast<void*>(&icedem3d_kernel), dim3(grid),
+                                                     dim3(kBlock), args, 0, s));
   TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(h->status_host, h->dev.status, sizeof(int), cudaMemcpyDeviceToHost, s));
   TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
   const int f = *h->status_host;
@@ -936,6 +1004,8 @@ int launch(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads,
                       "a particle's friction history exceeds " + std::to_string(kHistory) + " partners");
   if (f & kStatusEscaped)
     return tdem::fail(&h->err, TDEM_ERR_CAPACITY, "a particle left the 2^20-cell hash range");
+  if (f & kStatusBarrier)
+    return tdem::fail(&h->err, TDEM_ERR_CUDA, "a grid barrier of the cooperative launch timed out");
   return TDEM_OK;
 }
 
@@ -1040,6 +1110,23 @@ int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_to
       (rc = dalloc(h, &D.hist_cnt, n)) || (rc = dalloc(h, &D.hist_j, (size_t)n * kHistory)) ||
       (rc = dalloc(h, &D.hist_d, (size_t)n * kHistory * 3)) || (rc = dalloc(h, &D.ledger, TDEM_L3_COUNT)) ||
       (rc = dalloc(h, &D.status, 1)))
+    return fail_out(rc);
+  // cooperative grid: every block must be resident at once
+  int dev = 0, sms = 0, coop = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icedem3d_kernel, kBlock, 0) != cudaSuccess) {
+    h->err = "device query failed";
+    return fail_out(TDEM_ERR_CUDA);
+  }
+  if (!coop || per_sm < 1) {
+    h->err = "the device does not support cooperative launches of the 3-D step kernel";
+    return fail_out(TDEM_ERR_CUDA);
+  }
+  h->max_grid = sms * per_sm;
+  if ((rc = dalloc(h, &D.bar_count, 1)) || (rc = dalloc(h, &D.bar_gen, 1)) || (rc = dalloc(h, &D.cursor, 1)) ||
+      (rc = dalloc(h, &D.gflags, 2)) || (rc = dalloc(h, &D.part, (size_t)h->max_grid * kPartials)) ||
+      (rc = dalloc(h, &D.pmin, 2 * (size_t)h->max_grid)) || (rc = dalloc(h, &D.pdiss, (size_t)h->max_grid)))
     return fail_out(rc);
   std::vector<double> led(TDEM_L3_COUNT, 0.0);
   led[TDEM_L3_MIN_BREAK_MARGIN] = 1e300;

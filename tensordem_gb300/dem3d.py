@@ -460,9 +460,13 @@ class IceDEM3D:
             raise ValueError(f"dt exceeds conservative limit {config.recommended_dt:.6g} s")
         host = self._build_topology()
         dev = self.device
-        for name in ("positions", "initial_positions", "fixed", "pairs", "rest_lengths", "bonded",
-                     "reference_bond_vectors", "initial_normals"):
-            setattr(self, name, host[name].to(dev))
+        self.initial_positions = host["initial_positions"].to(dev)
+        self.fixed = host["fixed"].to(dev)
+        self.pairs = host["pairs"].to(dev)
+        self.rest_lengths = host["rest_lengths"].to(dev)
+        self.bonded = host["bonded"].to(dev)
+        self.reference_bond_vectors = host["reference_bond_vectors"].to(dev)
+        self.initial_normals = host["initial_normals"].to(dev)
         self.positions = self.initial_positions.clone()
         self.velocities = torch.zeros_like(self.positions)
         self.alive = self.bonded.clone()

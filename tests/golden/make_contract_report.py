@@ -6,10 +6,11 @@ Run where the reference source tree is available::
 
 It imports ``tensordem.binding_contract`` (src/tensordem/binding_contract.py)
 and runs its ``verify()`` on ``tensordem_gb300.IceDEM`` and
-``tensordem_gb300.CalibratedIceDEM`` against the contract's ``IceDEM`` entry.
+``tensordem_gb300.CalibratedIceDEM`` against the contract's ``IceDEM`` entry,
+and on ``tensordem_gb300.IceDEM3D`` against its ``IceDEM3D`` entry.
 ``verify()`` accepts a class and checks it statically: state attributes,
-properties, method names, parameters, kinds and annotations. The 3-D entry is
-outside this package. Output: tests/golden/binding_contract_report.json.
+properties, method names, parameters, kinds and annotations.
+Output: tests/golden/binding_contract_report.json.
 """
 
 from __future__ import annotations
@@ -26,13 +27,13 @@ def report() -> dict:
     sys.path.insert(0, str(ROOT))
     from tensordem import binding_contract as bc
 
-    from tensordem_gb300 import CalibratedIceDEM, IceDEM
-    contract = dict(bc.BINDING_CONTRACT)
-    contract["entries"] = {"IceDEM": bc.BINDING_CONTRACT["entries"]["IceDEM"]}
-    out = {"contract_version": bc.BINDING_CONTRACT.get("version", contract.get("contract_version")),
+    from tensordem_gb300 import CalibratedIceDEM, IceDEM, IceDEM3D
+    out = {"contract_version": bc.BINDING_CONTRACT.get("version", bc.BINDING_CONTRACT.get("contract_version")),
            "frozen_fingerprint": bc.FROZEN_FINGERPRINT, "classes": {}}
-    for cls in (IceDEM, CalibratedIceDEM):
-        r = bc.verify({"IceDEM": cls}, contract=contract)
+    for cls, entry in ((IceDEM, "IceDEM"), (CalibratedIceDEM, "IceDEM"), (IceDEM3D, "IceDEM3D")):
+        contract = dict(bc.BINDING_CONTRACT)
+        contract["entries"] = {entry: bc.BINDING_CONTRACT["entries"][entry]}
+        r = bc.verify({entry: cls}, contract=contract)
         out["classes"][cls.__name__] = {k: r[k] for k in ("status", "checks", "matched", "breaking", "other")}
         out["classes"][cls.__name__]["findings"] = r["findings"]
     return out

@@ -3,7 +3,7 @@
 The reference's ``binding_contract.verify()`` (src/tensordem/binding_contract.py:414)
 checks a class statically: state attributes, properties, methods, parameter
 names, kinds, defaults and annotations. ``tests/golden/make_contract_report.py``
-runs it on ``IceDEM`` and ``CalibratedIceDEM`` and commits the report; this test
+runs it on ``IceDEM``, ``CalibratedIceDEM`` and ``IceDEM3D`` and commits the report; this test
 checks the committed report, and re-runs ``verify()`` live whenever the
 reference package is importable.
 """
@@ -19,10 +19,10 @@ REPORT = Path(__file__).resolve().parent / "golden" / "binding_contract_report.j
 
 def test_committed_report_conforms():
     rep = json.loads(REPORT.read_text())
-    for name in ("IceDEM", "CalibratedIceDEM"):
+    for name in ("IceDEM", "CalibratedIceDEM", "IceDEM3D"):
         r = rep["classes"][name]
         assert r["status"] == "CONFORMS" and r["breaking"] == 0 and r["other"] == 0, name
-        assert r["checks"] == r["matched"] > 30, name
+        assert r["checks"] == r["matched"] > 20, name
 
 
 @pytest.mark.skipif(importlib.util.find_spec("tensordem") is None

@@ -167,3 +167,22 @@ def test_validation_and_errors(m3):
     with pytest.raises(FloatingPointError):
         sim.step()
     assert sim.step_count == 1
+
+
+def test_cli_restart_workflow(m3, tmp_path):
+    """tests/test_dem3d.py:116-141: history, checkpoint and restart through the CLI."""
+    from tensordem_gb300.cli import main
+    out = tmp_path / "run"
+    main(["dem-3d", "--nx", "3", "--ny", "3", "--nz", "2", "--steps", "2", "--save-every", "1",
+          "--output", str(out)])
+    ck = out / "checkpoint_3d.pt"
+    first = torch.load(ck, map_location="cpu", weights_only=False)
+    assert first["format"] == "tensordem-dem3d-checkpoint-v1" and first["state"]["step_count"] == 2
+    main(["dem-3d", "--steps", "2", "--save-every", "1", "--output", str(out), "--restart", str(ck)])
+    second = torch.load(ck, map_location="cpu", weights_only=False)
+    assert second["state"]["step_count"] == 4
+    assert abs(second["state"]["time"] - 4 * second["state"]["dt"]) <= 1e-15
+    rows = (out / "history.csv").read_text().strip().splitlines()
+    assert len(rows) == 1 + 5  # header, steps 0..2, then 3..4 appended
+    traj = torch.load(out / "trajectory_3d.pt", map_location="cpu", weights_only=False)
+    assert traj["dimension"] == 3 and traj["positions"].shape[1:] == (18, 3)
