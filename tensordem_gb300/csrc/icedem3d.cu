@@ -3,23 +3,27 @@
 //
 // Design. One cooperative launch runs many steps of one instance on all SMs
 // (FP64 throughput per SM is small on this part, so the work is spread as
-// wide as it goes). Phases of a step are separated by a grid barrier with a
-// bounded wait; every scratch array lives in the handle. A step is:
-//   A. objective shear strain per particle (dem3d.py:875-901), and the cell
-//      hash of the positions: cell = floor(x / 2r) keyed into an open-
-//      addressing table (dem3d.py:825-856 builds the same cells in a dict);
+// wide as it goes). Four phases per step, separated by a grid barrier with a
+// bounded wait; every scratch array lives in the handle. Cells are
+// cell = floor(x / 2r) keyed into open-addressing tables (dem3d.py:825-856
+// builds the same cells in a dict); there are two tables, by step parity, so
+// a step's positions are hashed at the end of the step before.
+//   A. cell ranges of this step's table from an atomic cursor; the other
+//      table cleared; objective shear strain per particle (dem3d.py:875-901),
+//      with each particle's bond list fetched in chunks of loads in flight;
 //   B. bond force, break test and commit, Maxwell branches, creep clock, one
-//      thread per bond (dem3d.py:984-1100, 1342-1360); cell ranges taken
-//      from an atomic cursor;
-//   C. members scattered into their cells; D. each cell's members sorted
-//      ascending (so the placement order of C does not matter);
-//   E. contacts: each particle evaluates its pairs with higher ids over the 27
-//      neighbour cells, in the reference's pair-list order, and lists its
-//      pairs with lower ids in that order too (dem3d.py:1374-1514);
-//   F. assembly and semi-implicit Euler: each particle sums its force in the
+//      thread per bond (dem3d.py:984-1100, 1342-1360); members into cells;
+//   C. contacts: each particle evaluates its pairs with higher ids over the 27
+//      neighbour cells (lookups of nine cells in flight together), in the
+//      reference's pair-list order: cells in offset order, members ascending
+//      (dem3d.py:1374-1514). The partner gets the pair in its inbox with the
+//      key of the reference's order for its side (first particle of this
+//      particle's cell, then this particle);
+//   D. assembly and semi-implicit Euler: each particle sums its force in the
 //      order of the reference's index_add_ calls (bond i-side then j-side,
-//      then per contact term the i-side then the j-side), then tool, platens
-//      and integration (dem3d.py:1516-1663); the cell table is cleared.
+//      then per contact term its own pairs then its sorted inbox), then tool,
+//      platens and integration (dem3d.py:1516-1663); the new positions go into
+//      the other table.
 // Pair forces that the reference adds as exact zeros are skipped. Every value
 // a particle or bond gets is computed by one thread, independent of the grid,
 // so trajectories are bitwise reproducible; ledger sums combine per-block
@@ -71,24 +75,23 @@ struct Dev {
   const unsigned char* frank;
   const int* inc_off;    // (n+1)
   const int* inc_split;  // (n) i-side entries of each particle
-  const int* inc_bond;   // (2B)
-  const int* inc_other;  // (2B)
+  const int2* inc;       // (2B) (bond, partner): i side ascending j, then j side ascending i
   // scratch
   double* shear;             // (n)
-  double* abf;               // (B,3) active bond force
-  unsigned long long* pkey;  // (n) packed cell
-  int* pslot;                // (n) hash slot, -1: not hashed
-  unsigned long long* hkey;  // (H)
-  int* hcnt;
-  int* hstart;
-  int* hfill;
-  int* hmin;
-  int* members;   // (n)
+  double* abf;               // (B,3) active bond force (zero for a dead bond)
+  unsigned long long* pkey;  // (n) packed cell of the current step
+  int* pslot;                // (n) its slot in the current table, -1: not hashed
+  unsigned long long* hkey;  // (2, H) two cell tables, by step parity
+  int* hcnt;                 // (2, H)
+  int* hfill;                // (2, H)
+  int* hstart;               // (H) ranges of the current table
+  int* members;              // (n)
   int* ci_cnt;    // (n)
   int* ci_j;      // (n, kContacts)
   double* ci_v;   // (n, kContacts, 9): friction force, rolling force on j, contact force
-  int* cj_cnt;    // (n)
-  int* cj_i;      // (n, kContacts)
+  int* ib_cnt;    // (n) inbox: pairs in which the particle is the higher id
+  unsigned long long* ib_key;  // (n, kContacts) reference order key: first id of the partner's cell, partner
+  int* ib_idx;    // (n, kContacts) the pair's entry in the partner's ci_v
   int* hist_cnt;  // (n)
   int* hist_j;    // (n, kHistory)
   double* hist_d; // (n, kHistory, 3)
@@ -98,7 +101,7 @@ struct Dev {
   // grid coordination
   unsigned* bar_count;
   unsigned* bar_gen;
-  int* cursor;     // cell-range allocation cursor
+  int* cursor;     // [2] cell-range allocation cursors, by table
   int* gflags;     // [2] status bits of the step, by step parity
   double* part;    // [grid, kPartials] per-block ledger partials
   double* pmin;    // [grid, 2] per-block min break margin, max history size
@@ -159,13 +162,13 @@ __device__ __forceinline__ unsigned long long pack_cell(long long cx, long long 
          (unsigned long long)(cz + kCoordHalf);
 }
 
-__device__ __forceinline__ int find_cell(const Dev& D, unsigned long long key) {
-  unsigned s = hash_slot(key, D.hmask);
-  for (unsigned probe = 0; probe <= D.hmask; ++probe) {
-    const unsigned long long k = D.hkey[s];
+__device__ __forceinline__ int find_cell(const unsigned long long* hkey, unsigned mask, unsigned long long key) {
+  unsigned s = hash_slot(key, mask);
+  for (unsigned probe = 0; probe <= mask; ++probe) {
+    const unsigned long long k = hkey[s];
     if (k == key) return (int)s;
     if (k == kEmpty) return -1;
-    s = (s + 1) & D.hmask;
+    s = (s + 1) & mask;
   }
   return -1;
 }
@@ -204,6 +207,35 @@ __device__ __forceinline__ double submerged(const tdem_icedem3d_config& P, doubl
   return f;
 }
 
+// Cell of particle k at position (x, y, z) into table t (dem3d.py:836-840).
+__device__ __forceinline__ void insert_cell(const Dev& D, int t, int k, double x, double y, double z, double width,
+                                            int& flags) {
+  const size_t H = (size_t)D.hmask + 1;
+  const double fx = floor(x / width), fy = floor(y / width), fz = floor(z / width);
+  const double lim = (double)kCoordHalf - 2.0;
+  int slot = -1;
+  if (fabs(fx) < lim && fabs(fy) < lim && fabs(fz) < lim) {
+    const unsigned long long key = pack_cell((long long)fx, (long long)fy, (long long)fz);
+    unsigned long long* hkey = D.hkey + t * H;
+    unsigned s = hash_slot(key, D.hmask);
+    for (unsigned probe = 0; probe <= D.hmask; ++probe) {
+      const unsigned long long prev = atomicCAS(&hkey[s], kEmpty, key);
+      if (prev == kEmpty || prev == key) {
+        slot = (int)s;
+        break;
+      }
+      s = (s + 1) & D.hmask;
+    }
+    if (slot >= 0) {  // always: the table has at least 2n slots
+      D.pkey[k] = key;
+      atomicAdd(&D.hcnt[t * H + slot], 1);
+    }
+  } else {
+    flags |= (fx == fx && fy == fy && fz == fz) ? kStatusEscaped : kStatusNonfinite;
+  }
+  D.pslot[k] = slot;
+}
+
 struct Out {
   double* force;      // (n,3) or null
   int mode;           // 0: steps; 1: one evaluation
@@ -211,6 +243,8 @@ struct Out {
   long long n_steps;
   double time;
 };
+
+constexpr int kChunk = 8;  // incidence entries whose loads are in flight together
 
 __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_config P, Dev D, tdem_icedem3d_state S,
                                                            const double* __restrict__ loads, Out O) {
@@ -223,6 +257,7 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
   const double width = 2.0 * P.radius;
   const bool friction = P.cone != TDEM_CONE_OFF;
   const bool platen_friction = P.platen_cone != TDEM_CONE_OFF;
+  const size_t H = (size_t)D.hmask + 1;
   double* pos = S.positions;
   double* vel = S.velocities;
   double time = O.time;
@@ -231,39 +266,75 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
   long long done = 0;
   double diss_launch = 0.0;  // this thread's dashpot dissipation over the launch
   const long long total = O.mode == 1 ? 1 : O.n_steps;
-  // the cell table starts cleared (by the host, then by phase F of each step)
+
+  // prologue: cells of the starting positions into table 0 (both tables
+  // start cleared by the host)
+  {
+    int flags = 0;
+    for (int k = gt; k < n; k += gs) insert_cell(D, 0, k, pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], width, flags);
+    if (flags) atomicOr(&D.gflags[0], flags);
+  }
+  TDEM_GRID_SYNC();
 
   for (long long step = 0; step < total; ++step) {
     const int uf = O.mode == 1 ? O.uf : 1;
     const int uh = O.mode == 1 ? O.uh : 1;
+    const int p = (int)(step & 1), q = p ^ 1;  // this step's cell table, the next step's
     int flags = 0;
-    if (gt == 0) *D.cursor = 0;  // its last use was phase B of the previous step
-    // ---- A: shear strain (dem3d.py:875-901)
+    // ---- A: cell ranges of table p; table q cleared; shear strain (dem3d.py:875-901)
+    for (unsigned s = gt; s <= D.hmask; s += gs) {
+      const int c = D.hcnt[p * H + s];
+      if (c) D.hstart[s] = atomicAdd(&D.cursor[p], c);
+      D.hkey[q * H + s] = kEmpty;
+      D.hcnt[q * H + s] = 0;
+      D.hfill[q * H + s] = 0;
+    }
+    if (gt == 0) D.cursor[q] = 0;
+    for (int k = gt; k < n; k += gs) D.ib_cnt[k] = 0;
     if (uf && nb > 0) {
       for (int k = gt; k < n; k += gs) {
         double c[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) c[q] = 0.0;
-        for (int e = D.inc_off[k]; e < D.inc_off[k + 1]; ++e) {
-          const int b = D.inc_bond[e];
-          const int i = D.bi[b], j = D.bj[b];
-          const double qx = pos[3 * j] - pos[3 * i];
-          const double qy = pos[3 * j + 1] - pos[3 * i + 1];
-          const double qz = pos[3 * j + 2] - pos[3 * i + 2];
-          const double rx = D.ref[3 * b], ry = D.ref[3 * b + 1], rz = D.ref[3 * b + 2];
-          c[0] += qx * rx; c[1] += qx * ry; c[2] += qx * rz;
-          c[3] += qy * rx; c[4] += qy * ry; c[5] += qy * rz;
-          c[6] += qz * rx; c[7] += qz * ry; c[8] += qz * rz;
+        for (int w = 0; w < 9; ++w) c[w] = 0.0;
+        const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
+        const int e0 = D.inc_off[k], es = e0 + D.inc_split[k], e1 = D.inc_off[k + 1];
+        for (int e = e0; e < e1; e += kChunk) {
+          int2 ent[kChunk];
+          double ox[kChunk], oy[kChunk], oz[kChunk], rx[kChunk], ry[kChunk], rz[kChunk];
+#pragma unroll
+          for (int w = 0; w < kChunk; ++w) ent[w] = e + w < e1 ? D.inc[e + w] : make_int2(0, k);
+#pragma unroll
+          for (int w = 0; w < kChunk; ++w) {
+            const int o = ent[w].y, b = ent[w].x;
+            ox[w] = pos[3 * o];
+            oy[w] = pos[3 * o + 1];
+            oz[w] = pos[3 * o + 2];
+            rx[w] = D.ref[3 * b];
+            ry[w] = D.ref[3 * b + 1];
+            rz[w] = D.ref[3 * b + 2];
+          }
+#pragma unroll
+          for (int w = 0; w < kChunk; ++w) {
+            if (e + w >= e1) break;
+            // q = x[j] - x[i] of the bond; this particle is i on its first es - e0 entries
+            const bool iside = e + w < es;
+            const double qx = iside ? ox[w] - pkx : pkx - ox[w];
+            const double qy = iside ? oy[w] - pky : pky - oy[w];
+            const double qz = iside ? oz[w] - pkz : pkz - oz[w];
+            c[0] += qx * rx[w]; c[1] += qx * ry[w]; c[2] += qx * rz[w];
+            c[3] += qy * rx[w]; c[4] += qy * ry[w]; c[5] += qy * rz[w];
+            c[6] += qz * rx[w]; c[7] += qz * ry[w]; c[8] += qz * rz[w];
+          }
         }
         double shear = 0.0;
         if (D.frank[k]) {
-          const double* p = D.pinv + 9 * (size_t)k;
+          const double* pi = D.pinv + 9 * (size_t)k;
           double f[9];
 #pragma unroll
           for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int b = 0; b < 3; ++b)
-              f[3 * a + b] = (c[3 * a] * p[b] + c[3 * a + 1] * p[3 + b]) + c[3 * a + 2] * p[6 + b];
+              f[3 * a + b] = (c[3 * a] * pi[b] + c[3 * a + 1] * pi[3 + b]) + c[3 * a + 2] * pi[6 + b];
           double e[9];
 #pragma unroll
           for (int a = 0; a < 3; ++a)
@@ -280,41 +351,14 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
           // values: the tail element, then the four lanes of two 4-wide loads
           double sq[9];
 #pragma unroll
-          for (int q = 0; q < 9; ++q) sq[q] = e[q] * e[q];
+          for (int w = 0; w < 9; ++w) sq[w] = e[w] * e[w];
           double s2 = sq[8];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) s2 = s2 + (sq[q] + sq[q + 4]);
+          for (int w = 0; w < 4; ++w) s2 = s2 + (sq[w] + sq[w + 4]);
           shear = sqrt((2.0 / 3.0) * fmax(s2, 0.0));
         }
         D.shear[k] = shear;
       }
-    }
-    // ---- A: cell hash (dem3d.py:825-856)
-    for (int k = gt; k < n; k += gs) {
-      const double fx = floor(pos[3 * k] / width);
-      const double fy = floor(pos[3 * k + 1] / width);
-      const double fz = floor(pos[3 * k + 2] / width);
-      const double lim = (double)kCoordHalf - 2.0;
-      int slot = -1;
-      if (fabs(fx) < lim && fabs(fy) < lim && fabs(fz) < lim) {
-        const unsigned long long key = pack_cell((long long)fx, (long long)fy, (long long)fz);
-        unsigned s = hash_slot(key, D.hmask);
-        for (unsigned probe = 0; probe <= D.hmask; ++probe) {
-          const unsigned long long prev = atomicCAS(&D.hkey[s], kEmpty, key);
-          if (prev == kEmpty || prev == key) {
-            slot = (int)s;
-            break;
-          }
-          s = (s + 1) & D.hmask;
-        }
-        if (slot >= 0) {  // always: the table has at least 2n slots
-          D.pkey[k] = key;
-          atomicAdd(&D.hcnt[slot], 1);
-        }
-      } else {
-        flags |= (fx == fx && fy == fy && fz == fz) ? kStatusEscaped : kStatusNonfinite;
-      }
-      D.pslot[k] = slot;
     }
     TDEM_GRID_SYNC();
     // every block has read the flags of the previous step (before the barrier
@@ -413,41 +457,23 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
       D.abf[3 * b + 1] = alive ? mag * ny : 0.0;
       D.abf[3 * b + 2] = alive ? mag * nz : 0.0;
     }
-    // ---- B: cell ranges from the cursor
-    for (unsigned s = gt; s <= D.hmask; s += gs) {
-      const int c = D.hcnt[s];
-      if (c) D.hstart[s] = atomicAdd(D.cursor, c);
-    }
-    TDEM_GRID_SYNC();
-    // ---- C: members into their cells
+    // ---- B: members into their cells of table p
     for (int k = gt; k < n; k += gs) {
       const int s = D.pslot[k];
-      if (s >= 0) D.members[D.hstart[s] + atomicAdd(&D.hfill[s], 1)] = k;
-    }
-    TDEM_GRID_SYNC();
-    // ---- D: each cell's members in ascending particle order
-    for (unsigned s = gt; s <= D.hmask; s += gs) {
-      const int c = D.hcnt[s];
-      if (c == 0) continue;
-      int* m = D.members + D.hstart[s];
-      for (int a = 1; a < c; ++a) {
-        const int x = m[a];
-        int b = a - 1;
-        while (b >= 0 && m[b] > x) {
-          m[b + 1] = m[b];
-          --b;
-        }
-        m[b + 1] = x;
-      }
-      D.hmin[s] = m[0];
+      if (s >= 0) D.members[D.hstart[s] + atomicAdd(&D.hfill[p * H + s], 1)] = k;
     }
     TDEM_GRID_SYNC();
 
-    // ---- E: contacts (dem3d.py:1374-1514)
+    // ---- C: contacts (dem3d.py:1374-1514). Each particle evaluates its pairs
+    // with higher ids, over the 27 neighbour cells in the reference's order
+    // and each cell's members ascending; the higher id gets the pair in its inbox.
     double acc_fp = 0.0, acc_rp = 0.0, acc_en = 0.0, acc_nc = 0.0;
+    const unsigned long long* hkey_p = D.hkey + p * H;
+    const int* hcnt_p = D.hcnt + p * H;
     for (int k = gt; k < n; k += gs) {
-      int nci = 0, ncj = 0;
-      if (D.pslot[k] >= 0) {
+      int nci = 0;
+      const int sk = D.pslot[k];
+      if (sk >= 0) {
         const unsigned long long kk = D.pkey[k];
         const long long cx = (long long)(kk >> 42) - kCoordHalf;
         const long long cy = (long long)((kk >> 21) & ((1ull << 21) - 1)) - kCoordHalf;
@@ -455,160 +481,175 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
         const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
         const double vkx = vel[3 * k], vky = vel[3 * k + 1], vkz = vel[3 * k + 2];
         const bool fk = S.fixed[k] != 0;
-        unsigned long long cj_key[kContacts];
         int* hj = D.hist_j + (size_t)k * kHistory;
         double* hd = D.hist_d + (size_t)k * kHistory * 3;
         int hc = friction ? D.hist_cnt[k] : 0;
         const int ib0 = D.inc_off[k], ib1 = ib0 + D.inc_split[k];
-        for (int dx = -1; dx <= 1; ++dx)
-          for (int dy = -1; dy <= 1; ++dy)
-            for (int dz = -1; dz <= 1; ++dz) {
-              const int s = find_cell(D, pack_cell(cx + dx, cy + dy, cz + dz));
-              if (s < 0) continue;
-              const int m0 = D.hstart[s], m1 = m0 + D.hcnt[s];
-              for (int m = m0; m < m1; ++m) {
-                const int j = D.members[m];
-                if (j == k) continue;
-                if (j < k) {
-                  // pair (j, k): k is its second particle; same arithmetic as j's side
-                  const double ex = pkx - pos[3 * j], ey = pky - pos[3 * j + 1], ez = pkz - pos[3 * j + 2];
-                  const double ov = fmax(two_r - norm3(ex, ey, ez), 0.0);
-                  if (!(ov > 0.0)) continue;
-                  if (ncj == kContacts) {
-                    flags |= kStatusContacts;
-                    continue;
-                  }
-                  // reference order of this side: by the cell's first particle, then id
-                  const unsigned long long key = ((unsigned long long)D.hmin[s] << 32) | (unsigned)j;
-                  int a = ncj - 1;
-                  while (a >= 0 && cj_key[a] > key) {
-                    cj_key[a + 1] = cj_key[a];
-                    --a;
-                  }
-                  cj_key[a + 1] = key;
-                  ++ncj;
-                  continue;
+        // the first particle of this particle's cell orders the pair in the partner's inbox
+        int own_min = k;
+        {
+          const int m0 = D.hstart[sk], m1 = m0 + hcnt_p[sk];
+          for (int m = m0; m < m1; ++m) own_min = min(own_min, D.members[m]);
+        }
+        const unsigned long long own_key = (unsigned long long)own_min << 32;
+        for (int dx = -1; dx <= 1; ++dx) {
+          // the nine cells of this dx: lookups, then counts and starts, in flight together
+          int sl[9], cnt[9], st[9];
+          unsigned long long ck[9], first[9];
+          unsigned hs[9];
+#pragma unroll
+          for (int o = 0; o < 9; ++o) {
+            ck[o] = pack_cell(cx + dx, cy + o / 3 - 1, cz + o % 3 - 1);
+            hs[o] = hash_slot(ck[o], D.hmask);
+            first[o] = hkey_p[hs[o]];
+          }
+#pragma unroll
+          for (int o = 0; o < 9; ++o)  // a collision probes on (rare)
+            sl[o] = first[o] == ck[o] ? (int)hs[o] : (first[o] == kEmpty ? -1 : find_cell(hkey_p, D.hmask, ck[o]));
+#pragma unroll
+          for (int o = 0; o < 9; ++o) {
+            cnt[o] = sl[o] >= 0 ? hcnt_p[sl[o]] : 0;
+            st[o] = sl[o] >= 0 ? D.hstart[sl[o]] : 0;
+          }
+          for (int o = 0; o < 9; ++o) {
+            // members of the cell ascending: repeated selection (cells hold a few)
+            int last = -1;
+            for (int t = 0; t < cnt[o]; ++t) {
+              int j = INT_MAX;
+              for (int m = st[o]; m < st[o] + cnt[o]; ++m) {
+                const int x = D.members[m];
+                if (x > last && x < j) j = x;
+              }
+              last = j;
+              if (j <= k) continue;
+              const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
+              const double dist = norm3(ex, ey, ez);
+              const double ov = fmax(two_r - dist, 0.0);
+              if (!(ov > 0.0)) continue;
+              if (nci == kContacts) {
+                flags |= kStatusContacts;
+                continue;
+              }
+              bool balive = false;
+              for (int e = ib0; e < ib1; ++e) {
+                const int2 en = D.inc[e];
+                if (en.y == j) {
+                  balive = S.alive[en.x] != 0;
+                  break;
                 }
-                const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
-                const double dist = norm3(ex, ey, ez);
-                const double ov = fmax(two_r - dist, 0.0);
-                if (!(ov > 0.0)) continue;
-                if (nci == kContacts) {
-                  flags |= kStatusContacts;
-                  continue;
-                }
-                bool balive = false;
-                for (int e = ib0; e < ib1; ++e)
-                  if (D.inc_other[e] == j) {
-                    balive = S.alive[D.inc_bond[e]] != 0;
+              }
+              const double dc = fmax(dist, kEps);
+              const double nx = ex / dc, ny = ey / dc, nz = ez / dc;
+              const double vjx = vel[3 * j], vjy = vel[3 * j + 1], vjz = vel[3 * j + 2];
+              const double rvx = vjx - vkx, rvy = vjy - vky, rvz = vjz - vkz;
+              const double vn = (rvx * nx + rvy * ny) + rvz * nz;
+              const bool pinned = P.any_fixed && (fk != (S.fixed[j] != 0));
+              const double k_local = P.hertz ? P.hertz_kn * sqrt(ov) : P.contact_k;
+              double gamma = 0.0;
+              if (P.damping == 2) {
+                gamma = P.damping_c;
+              } else if (P.damping == 1) {
+                gamma = P.hertz ? P.damping_c * sqrt(k_local * (pinned ? P.mass_pinned : P.mass_mobile))
+                              : (pinned ? P.gamma_pinned : P.gamma_mobile);
+              }
+              double mag = fmax(k_local * ov - gamma * vn, 0.0);
+              if (balive) mag = 0.0;
+              else acc_en += P.hertz ? P.hertz_pot * pow(ov, 2.5) : (0.5 * P.contact_k) * (ov * ov);
+              double* out = D.ci_v + ((size_t)k * kContacts + nci) * 9;
+              const double vtx = rvx - vn * nx, vty = rvy - vn * ny, vtz = rvz - vn * nz;
+              if (friction) {
+                // Cundall-Strack spring with the pair's stored displacement
+                int h = -1;
+                for (int q = 0; q < hc; ++q)
+                  if (hj[q] == j) {
+                    h = q;
                     break;
                   }
-                const double dc = fmax(dist, kEps);
-                const double nx = ex / dc, ny = ey / dc, nz = ez / dc;
-                const double vjx = vel[3 * j], vjy = vel[3 * j + 1], vjz = vel[3 * j + 2];
-                const double rvx = vjx - vkx, rvy = vjy - vky, rvz = vjz - vkz;
-                const double vn = (rvx * nx + rvy * ny) + rvz * nz;
-                const bool pinned = P.any_fixed && (fk != (S.fixed[j] != 0));
-                const double k_local = P.hertz ? P.hertz_kn * sqrt(ov) : P.contact_k;
-                double gamma = 0.0;
-                if (P.damping == 2) {
-                  gamma = P.damping_c;
-                } else if (P.damping == 1) {
-                  gamma = P.hertz ? P.damping_c * sqrt(k_local * (pinned ? P.mass_pinned : P.mass_mobile))
-                                  : (pinned ? P.gamma_pinned : P.gamma_mobile);
+                double tx = 0.0, ty = 0.0, tz = 0.0;
+                if (h >= 0) {
+                  tx = hd[3 * h];
+                  ty = hd[3 * h + 1];
+                  tz = hd[3 * h + 2];
                 }
-                double mag = fmax(k_local * ov - gamma * vn, 0.0);
-                if (balive) mag = 0.0;
-                else acc_en += P.hertz ? P.hertz_pot * pow(ov, 2.5) : (0.5 * P.contact_k) * (ov * ov);
-                double* out = D.ci_v + ((size_t)k * kContacts + nci) * 9;
-                const double vtx = rvx - vn * nx, vty = rvy - vn * ny, vtz = rvz - vn * nz;
-                if (friction) {
-                  // Cundall-Strack spring with the pair's stored displacement
-                  int h = -1;
-                  for (int q = 0; q < hc; ++q)
-                    if (hj[q] == j) {
-                      h = q;
-                      break;
-                    }
-                  double tx = 0.0, ty = 0.0, tz = 0.0;
+                if (uh) {
+                  tx = tx + vtx * P.dt;
+                  ty = ty + vty * P.dt;
+                  tz = tz + vtz * P.dt;
+                }
+                const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
+                const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
+                const double fm = norm3(fx, fy, fz);
+                const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
+                const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
+                const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
+                out[0] = Fx;
+                out[1] = Fy;
+                out[2] = Fz;
+                acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
+                if (uh) {
+                  const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
                   if (h >= 0) {
-                    tx = hd[3 * h];
-                    ty = hd[3 * h + 1];
-                    tz = hd[3 * h + 2];
-                  }
-                  if (uh) {
-                    tx = tx + vtx * P.dt;
-                    ty = ty + vty * P.dt;
-                    tz = tz + vtz * P.dt;
-                  }
-                  const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
-                  const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
-                  const double fm = norm3(fx, fy, fz);
-                  const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
-                  const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
-                  const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
-                  out[0] = Fx;
-                  out[1] = Fy;
-                  out[2] = Fz;
-                  acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
-                  if (uh) {
-                    const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
-                    if (h >= 0) {
-                      hd[3 * h] = sx;
-                      hd[3 * h + 1] = sy;
-                      hd[3 * h + 2] = sz;
-                    } else if (sx != 0.0 || sy != 0.0 || sz != 0.0) {
-                      // an absent entry reads as zero, so only non-zero values need a slot
-                      if (hc == kHistory) {
-                        flags |= kStatusHistory;
-                      } else {
-                        hj[hc] = j;
-                        hd[3 * hc] = sx;
-                        hd[3 * hc + 1] = sy;
-                        hd[3 * hc + 2] = sz;
-                        ++hc;
-                      }
+                    hd[3 * h] = sx;
+                    hd[3 * h + 1] = sy;
+                    hd[3 * h + 2] = sz;
+                  } else if (sx != 0.0 || sy != 0.0 || sz != 0.0) {
+                    // an absent entry reads as zero, so only non-zero values need a slot
+                    if (hc == kHistory) {
+                      flags |= kStatusHistory;
+                    } else {
+                      hj[hc] = j;
+                      hd[3 * hc] = sx;
+                      hd[3 * hc + 1] = sy;
+                      hd[3 * hc + 2] = sz;
+                      ++hc;
                     }
                   }
                 }
-                if (P.rolling) {
-                  // rolling-resistance couple (dem3d.py:1242-1299)
-                  const double vtm = norm3(vtx, vty, vtz);
-                  double hx = 0.0, hy = 0.0, hz = 0.0;
-                  if (vtm > 1e-15) {
-                    const double vc = fmax(vtm, kEps);
-                    hx = vtx / vc;
-                    hy = vty / vc;
-                    hz = vtz / vc;
-                  }
-                  const double fm = -(P.roll_mu * mag);
-                  const double jx = fm * hx, jy = fm * hy, jz = fm * hz;
-                  out[3] = jx;
-                  out[4] = jy;
-                  out[5] = jz;
-                  acc_rp += ((-jx) * (vkx - vjx) + (-jy) * (vky - vjy)) + (-jz) * (vkz - vjz);
-                }
-                const double cm = -mag;
-                out[6] = cm * nx;
-                out[7] = cm * ny;
-                out[8] = cm * nz;
-                D.ci_j[(size_t)k * kContacts + nci] = j;
-                ++nci;
               }
+              if (P.rolling) {
+                // rolling-resistance couple (dem3d.py:1242-1299)
+                const double vtm = norm3(vtx, vty, vtz);
+                double hx = 0.0, hy = 0.0, hz = 0.0;
+                if (vtm > 1e-15) {
+                  const double vc = fmax(vtm, kEps);
+                  hx = vtx / vc;
+                  hy = vty / vc;
+                  hz = vtz / vc;
+                }
+                const double fm = -(P.roll_mu * mag);
+                const double jx = fm * hx, jy = fm * hy, jz = fm * hz;
+                out[3] = jx;
+                out[4] = jy;
+                out[5] = jz;
+                acc_rp += ((-jx) * (vkx - vjx) + (-jy) * (vky - vjy)) + (-jz) * (vkz - vjz);
+              }
+              const double cm = -mag;
+              out[6] = cm * nx;
+              out[7] = cm * ny;
+              out[8] = cm * nz;
+              D.ci_j[(size_t)k * kContacts + nci] = j;
+              const int slot = atomicAdd(&D.ib_cnt[j], 1);
+              if (slot < kContacts) {
+                D.ib_key[(size_t)j * kContacts + slot] = own_key | (unsigned)k;
+                D.ib_idx[(size_t)j * kContacts + slot] = k * kContacts + nci;
+              } else {
+                flags |= kStatusContacts;
+              }
+              ++nci;
             }
+          }
+        }
         if (friction) {
           D.hist_cnt[k] = hc;
           hist_max = max(hist_max, hc);
         }
-        for (int a = 0; a < ncj; ++a) D.cj_i[(size_t)k * kContacts + a] = (int)(cj_key[a] & 0xffffffffull);
       }
       D.ci_cnt[k] = nci;
-      D.cj_cnt[k] = ncj;
       acc_nc += (double)nci;
     }
     TDEM_GRID_SYNC();
 
-    // ---- F: assembly and semi-implicit Euler (dem3d.py:1326-1340, 1516-1663)
+    // ---- D: assembly and semi-implicit Euler (dem3d.py:1326-1340, 1516-1663)
     double acc[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q] = 0.0;
@@ -649,41 +690,61 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
         fy = fy + loads[3 * k + 1];
         fz = fz + loads[3 * k + 2];
       }
+      // bonds: i side then j side in bond order, as the two index_add_ calls
+      // add them (a dead bond adds its zero too)
       const int e0 = D.inc_off[k], es = e0 + D.inc_split[k], e1 = D.inc_off[k + 1];
-      for (int e = e0; e < e1; ++e) {
-        const int b = D.inc_bond[e];
-        if (!S.alive[b]) continue;
-        const double* a = D.abf + 3 * (size_t)b;
-        if (e < es) {
-          fx += a[0];
-          fy += a[1];
-          fz += a[2];
-        } else {
-          fx += -a[0];
-          fy += -a[1];
-          fz += -a[2];
+      for (int e = e0; e < e1; e += kChunk) {
+        int2 ent[kChunk];
+        double ax[kChunk], ay[kChunk], az[kChunk];
+#pragma unroll
+        for (int w = 0; w < kChunk; ++w) ent[w] = e + w < e1 ? D.inc[e + w] : make_int2(0, 0);
+#pragma unroll
+        for (int w = 0; w < kChunk; ++w) {
+          const double* a = D.abf + 3 * (size_t)ent[w].x;
+          ax[w] = a[0];
+          ay[w] = a[1];
+          az[w] = a[2];
+        }
+#pragma unroll
+        for (int w = 0; w < kChunk; ++w) {
+          if (e + w >= e1) break;
+          if (e + w < es) {
+            fx += ax[w];
+            fy += ay[w];
+            fz += az[w];
+          } else {
+            fx += -ax[w];
+            fy += -ay[w];
+            fz += -az[w];
+          }
         }
       }
-      const int nci = D.ci_cnt[k], ncj = D.cj_cnt[k];
+      const int nci = D.ci_cnt[k];
       const double* mine = D.ci_v + (size_t)k * kContacts * 9;
-      // value slot `o` of the pair (i, k) in i's contact list
-      auto theirs = [&](int c) -> const double* {
-        const int i = D.cj_i[(size_t)k * kContacts + c];
-        const int cnt = D.ci_cnt[i];
-        const int* js = D.ci_j + (size_t)i * kContacts;
-        for (int q = 0; q < cnt; ++q)
-          if (js[q] == k) return D.ci_v + ((size_t)i * kContacts + q) * 9;
-        return nullptr;
-      };
+      // inbox in the reference's order of the pairs in which this particle is second
+      const int nib = min(D.ib_cnt[k], kContacts);
+      unsigned long long ik[kContacts];
+      int ix[kContacts];
+      for (int a = 0; a < nib; ++a) {
+        const unsigned long long key = D.ib_key[(size_t)k * kContacts + a];
+        const int idx = D.ib_idx[(size_t)k * kContacts + a];
+        int b = a - 1;
+        while (b >= 0 && ik[b] > key) {
+          ik[b + 1] = ik[b];
+          ix[b + 1] = ix[b];
+          --b;
+        }
+        ik[b + 1] = key;
+        ix[b + 1] = idx;
+      }
       if (friction) {
         for (int c = 0; c < nci; ++c) {
           fx += mine[9 * c];
           fy += mine[9 * c + 1];
           fz += mine[9 * c + 2];
         }
-        for (int c = 0; c < ncj; ++c) {
-          const double* t = theirs(c);
-          if (!t) continue;
+        for (int c = 0; c < nib; ++c) {
+          const double* t = D.ci_v + (size_t)ix[c] * 9;
           fx += -t[0];
           fy += -t[1];
           fz += -t[2];
@@ -695,9 +756,8 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
           fy += -mine[9 * c + 4];
           fz += -mine[9 * c + 5];
         }
-        for (int c = 0; c < ncj; ++c) {
-          const double* t = theirs(c);
-          if (!t) continue;
+        for (int c = 0; c < nib; ++c) {
+          const double* t = D.ci_v + (size_t)ix[c] * 9;
           fx += t[3];
           fy += t[4];
           fz += t[5];
@@ -708,9 +768,8 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
         fy += mine[9 * c + 7];
         fz += mine[9 * c + 8];
       }
-      for (int c = 0; c < ncj; ++c) {
-        const double* t = theirs(c);
-        if (!t) continue;
+      for (int c = 0; c < nib; ++c) {
+        const double* t = D.ci_v + (size_t)ix[c] * 9;
         fx += -t[6];
         fy += -t[7];
         fz += -t[8];
@@ -833,12 +892,7 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
       pos[3 * k + 2] = npz;
       if (!(isfinite(npx) && isfinite(npy) && isfinite(npz) && isfinite(nvx) && isfinite(nvy) && isfinite(nvz)))
         flags |= kStatusNonfinite;
-    }
-    // clear the cell table for the next step (nobody reads it in this phase)
-    for (unsigned s = gt; s <= D.hmask; s += gs) {
-      D.hkey[s] = kEmpty;
-      D.hcnt[s] = 0;
-      D.hfill[s] = 0;
+      insert_cell(D, q, k, npx, npy, npz, width, flags);  // the next step's cell table
     }
     acc[9] = acc_fp;
     acc[10] = acc_rp;
@@ -980,9 +1034,10 @@ int launch(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads,
   TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.status, 0, sizeof(int), s));
   TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.bar_count, 0, sizeof(unsigned), s));
   TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.gflags, 0, 2 * sizeof(int), s));
-  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hkey, 0xff, H * sizeof(unsigned long long), s));
-  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hcnt, 0, H * sizeof(int), s));
-  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hfill, 0, H * sizeof(int), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hkey, 0xff, 2 * H * sizeof(unsigned long long), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hcnt, 0, 2 * H * sizeof(int), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.hfill, 0, 2 * H * sizeof(int), s));
+  TDEM_CUDA_TRY(&h->err, cudaMemsetAsync(D.cursor, 0, 2 * sizeof(int), s));
   const long long items = std::max<long long>(h->n, h->nb);
   const int grid = (int)std::max<long long>(1, std::min<long long>(h->max_grid, (items + kItemsPerBlock - 1) /
                                                                                   kItemsPerBlock));
@@ -1048,7 +1103,8 @@ int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_to
     ++cnt_i[i];
     ++cnt_j[j];
   }
-  std::vector<int> off(n + 1, 0), split(n), inc_bond(2 * (size_t)nb), inc_other(2 * (size_t)nb);
+  std::vector<int> off(n + 1, 0), split(n);
+  std::vector<int2> inc(2 * (size_t)nb);
   for (int k = 0; k < n; ++k) {
     off[k + 1] = off[k] + cnt_i[k] + cnt_j[k];
     split[k] = cnt_i[k];
@@ -1060,10 +1116,8 @@ int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_to
   }
   for (int b = 0; b < nb; ++b) {
     const int i = topo->bond_i[b], j = topo->bond_j[b];
-    inc_bond[fi[i]] = b;
-    inc_other[fi[i]++] = j;
-    inc_bond[fj[j]] = b;
-    inc_other[fj[j]++] = i;
+    inc[fi[i]++] = make_int2(b, j);
+    inc[fj[j]++] = make_int2(b, i);
   }
   tdem_icedem3d* h = new tdem_icedem3d();
   h->cfg = *cfg;
@@ -1091,22 +1145,20 @@ int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_to
   if (topo->creep_reference && (rc = dupload(h, &D.cref, topo->creep_reference, nb))) return fail_out(rc);
   const int* p_off = nullptr;
   const int* p_split = nullptr;
-  const int* p_bond = nullptr;
-  const int* p_other = nullptr;
+  const int2* p_inc = nullptr;
   if ((rc = dupload(h, &p_off, off.data(), off.size())) || (rc = dupload(h, &p_split, split.data(), split.size())) ||
-      (rc = dupload(h, &p_bond, inc_bond.data(), inc_bond.size())) ||
-      (rc = dupload(h, &p_other, inc_other.data(), inc_other.size())))
+      (rc = dupload(h, &p_inc, inc.data(), inc.size())))
     return fail_out(rc);
   D.inc_off = p_off;
   D.inc_split = p_split;
-  D.inc_bond = p_bond;
-  D.inc_other = p_other;
+  D.inc = p_inc;
   if ((rc = dalloc(h, &D.shear, n)) || (rc = dalloc(h, &D.abf, 3 * (size_t)nb)) || (rc = dalloc(h, &D.pkey, n)) ||
-      (rc = dalloc(h, &D.pslot, n)) || (rc = dalloc(h, &D.hkey, H)) || (rc = dalloc(h, &D.hcnt, H)) ||
-      (rc = dalloc(h, &D.hstart, H)) || (rc = dalloc(h, &D.hfill, H)) || (rc = dalloc(h, &D.hmin, H)) ||
-      (rc = dalloc(h, &D.members, n)) || (rc = dalloc(h, &D.ci_cnt, n)) ||
+      (rc = dalloc(h, &D.pslot, n)) || (rc = dalloc(h, &D.hkey, 2 * (size_t)H)) ||
+      (rc = dalloc(h, &D.hcnt, 2 * (size_t)H)) || (rc = dalloc(h, &D.hstart, H)) ||
+      (rc = dalloc(h, &D.hfill, 2 * (size_t)H)) || (rc = dalloc(h, &D.members, n)) || (rc = dalloc(h, &D.ci_cnt, n)) ||
       (rc = dalloc(h, &D.ci_j, (size_t)n * kContacts)) || (rc = dalloc(h, &D.ci_v, (size_t)n * kContacts * 9)) ||
-      (rc = dalloc(h, &D.cj_cnt, n)) || (rc = dalloc(h, &D.cj_i, (size_t)n * kContacts)) ||
+      (rc = dalloc(h, &D.ib_cnt, n)) || (rc = dalloc(h, &D.ib_key, (size_t)n * kContacts)) ||
+      (rc = dalloc(h, &D.ib_idx, (size_t)n * kContacts)) ||
       (rc = dalloc(h, &D.hist_cnt, n)) || (rc = dalloc(h, &D.hist_j, (size_t)n * kHistory)) ||
       (rc = dalloc(h, &D.hist_d, (size_t)n * kHistory * 3)) || (rc = dalloc(h, &D.ledger, TDEM_L3_COUNT)) ||
       (rc = dalloc(h, &D.status, 1)))
@@ -1124,7 +1176,7 @@ int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_to
     return fail_out(TDEM_ERR_CUDA);
   }
   h->max_grid = sms * per_sm;
-  if ((rc = dalloc(h, &D.bar_count, 1)) || (rc = dalloc(h, &D.bar_gen, 1)) || (rc = dalloc(h, &D.cursor, 1)) ||
+  if ((rc = dalloc(h, &D.bar_count, 1)) || (rc = dalloc(h, &D.bar_gen, 1)) || (rc = dalloc(h, &D.cursor, 2)) ||
       (rc = dalloc(h, &D.gflags, 2)) || (rc = dalloc(h, &D.part, (size_t)h->max_grid * kPartials)) ||
       (rc = dalloc(h, &D.pmin, 2 * (size_t)h->max_grid)) || (rc = dalloc(h, &D.pdiss, (size_t)h->max_grid)))
     return fail_out(rc);
