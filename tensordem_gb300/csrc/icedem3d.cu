@@ -1,29 +1,34 @@
 // 3-D reference mode: the FP64 bonded-sphere step of the reference's IceDEM3D
 // (src/tensordem/dem3d.py:564-1663), on sm_103a.
 //
-// Design. One cooperative launch runs many steps of one instance on all SMs
-// (FP64 throughput per SM is small on this part, so the work is spread as
-// wide as it goes). Four phases per step, separated by a grid barrier with a
-// bounded wait; every scratch array lives in the handle. Cells are
-// cell = floor(x / 2r) keyed into open-addressing tables (dem3d.py:825-856
-// builds the same cells in a dict); there are two tables, by step parity, so
-// a step's positions are hashed at the end of the step before.
+// Design. One cooperative launch runs many steps of one instance on all SMs.
+// This part's FP64 pipes are narrow (tens of cycles per warp-wide FP64
+// instruction), so a step is as long as its longest per-thread FP64 chain:
+// the work is cut so that no thread carries more than one particle's share of
+// one sum, without reordering any sum. Five phases per step, separated by a
+// grid barrier with a bounded wait; every scratch array lives in the handle.
+// Cells are cell = floor(x / 2r) keyed into open-addressing tables
+// (dem3d.py:825-856 builds the same cells in a dict); there are two tables,
+// by step parity, so a step's positions are hashed at the end of the step
+// before.
 //   A. cell ranges of this step's table from an atomic cursor; the other
-//      table cleared; objective shear strain per particle (dem3d.py:875-901),
-//      with each particle's bond list fetched in chunks of loads in flight;
+//      table cleared; objective shear strain (dem3d.py:875-901), a 16-lane
+//      group per particle, lane w summing component w of the bond sum in the
+//      bond list's order;
 //   B. bond force, break test and commit, Maxwell branches, creep clock, one
 //      thread per bond (dem3d.py:984-1100, 1342-1360); members into cells;
-//   C. contacts: each particle evaluates its pairs with higher ids over the 27
-//      neighbour cells (lookups of nine cells in flight together), in the
+//   C1. each particle lists its overlapping partners with higher ids in the
 //      reference's pair-list order: cells in offset order, members ascending
-//      (dem3d.py:1374-1514). The partner gets the pair in its inbox with the
-//      key of the reference's order for its side (first particle of this
-//      particle's cell, then this particle);
-//   D. assembly and semi-implicit Euler: each particle sums its force in the
-//      order of the reference's index_add_ calls (bond i-side then j-side,
-//      then per contact term its own pairs then its sorted inbox), then tool,
-//      platens and integration (dem3d.py:1516-1663); the new positions go into
-//      the other table.
+//      (lookups of nine cells in flight together);
+//   C2. one thread per overlapping pair: normal force, friction with the
+//      pair's history, rolling couple (dem3d.py:1382-1514); the partner gets
+//      the pair in its inbox with the key of the reference's order for its
+//      side (first particle of this particle's cell, then this particle);
+//   D. assembly and semi-implicit Euler, four lanes per particle, lane w
+//      summing force component w in the order of the reference's index_add_
+//      calls (bond i-side then j-side, then per contact term its own pairs
+//      then its sorted inbox), then tool, platens and integration
+//      (dem3d.py:1516-1663); the new positions go into the other table.
 // Pair forces that the reference adds as exact zeros are skipped. Every value
 // a particle or bond gets is computed by one thread, independent of the grid,
 // so trajectories are bitwise reproducible; ledger sums combine per-block
@@ -92,7 +97,9 @@ struct Dev {
   int* ib_cnt;    // (n) inbox: pairs in which the particle is the higher id
   unsigned long long* ib_key;  // (n, kContacts) reference order key: first id of the partner's cell, partner
   int* ib_idx;    // (n, kContacts) the pair's entry in the partner's ci_v
-  int* hist_cnt;  // (n)
+  int* hist_cnt;  // (n) entries of each particle's history table
+  int* hist_old;  // (n) entries when the step's contact phase began
+  int* cellmin;   // (n) first particle of each particle's cell
   int* hist_j;    // (n, kHistory)
   double* hist_d; // (n, kHistory, 3)
   double* ledger; // TDEM_L3_COUNT
@@ -258,6 +265,10 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
   const bool friction = P.cone != TDEM_CONE_OFF;
   const bool platen_friction = P.platen_cone != TDEM_CONE_OFF;
   const size_t H = (size_t)D.hmask + 1;
+  // small instances: several lanes per particle (a 16-lane group fits every
+  // particle); large ones: one thread per particle, as lanes would only add
+  // idle and repeated FP64 work
+  const bool wide = (long long)n * 16 <= (long long)gs;
   double* pos = S.positions;
   double* vel = S.velocities;
   double time = O.time;
@@ -291,7 +302,78 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
     }
     if (gt == 0) D.cursor[q] = 0;
     for (int k = gt; k < n; k += gs) D.ib_cnt[k] = 0;
-    if (uf && nb > 0) {
+    if (uf && nb > 0 && wide) {
+      // a 16-lane group per particle; lane w < 9 sums component w = (a, b) of
+      // sum_e q_a r_b over the bond list in order (each component's sum is
+      // the reference's, in its order); the group leader finishes the strain
+      const int sub = threadIdx.x & 15, a = sub / 3, b = sub % 3;
+      const bool comp = sub < 9;
+      const int ngroups = gs >> 4;
+      for (int kb = (gt >> 5) << 1; kb < n; kb += ngroups) {  // warp-uniform: two particles per warp
+        const int k = kb + ((threadIdx.x >> 4) & 1);
+        double c = 0.0;
+        if (k < n && comp) {
+          const double pka = pos[3 * k + a];
+          const int e0 = D.inc_off[k], es = e0 + D.inc_split[k], e1 = D.inc_off[k + 1];
+          for (int e = e0; e < e1; e += kChunk) {
+            int2 ent[kChunk];
+            double oa[kChunk], rb[kChunk];
+#pragma unroll
+            for (int w = 0; w < kChunk; ++w) ent[w] = e + w < e1 ? D.inc[e + w] : make_int2(0, k);
+#pragma unroll
+            for (int w = 0; w < kChunk; ++w) {
+              oa[w] = pos[3 * ent[w].y + a];
+              rb[w] = D.ref[3 * ent[w].x + b];
+            }
+#pragma unroll
+            for (int w = 0; w < kChunk; ++w) {
+              if (e + w >= e1) break;
+              // q = x[j] - x[i] of the bond; this particle is i on its first es - e0 entries
+              const double qa = e + w < es ? oa[w] - pka : pka - oa[w];
+              c += qa * rb[w];
+            }
+          }
+        }
+        double cc[9];
+#pragma unroll
+        for (int w = 0; w < 9; ++w) cc[w] = __shfl_sync(0xffffffffu, c, w, 16);
+        if (k < n && sub == 0) {
+          double shear = 0.0;
+          if (D.frank[k]) {
+            const double* pi = D.pinv + 9 * (size_t)k;
+            double f[9];
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+#pragma unroll
+              for (int y = 0; y < 3; ++y)
+                f[3 * x + y] = (cc[3 * x] * pi[y] + cc[3 * x + 1] * pi[3 + y]) + cc[3 * x + 2] * pi[6 + y];
+            double e[9];
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+#pragma unroll
+              for (int y = 0; y < 3; ++y) {
+                const double g = (f[x] * f[y] + f[3 + x] * f[3 + y]) + f[6 + x] * f[6 + y];
+                e[3 * x + y] = 0.5 * (g - (x == y ? 1.0 : 0.0));
+              }
+            const double mean = ((e[0] + e[4]) + e[8]) / 3.0;
+            e[0] = e[0] - mean;
+            e[4] = e[4] - mean;
+            e[8] = e[8] - mean;
+            // dev.square().sum(dim=(1, 2)): torch's contiguous inner sum of 9
+            // values: the tail element, then the four lanes of two 4-wide loads
+            double sq[9];
+#pragma unroll
+            for (int w = 0; w < 9; ++w) sq[w] = e[w] * e[w];
+            double s2 = sq[8];
+#pragma unroll
+            for (int w = 0; w < 4; ++w) s2 = s2 + (sq[w] + sq[w + 4]);
+            shear = sqrt((2.0 / 3.0) * fmax(s2, 0.0));
+          }
+          D.shear[k] = shear;
+        }
+      }
+    } else if (uf && nb > 0) {
+      // one thread per particle, its bond list fetched in chunks of loads in flight
       for (int k = gt; k < n; k += gs) {
         double c[9];
 #pragma unroll
@@ -464,188 +546,380 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
     }
     TDEM_GRID_SYNC();
 
-    // ---- C: contacts (dem3d.py:1374-1514). Each particle evaluates its pairs
-    // with higher ids, over the 27 neighbour cells in the reference's order
-    // and each cell's members ascending; the higher id gets the pair in its inbox.
-    double acc_fp = 0.0, acc_rp = 0.0, acc_en = 0.0, acc_nc = 0.0;
     const unsigned long long* hkey_p = D.hkey + p * H;
     const int* hcnt_p = D.hcnt + p * H;
-    for (int k = gt; k < n; k += gs) {
-      int nci = 0;
-      const int sk = D.pslot[k];
-      if (sk >= 0) {
-        const unsigned long long kk = D.pkey[k];
-        const long long cx = (long long)(kk >> 42) - kCoordHalf;
-        const long long cy = (long long)((kk >> 21) & ((1ull << 21) - 1)) - kCoordHalf;
-        const long long cz = (long long)(kk & ((1ull << 21) - 1)) - kCoordHalf;
-        const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
-        const double vkx = vel[3 * k], vky = vel[3 * k + 1], vkz = vel[3 * k + 2];
-        const bool fk = S.fixed[k] != 0;
-        int* hj = D.hist_j + (size_t)k * kHistory;
-        double* hd = D.hist_d + (size_t)k * kHistory * 3;
-        int hc = friction ? D.hist_cnt[k] : 0;
-        const int ib0 = D.inc_off[k], ib1 = ib0 + D.inc_split[k];
-        // the first particle of this particle's cell orders the pair in the partner's inbox
-        int own_min = k;
-        {
-          const int m0 = D.hstart[sk], m1 = m0 + hcnt_p[sk];
-          for (int m = m0; m < m1; ++m) own_min = min(own_min, D.members[m]);
-        }
-        const unsigned long long own_key = (unsigned long long)own_min << 32;
-        for (int dx = -1; dx <= 1; ++dx) {
-          // the nine cells of this dx: lookups, then counts and starts, in flight together
-          int sl[9], cnt[9], st[9];
-          unsigned long long ck[9], first[9];
-          unsigned hs[9];
-#pragma unroll
-          for (int o = 0; o < 9; ++o) {
-            ck[o] = pack_cell(cx + dx, cy + o / 3 - 1, cz + o % 3 - 1);
-            hs[o] = hash_slot(ck[o], D.hmask);
-            first[o] = hkey_p[hs[o]];
+    double acc_fp = 0.0, acc_rp = 0.0, acc_en = 0.0, acc_nc = 0.0;
+    if (wide) {
+      // ---- C1: contact candidates (dem3d.py:825-856, 1374-1381). Each particle
+      // lists its overlapping partners with higher ids in the reference's
+      // pair-list order: neighbour cells in offset order, members ascending.
+      for (int k = gt; k < n; k += gs) {
+        int nci = 0;
+        const int sk = D.pslot[k];
+        if (friction) D.hist_old[k] = min(D.hist_cnt[k], kHistory);
+        if (sk >= 0) {
+          const unsigned long long kk = D.pkey[k];
+          const long long cx = (long long)(kk >> 42) - kCoordHalf;
+          const long long cy = (long long)((kk >> 21) & ((1ull << 21) - 1)) - kCoordHalf;
+          const long long cz = (long long)(kk & ((1ull << 21) - 1)) - kCoordHalf;
+          const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
+          // the first particle of this particle's cell orders its pairs in the partners' inboxes
+          int own_min = k;
+          {
+            const int m0 = D.hstart[sk], m1 = m0 + hcnt_p[sk];
+            for (int m = m0; m < m1; ++m) own_min = min(own_min, D.members[m]);
           }
-#pragma unroll
-          for (int o = 0; o < 9; ++o)  // a collision probes on (rare)
-            sl[o] = first[o] == ck[o] ? (int)hs[o] : (first[o] == kEmpty ? -1 : find_cell(hkey_p, D.hmask, ck[o]));
-#pragma unroll
-          for (int o = 0; o < 9; ++o) {
-            cnt[o] = sl[o] >= 0 ? hcnt_p[sl[o]] : 0;
-            st[o] = sl[o] >= 0 ? D.hstart[sl[o]] : 0;
-          }
-          for (int o = 0; o < 9; ++o) {
-            // members of the cell ascending: repeated selection (cells hold a few)
-            int last = -1;
-            for (int t = 0; t < cnt[o]; ++t) {
-              int j = INT_MAX;
-              for (int m = st[o]; m < st[o] + cnt[o]; ++m) {
-                const int x = D.members[m];
-                if (x > last && x < j) j = x;
-              }
-              last = j;
-              if (j <= k) continue;
-              const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
-              const double dist = norm3(ex, ey, ez);
-              const double ov = fmax(two_r - dist, 0.0);
-              if (!(ov > 0.0)) continue;
-              if (nci == kContacts) {
-                flags |= kStatusContacts;
-                continue;
-              }
-              bool balive = false;
-              for (int e = ib0; e < ib1; ++e) {
-                const int2 en = D.inc[e];
-                if (en.y == j) {
-                  balive = S.alive[en.x] != 0;
-                  break;
+          D.cellmin[k] = own_min;
+          for (int dx = -1; dx <= 1; ++dx) {
+            // the nine cells of this dx: lookups, then counts and starts, in flight together
+            int sl[9], cnt[9], st[9];
+            unsigned long long ck[9], first[9];
+            unsigned hs[9];
+  #pragma unroll
+            for (int o = 0; o < 9; ++o) {
+              ck[o] = pack_cell(cx + dx, cy + o / 3 - 1, cz + o % 3 - 1);
+              hs[o] = hash_slot(ck[o], D.hmask);
+              first[o] = hkey_p[hs[o]];
+            }
+  #pragma unroll
+            for (int o = 0; o < 9; ++o)  // a collision probes on (rare)
+              sl[o] = first[o] == ck[o] ? (int)hs[o] : (first[o] == kEmpty ? -1 : find_cell(hkey_p, D.hmask, ck[o]));
+  #pragma unroll
+            for (int o = 0; o < 9; ++o) {
+              cnt[o] = sl[o] >= 0 ? hcnt_p[sl[o]] : 0;
+              st[o] = sl[o] >= 0 ? D.hstart[sl[o]] : 0;
+            }
+            for (int o = 0; o < 9; ++o) {
+              // members of the cell ascending: repeated selection (cells hold a few)
+              int last = -1;
+              for (int t = 0; t < cnt[o]; ++t) {
+                int j = INT_MAX;
+                for (int m = st[o]; m < st[o] + cnt[o]; ++m) {
+                  const int x = D.members[m];
+                  if (x > last && x < j) j = x;
                 }
-              }
-              const double dc = fmax(dist, kEps);
-              const double nx = ex / dc, ny = ey / dc, nz = ez / dc;
-              const double vjx = vel[3 * j], vjy = vel[3 * j + 1], vjz = vel[3 * j + 2];
-              const double rvx = vjx - vkx, rvy = vjy - vky, rvz = vjz - vkz;
-              const double vn = (rvx * nx + rvy * ny) + rvz * nz;
-              const bool pinned = P.any_fixed && (fk != (S.fixed[j] != 0));
-              const double k_local = P.hertz ? P.hertz_kn * sqrt(ov) : P.contact_k;
-              double gamma = 0.0;
-              if (P.damping == 2) {
-                gamma = P.damping_c;
-              } else if (P.damping == 1) {
-                gamma = P.hertz ? P.damping_c * sqrt(k_local * (pinned ? P.mass_pinned : P.mass_mobile))
-                              : (pinned ? P.gamma_pinned : P.gamma_mobile);
-              }
-              double mag = fmax(k_local * ov - gamma * vn, 0.0);
-              if (balive) mag = 0.0;
-              else acc_en += P.hertz ? P.hertz_pot * pow(ov, 2.5) : (0.5 * P.contact_k) * (ov * ov);
-              double* out = D.ci_v + ((size_t)k * kContacts + nci) * 9;
-              const double vtx = rvx - vn * nx, vty = rvy - vn * ny, vtz = rvz - vn * nz;
-              if (friction) {
-                // Cundall-Strack spring with the pair's stored displacement
-                int h = -1;
-                for (int q = 0; q < hc; ++q)
-                  if (hj[q] == j) {
-                    h = q;
-                    break;
-                  }
-                double tx = 0.0, ty = 0.0, tz = 0.0;
-                if (h >= 0) {
-                  tx = hd[3 * h];
-                  ty = hd[3 * h + 1];
-                  tz = hd[3 * h + 2];
+                last = j;
+                if (j <= k) continue;
+                const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
+                const double ov = fmax(two_r - norm3(ex, ey, ez), 0.0);
+                if (!(ov > 0.0)) continue;
+                if (nci == kContacts) {
+                  flags |= kStatusContacts;
+                  continue;
                 }
-                if (uh) {
-                  tx = tx + vtx * P.dt;
-                  ty = ty + vty * P.dt;
-                  tz = tz + vtz * P.dt;
-                }
-                const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
-                const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
-                const double fm = norm3(fx, fy, fz);
-                const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
-                const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
-                const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
-                out[0] = Fx;
-                out[1] = Fy;
-                out[2] = Fz;
-                acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
-                if (uh) {
-                  const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
-                  if (h >= 0) {
-                    hd[3 * h] = sx;
-                    hd[3 * h + 1] = sy;
-                    hd[3 * h + 2] = sz;
-                  } else if (sx != 0.0 || sy != 0.0 || sz != 0.0) {
-                    // an absent entry reads as zero, so only non-zero values need a slot
-                    if (hc == kHistory) {
-                      flags |= kStatusHistory;
-                    } else {
-                      hj[hc] = j;
-                      hd[3 * hc] = sx;
-                      hd[3 * hc + 1] = sy;
-                      hd[3 * hc + 2] = sz;
-                      ++hc;
-                    }
-                  }
-                }
+                D.ci_j[(size_t)k * kContacts + nci] = j;
+                ++nci;
               }
-              if (P.rolling) {
-                // rolling-resistance couple (dem3d.py:1242-1299)
-                const double vtm = norm3(vtx, vty, vtz);
-                double hx = 0.0, hy = 0.0, hz = 0.0;
-                if (vtm > 1e-15) {
-                  const double vc = fmax(vtm, kEps);
-                  hx = vtx / vc;
-                  hy = vty / vc;
-                  hz = vtz / vc;
-                }
-                const double fm = -(P.roll_mu * mag);
-                const double jx = fm * hx, jy = fm * hy, jz = fm * hz;
-                out[3] = jx;
-                out[4] = jy;
-                out[5] = jz;
-                acc_rp += ((-jx) * (vkx - vjx) + (-jy) * (vky - vjy)) + (-jz) * (vkz - vjz);
-              }
-              const double cm = -mag;
-              out[6] = cm * nx;
-              out[7] = cm * ny;
-              out[8] = cm * nz;
-              D.ci_j[(size_t)k * kContacts + nci] = j;
-              const int slot = atomicAdd(&D.ib_cnt[j], 1);
-              if (slot < kContacts) {
-                D.ib_key[(size_t)j * kContacts + slot] = own_key | (unsigned)k;
-                D.ib_idx[(size_t)j * kContacts + slot] = k * kContacts + nci;
-              } else {
-                flags |= kStatusContacts;
-              }
-              ++nci;
             }
           }
         }
-        if (friction) {
-          D.hist_cnt[k] = hc;
-          hist_max = max(hist_max, hc);
+        D.ci_cnt[k] = nci;
+      }
+      TDEM_GRID_SYNC();
+      // ---- C2: one thread per overlapping pair (dem3d.py:1382-1514): normal
+      // force, friction with the pair's history, rolling couple; the partner
+      // gets the pair in its inbox with the reference's order key of its side.
+      for (long long tt = gt; tt < (long long)n * kContacts; tt += gs) {
+        const int k = (int)(tt / kContacts), c = (int)(tt % kContacts);
+        if (c >= D.ci_cnt[k]) continue;
+        const int j = D.ci_j[(size_t)k * kContacts + c];
+        const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
+        const double vkx = vel[3 * k], vky = vel[3 * k + 1], vkz = vel[3 * k + 2];
+        const bool fk = S.fixed[k] != 0;
+        const int ib0 = D.inc_off[k], ib1 = ib0 + D.inc_split[k];
+        int* hj = D.hist_j + (size_t)k * kHistory;
+        double* hd = D.hist_d + (size_t)k * kHistory * 3;
+        const int hc = friction ? D.hist_old[k] : 0;
+        const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
+        const double dist = norm3(ex, ey, ez);
+        const double ov = fmax(two_r - dist, 0.0);
+        acc_nc += 1.0;
+                bool balive = false;
+                for (int e = ib0; e < ib1; ++e) {
+                  const int2 en = D.inc[e];
+                  if (en.y == j) {
+                    balive = S.alive[en.x] != 0;
+                    break;
+                  }
+                }
+                const double dc = fmax(dist, kEps);
+                const double nx = ex / dc, ny = ey / dc, nz = ez / dc;
+                const double vjx = vel[3 * j], vjy = vel[3 * j + 1], vjz = vel[3 * j + 2];
+                const double rvx = vjx - vkx, rvy = vjy - vky, rvz = vjz - vkz;
+                const double vn = (rvx * nx + rvy * ny) + rvz * nz;
+                const bool pinned = P.any_fixed && (fk != (S.fixed[j] != 0));
+                const double k_local = P.hertz ? P.hertz_kn * sqrt(ov) : P.contact_k;
+                double gamma = 0.0;
+                if (P.damping == 2) {
+                  gamma = P.damping_c;
+                } else if (P.damping == 1) {
+                  gamma = P.hertz ? P.damping_c * sqrt(k_local * (pinned ? P.mass_pinned : P.mass_mobile))
+                                : (pinned ? P.gamma_pinned : P.gamma_mobile);
+                }
+                double mag = fmax(k_local * ov - gamma * vn, 0.0);
+                if (balive) mag = 0.0;
+                else acc_en += P.hertz ? P.hertz_pot * pow(ov, 2.5) : (0.5 * P.contact_k) * (ov * ov);
+                double* out = D.ci_v + ((size_t)k * kContacts + c) * 9;
+                const double vtx = rvx - vn * nx, vty = rvy - vn * ny, vtz = rvz - vn * nz;
+                if (friction) {
+                  // Cundall-Strack spring with the pair's stored displacement
+                  int h = -1;
+                  for (int q = 0; q < hc; ++q)  // the entries that existed when the step began
+                    if (hj[q] == j) {
+                      h = q;
+                      break;
+                    }
+                  double tx = 0.0, ty = 0.0, tz = 0.0;
+                  if (h >= 0) {
+                    tx = hd[3 * h];
+                    ty = hd[3 * h + 1];
+                    tz = hd[3 * h + 2];
+                  }
+                  if (uh) {
+                    tx = tx + vtx * P.dt;
+                    ty = ty + vty * P.dt;
+                    tz = tz + vtz * P.dt;
+                  }
+                  const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
+                  const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
+                  const double fm = norm3(fx, fy, fz);
+                  const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
+                  const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
+                  const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
+                  out[0] = Fx;
+                  out[1] = Fy;
+                  out[2] = Fz;
+                  acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
+                  if (uh) {
+                    const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
+                    if (h >= 0) {
+                      hd[3 * h] = sx;
+                      hd[3 * h + 1] = sy;
+                      hd[3 * h + 2] = sz;
+                    } else if (sx != 0.0 || sy != 0.0 || sz != 0.0) {
+                      // an absent entry reads as zero, so only non-zero values need a slot
+                      const int slot = atomicAdd(&D.hist_cnt[k], 1);
+                      if (slot >= kHistory) {
+                        flags |= kStatusHistory;
+                      } else {
+                        hj[slot] = j;
+                        hd[3 * slot] = sx;
+                        hd[3 * slot + 1] = sy;
+                        hd[3 * slot + 2] = sz;
+                      }
+                    }
+                  }
+                }
+                if (P.rolling) {
+                  // rolling-resistance couple (dem3d.py:1242-1299)
+                  const double vtm = norm3(vtx, vty, vtz);
+                  double hx = 0.0, hy = 0.0, hz = 0.0;
+                  if (vtm > 1e-15) {
+                    const double vc = fmax(vtm, kEps);
+                    hx = vtx / vc;
+                    hy = vty / vc;
+                    hz = vtz / vc;
+                  }
+                  const double fm = -(P.roll_mu * mag);
+                  const double jx = fm * hx, jy = fm * hy, jz = fm * hz;
+                  out[3] = jx;
+                  out[4] = jy;
+                  out[5] = jz;
+                  acc_rp += ((-jx) * (vkx - vjx) + (-jy) * (vky - vjy)) + (-jz) * (vkz - vjz);
+                }
+                const double cm = -mag;
+                out[6] = cm * nx;
+                out[7] = cm * ny;
+                out[8] = cm * nz;
+        const int slot = atomicAdd(&D.ib_cnt[j], 1);
+        if (slot < kContacts) {
+          D.ib_key[(size_t)j * kContacts + slot] = ((unsigned long long)D.cellmin[k] << 32) | (unsigned)k;
+          D.ib_idx[(size_t)j * kContacts + slot] = k * kContacts + c;
+        } else {
+          flags |= kStatusContacts;
         }
       }
-      D.ci_cnt[k] = nci;
-      acc_nc += (double)nci;
+    } else {
+      // ---- C: contacts (dem3d.py:1374-1514). Each particle evaluates its pairs
+      // with higher ids, over the 27 neighbour cells in the reference's order
+      // and each cell's members ascending; the higher id gets the pair in its inbox.
+      for (int k = gt; k < n; k += gs) {
+        int nci = 0;
+        const int sk = D.pslot[k];
+        if (sk >= 0) {
+          const unsigned long long kk = D.pkey[k];
+          const long long cx = (long long)(kk >> 42) - kCoordHalf;
+          const long long cy = (long long)((kk >> 21) & ((1ull << 21) - 1)) - kCoordHalf;
+          const long long cz = (long long)(kk & ((1ull << 21) - 1)) - kCoordHalf;
+          const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
+          const double vkx = vel[3 * k], vky = vel[3 * k + 1], vkz = vel[3 * k + 2];
+          const bool fk = S.fixed[k] != 0;
+          int* hj = D.hist_j + (size_t)k * kHistory;
+          double* hd = D.hist_d + (size_t)k * kHistory * 3;
+          int hc = friction ? D.hist_cnt[k] : 0;
+          const int ib0 = D.inc_off[k], ib1 = ib0 + D.inc_split[k];
+          // the first particle of this particle's cell orders the pair in the partner's inbox
+          int own_min = k;
+          {
+            const int m0 = D.hstart[sk], m1 = m0 + hcnt_p[sk];
+            for (int m = m0; m < m1; ++m) own_min = min(own_min, D.members[m]);
+          }
+          const unsigned long long own_key = (unsigned long long)own_min << 32;
+          for (int dx = -1; dx <= 1; ++dx) {
+            // the nine cells of this dx: lookups, then counts and starts, in flight together
+            int sl[9], cnt[9], st[9];
+            unsigned long long ck[9], first[9];
+            unsigned hs[9];
+  #pragma unroll
+            for (int o = 0; o < 9; ++o) {
+              ck[o] = pack_cell(cx + dx, cy + o / 3 - 1, cz + o % 3 - 1);
+              hs[o] = hash_slot(ck[o], D.hmask);
+              first[o] = hkey_p[hs[o]];
+            }
+  #pragma unroll
+            for (int o = 0; o < 9; ++o)  // a collision probes on (rare)
+              sl[o] = first[o] == ck[o] ? (int)hs[o] : (first[o] == kEmpty ? -1 : find_cell(hkey_p, D.hmask, ck[o]));
+  #pragma unroll
+            for (int o = 0; o < 9; ++o) {
+              cnt[o] = sl[o] >= 0 ? hcnt_p[sl[o]] : 0;
+              st[o] = sl[o] >= 0 ? D.hstart[sl[o]] : 0;
+            }
+            for (int o = 0; o < 9; ++o) {
+              // members of the cell ascending: repeated selection (cells hold a few)
+              int last = -1;
+              for (int t = 0; t < cnt[o]; ++t) {
+                int j = INT_MAX;
+                for (int m = st[o]; m < st[o] + cnt[o]; ++m) {
+                  const int x = D.members[m];
+                  if (x > last && x < j) j = x;
+                }
+                last = j;
+                if (j <= k) continue;
+                const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
+                const double dist = norm3(ex, ey, ez);
+                const double ov = fmax(two_r - dist, 0.0);
+                if (!(ov > 0.0)) continue;
+                if (nci == kContacts) {
+                  flags |= kStatusContacts;
+                  continue;
+                }
+                bool balive = false;
+                for (int e = ib0; e < ib1; ++e) {
+                  const int2 en = D.inc[e];
+                  if (en.y == j) {
+                    balive = S.alive[en.x] != 0;
+                    break;
+                  }
+                }
+                const double dc = fmax(dist, kEps);
+                const double nx = ex / dc, ny = ey / dc, nz = ez / dc;
+                const double vjx = vel[3 * j], vjy = vel[3 * j + 1], vjz = vel[3 * j + 2];
+                const double rvx = vjx - vkx, rvy = vjy - vky, rvz = vjz - vkz;
+                const double vn = (rvx * nx + rvy * ny) + rvz * nz;
+                const bool pinned = P.any_fixed && (fk != (S.fixed[j] != 0));
+                const double k_local = P.hertz ? P.hertz_kn * sqrt(ov) : P.contact_k;
+                double gamma = 0.0;
+                if (P.damping == 2) {
+                  gamma = P.damping_c;
+                } else if (P.damping == 1) {
+                  gamma = P.hertz ? P.damping_c * sqrt(k_local * (pinned ? P.mass_pinned : P.mass_mobile))
+                                : (pinned ? P.gamma_pinned : P.gamma_mobile);
+                }
+                double mag = fmax(k_local * ov - gamma * vn, 0.0);
+                if (balive) mag = 0.0;
+                else acc_en += P.hertz ? P.hertz_pot * pow(ov, 2.5) : (0.5 * P.contact_k) * (ov * ov);
+                double* out = D.ci_v + ((size_t)k * kContacts + nci) * 9;
+                const double vtx = rvx - vn * nx, vty = rvy - vn * ny, vtz = rvz - vn * nz;
+                if (friction) {
+                  // Cundall-Strack spring with the pair's stored displacement
+                  int h = -1;
+                  for (int q = 0; q < hc; ++q)
+                    if (hj[q] == j) {
+                      h = q;
+                      break;
+                    }
+                  double tx = 0.0, ty = 0.0, tz = 0.0;
+                  if (h >= 0) {
+                    tx = hd[3 * h];
+                    ty = hd[3 * h + 1];
+                    tz = hd[3 * h + 2];
+                  }
+                  if (uh) {
+                    tx = tx + vtx * P.dt;
+                    ty = ty + vty * P.dt;
+                    tz = tz + vtz * P.dt;
+                  }
+                  const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
+                  const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
+                  const double fm = norm3(fx, fy, fz);
+                  const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
+                  const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
+                  const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
+                  out[0] = Fx;
+                  out[1] = Fy;
+                  out[2] = Fz;
+                  acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
+                  if (uh) {
+                    const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
+                    if (h >= 0) {
+                      hd[3 * h] = sx;
+                      hd[3 * h + 1] = sy;
+                      hd[3 * h + 2] = sz;
+                    } else if (sx != 0.0 || sy != 0.0 || sz != 0.0) {
+                      // an absent entry reads as zero, so only non-zero values need a slot
+                      if (hc == kHistory) {
+                        flags |= kStatusHistory;
+                      } else {
+                        hj[hc] = j;
+                        hd[3 * hc] = sx;
+                        hd[3 * hc + 1] = sy;
+                        hd[3 * hc + 2] = sz;
+                        ++hc;
+                      }
+                    }
+                  }
+                }
+                if (P.rolling) {
+                  // rolling-resistance couple (dem3d.py:1242-1299)
+                  const double vtm = norm3(vtx, vty, vtz);
+                  double hx = 0.0, hy = 0.0, hz = 0.0;
+                  if (vtm > 1e-15) {
+                    const double vc = fmax(vtm, kEps);
+                    hx = vtx / vc;
+                    hy = vty / vc;
+                    hz = vtz / vc;
+                  }
+                  const double fm = -(P.roll_mu * mag);
+                  const double jx = fm * hx, jy = fm * hy, jz = fm * hz;
+                  out[3] = jx;
+                  out[4] = jy;
+                  out[5] = jz;
+                  acc_rp += ((-jx) * (vkx - vjx) + (-jy) * (vky - vjy)) + (-jz) * (vkz - vjz);
+                }
+                const double cm = -mag;
+                out[6] = cm * nx;
+                out[7] = cm * ny;
+                out[8] = cm * nz;
+                D.ci_j[(size_t)k * kContacts + nci] = j;
+                const int slot = atomicAdd(&D.ib_cnt[j], 1);
+                if (slot < kContacts) {
+                  D.ib_key[(size_t)j * kContacts + slot] = own_key | (unsigned)k;
+                  D.ib_idx[(size_t)j * kContacts + slot] = k * kContacts + nci;
+                } else {
+                  flags |= kStatusContacts;
+                }
+                ++nci;
+              }
+            }
+          }
+          if (friction) {
+            D.hist_cnt[k] = hc;
+            hist_max = max(hist_max, hc);
+          }
+        }
+        D.ci_cnt[k] = nci;
+        acc_nc += (double)nci;
+      }
     }
     TDEM_GRID_SYNC();
 
@@ -664,235 +938,433 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
       lvx = S.lateral_velocity[0];
       lvy = S.lateral_velocity[2];
     }
-    for (int k = gt; k < n; k += gs) {
-      const double px = pos[3 * k], py = pos[3 * k + 1], pz = pos[3 * k + 2];
-      const double vx = vel[3 * k], vy = vel[3 * k + 1], vz = vel[3 * k + 2];
-      double fx = (-P.drag) * vx, fy = (-P.drag) * vy, fz = (-P.drag) * vz;
-      if (P.body & 1) {
-        double bx = 0.0, by = 0.0, bz = 0.0;
-        if (P.gravity_force > 0.0) bz = bz - P.gravity_force;
-        if (P.body & 2) {
-          const double fs = submerged(P, pz);
-          bz = bz + P.buoyancy_force * fs;
-          if (P.body & 4) {
-            const double c = P.wet_drag * fs;
-            bx = bx - c * vx;
-            by = by - c * vy;
-            bz = bz - c * vz;
+    if (wide) {
+      const int w = threadIdx.x & 3;
+      const int ngroups = gs >> 2;
+      for (int kb = (gt >> 5) << 3; kb < n; kb += ngroups) {  // warp-uniform: eight particles per warp
+        const int k = kb + ((threadIdx.x >> 2) & 7);
+        const bool act = k < n, on = act && w < 3;
+        double px = 0.0, py = 0.0, pz = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+        double tdv[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+        if (act) {
+          px = pos[3 * k];
+          py = pos[3 * k + 1];
+          pz = pos[3 * k + 2];
+          vx = vel[3 * k];
+          vy = vel[3 * k + 1];
+          vz = vel[3 * k + 2];
+          if (platen_friction)
+            for (int c = 0; c < 3; ++c) {
+              tdv[0][c] = S.top_tangential[3 * (size_t)k + c];
+              tdv[1][c] = S.bottom_tangential[3 * (size_t)k + c];
+            }
+        }
+        const double pw = w == 0 ? px : (w == 1 ? py : pz);
+        const double vw = w == 0 ? vx : (w == 1 ? vy : vz);
+        double f = 0.0, nv = 0.0, np = 0.0;
+        if (on) {
+          f = (-P.drag) * vw;
+          if (P.body & 1) {
+            double bw = 0.0;
+            if (w == 2 && P.gravity_force > 0.0) bw = bw - P.gravity_force;
+            if (P.body & 2) {
+              const double fs = submerged(P, pz);
+              if (w == 2) bw = bw + P.buoyancy_force * fs;
+              if (P.body & 4) {
+                const double c = P.wet_drag * fs;
+                bw = bw - c * vw;
+              }
+            }
+            f = f + bw;
           }
-        }
-        fx = fx + bx;
-        fy = fy + by;
-        fz = fz + bz;
-      }
-      if (loads) {
-        fx = fx + loads[3 * k];
-        fy = fy + loads[3 * k + 1];
-        fz = fz + loads[3 * k + 2];
-      }
-      // bonds: i side then j side in bond order, as the two index_add_ calls
-      // add them (a dead bond adds its zero too)
-      const int e0 = D.inc_off[k], es = e0 + D.inc_split[k], e1 = D.inc_off[k + 1];
-      for (int e = e0; e < e1; e += kChunk) {
-        int2 ent[kChunk];
-        double ax[kChunk], ay[kChunk], az[kChunk];
+          if (loads) f = f + loads[3 * k + w];
+          // bonds: i side then j side in bond order, as the two index_add_ calls
+          // add them (a dead bond adds its zero too)
+          const int e0 = D.inc_off[k], es = e0 + D.inc_split[k], e1 = D.inc_off[k + 1];
+          for (int e = e0; e < e1; e += kChunk) {
+            int2 ent[kChunk];
+            double aw[kChunk];
 #pragma unroll
-        for (int w = 0; w < kChunk; ++w) ent[w] = e + w < e1 ? D.inc[e + w] : make_int2(0, 0);
+            for (int c = 0; c < kChunk; ++c) ent[c] = e + c < e1 ? D.inc[e + c] : make_int2(0, 0);
 #pragma unroll
-        for (int w = 0; w < kChunk; ++w) {
-          const double* a = D.abf + 3 * (size_t)ent[w].x;
-          ax[w] = a[0];
-          ay[w] = a[1];
-          az[w] = a[2];
-        }
+            for (int c = 0; c < kChunk; ++c) aw[c] = D.abf[3 * (size_t)ent[c].x + w];
 #pragma unroll
-        for (int w = 0; w < kChunk; ++w) {
-          if (e + w >= e1) break;
-          if (e + w < es) {
-            fx += ax[w];
-            fy += ay[w];
-            fz += az[w];
+            for (int c = 0; c < kChunk; ++c) {
+              if (e + c >= e1) break;
+              if (e + c < es) f += aw[c];
+              else f += -aw[c];
+            }
+          }
+          const int nci = D.ci_cnt[k];
+          const double* mine = D.ci_v + (size_t)k * kContacts * 9;
+          // inbox in the reference's order of the pairs in which this particle is second
+          const int nib = min(D.ib_cnt[k], kContacts);
+          unsigned long long ik[kContacts];
+          int ix[kContacts];
+          for (int a = 0; a < nib; ++a) {
+            const unsigned long long key = D.ib_key[(size_t)k * kContacts + a];
+            const int idx = D.ib_idx[(size_t)k * kContacts + a];
+            int b = a - 1;
+            while (b >= 0 && ik[b] > key) {
+              ik[b + 1] = ik[b];
+              ix[b + 1] = ix[b];
+              --b;
+            }
+            ik[b + 1] = key;
+            ix[b + 1] = idx;
+          }
+          if (friction) {
+            for (int c = 0; c < nci; ++c) f += mine[9 * c + w];
+            for (int c = 0; c < nib; ++c) f += -D.ci_v[(size_t)ix[c] * 9 + w];
+          }
+          if (P.rolling) {
+            for (int c = 0; c < nci; ++c) f += -mine[9 * c + 3 + w];
+            for (int c = 0; c < nib; ++c) f += D.ci_v[(size_t)ix[c] * 9 + 3 + w];
+          }
+          for (int c = 0; c < nci; ++c) f += mine[9 * c + 6 + w];
+          for (int c = 0; c < nib; ++c) f += -D.ci_v[(size_t)ix[c] * 9 + 6 + w];
+          // spherical indenter (dem3d.py:1519-1532)
+          {
+            const double dx = px - tpx, dy = py - tpy, dz = pz - tpz;
+            const double dist = norm3(dx, dy, dz);
+            double nx = 0.0, ny = 0.0, nz = -1.0;
+            if (dist > kEps) {
+              const double dc = fmax(dist, kEps);
+              nx = dx / dc;
+              ny = dy / dc;
+              nz = dz / dc;
+            }
+            const double ov = fmax((P.radius + P.tool_radius) - dist, 0.0);
+            const double vn = ((vx - P.tool_velocity[0]) * nx + (vy - P.tool_velocity[1]) * ny) +
+                              (vz - P.tool_velocity[2]) * nz;
+            const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.contact_k * ov;
+            double mag = fmax(el - P.tool_damping * vn, 0.0);
+            if (!(ov > 0.0)) mag = 0.0;
+            const double tw = mag * (w == 0 ? nx : (w == 1 ? ny : nz));
+            acc[w] += tw;
+            f += tw;
+          }
+          // plane platens (dem3d.py:1534-1580) with Coulomb friction (dem3d.py:1187-1240)
+          for (int side = 0; side < 2; ++side) {
+            if (!(P.platens & (1 << side))) continue;
+            double ov, mag;
+            if (side == 0) {
+              ov = fmax((pz + P.radius) - top_z, 0.0);
+              const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
+              mag = fmax(el + P.platen_c * (vz - P.top_velocity), 0.0);
+              if (!(ov > 0.0)) mag = 0.0;
+              if (w == 2) {
+                f += -mag;
+                acc[3] += mag;
+              }
+            } else {
+              ov = fmax((bottom_z + P.radius) - pz, 0.0);
+              const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
+              mag = fmax(el - P.platen_c * (vz - P.bottom_velocity), 0.0);
+              if (!(ov > 0.0)) mag = 0.0;
+              if (w == 2) {
+                f += mag;
+                acc[4] += -mag;
+              }
+            }
+            if (platen_friction) {
+              const bool touch = ov > 0.0;
+              const double ux = touch ? vx : 0.0, uy = touch ? vy : 0.0;
+              const double slip = norm3(ux, uy, 0.0);
+              double* t = tdv[side];
+              if (uh) {
+                t[0] = t[0] + ux * P.dt;
+                t[1] = t[1] + uy * P.dt;
+                t[2] = t[2] + 0.0 * P.dt;
+                if (!touch) t[0] = t[1] = t[2] = 0.0;
+              }
+              const double kk = -P.platen_kt;
+              const double sx = kk * t[0], sy = kk * t[1], sz = kk * t[2];
+              const double sm = norm3(sx, sy, sz);
+              const double lim = cone_limit(P.platen_cone, P.platen_cone_c, sm, mag, slip);
+              const double sc = sm > lim ? lim / fmax(sm, kEps) : 1.0;
+              f += (w == 0 ? sx : (w == 1 ? sy : sz)) * sc;
+            }
+          }
+          if ((P.platens & 4) && w < 2) {
+            // lateral servo platens (dem3d.py:1582-1623): lane 0 the x planes, lane 1 the y planes
+            const double r = P.radius;
+            const double lv = w == 0 ? lvx : lvy;
+            double ov = fmax((lp[2 * w] - pw) + r, 0.0);
+            double mg = fmax(P.lateral_k * ov - P.lateral_c * (vw - lv), 0.0);
+            if (!(ov > 0.0)) mg = 0.0;
+            f += mg;
+            acc[5 + 2 * w] += -mg;
+            ov = fmax((pw + r) - lp[2 * w + 1], 0.0);
+            mg = fmax(P.lateral_k * ov + P.lateral_c * (vw - lv), 0.0);
+            if (!(ov > 0.0)) mg = 0.0;
+            f -= mg;
+            acc[6 + 2 * w] += mg;
+          }
+          if (O.mode == 1) {
+            O.force[3 * k + w] = f;
           } else {
-            fx += -ax[w];
-            fy += -ay[w];
-            fz += -az[w];
+            const bool fixed = S.fixed[k] != 0;
+            double a = f / P.mass;
+            if (fixed) a = 0.0;
+            nv = vw + a * P.dt;
+            if (fixed) nv = 0.0;
+            np = pw + nv * P.dt;
+            if (fixed) np = S.initial_positions[3 * k + w];
           }
         }
-      }
-      const int nci = D.ci_cnt[k];
-      const double* mine = D.ci_v + (size_t)k * kContacts * 9;
-      // inbox in the reference's order of the pairs in which this particle is second
-      const int nib = min(D.ib_cnt[k], kContacts);
-      unsigned long long ik[kContacts];
-      int ix[kContacts];
-      for (int a = 0; a < nib; ++a) {
-        const unsigned long long key = D.ib_key[(size_t)k * kContacts + a];
-        const int idx = D.ib_idx[(size_t)k * kContacts + a];
-        int b = a - 1;
-        while (b >= 0 && ik[b] > key) {
-          ik[b + 1] = ik[b];
-          ix[b + 1] = ix[b];
-          --b;
+        __syncwarp();  // every lane has read the particle's state
+        if (on && O.mode != 1) {
+          vel[3 * k + w] = nv;
+          pos[3 * k + w] = np;
+          if (platen_friction && uh) {
+            if (P.platens & 1) S.top_tangential[3 * (size_t)k + w] = tdv[0][w];
+            if (P.platens & 2) S.bottom_tangential[3 * (size_t)k + w] = tdv[1][w];
+          }
+          if (!(isfinite(np) && isfinite(nv))) flags |= kStatusNonfinite;
         }
-        ik[b + 1] = key;
-        ix[b + 1] = idx;
+        const double n0 = __shfl_sync(0xffffffffu, np, 0, 4);
+        const double n1 = __shfl_sync(0xffffffffu, np, 1, 4);
+        const double n2 = __shfl_sync(0xffffffffu, np, 2, 4);
+        if (act && w == 0) {
+          if (O.mode != 1) insert_cell(D, q, k, n0, n1, n2, width, flags);  // the next step's cell table
+          if (friction) hist_max = max(hist_max, min(D.hist_cnt[k], kHistory));
+        }
       }
-      if (friction) {
+    } else {
+      // one thread per particle
+      for (int k = gt; k < n; k += gs) {
+        const double px = pos[3 * k], py = pos[3 * k + 1], pz = pos[3 * k + 2];
+        const double vx = vel[3 * k], vy = vel[3 * k + 1], vz = vel[3 * k + 2];
+        double fx = (-P.drag) * vx, fy = (-P.drag) * vy, fz = (-P.drag) * vz;
+        if (P.body & 1) {
+          double bx = 0.0, by = 0.0, bz = 0.0;
+          if (P.gravity_force > 0.0) bz = bz - P.gravity_force;
+          if (P.body & 2) {
+            const double fs = submerged(P, pz);
+            bz = bz + P.buoyancy_force * fs;
+            if (P.body & 4) {
+              const double c = P.wet_drag * fs;
+              bx = bx - c * vx;
+              by = by - c * vy;
+              bz = bz - c * vz;
+            }
+          }
+          fx = fx + bx;
+          fy = fy + by;
+          fz = fz + bz;
+        }
+        if (loads) {
+          fx = fx + loads[3 * k];
+          fy = fy + loads[3 * k + 1];
+          fz = fz + loads[3 * k + 2];
+        }
+        // bonds: i side then j side in bond order, as the two index_add_ calls
+        // add them (a dead bond adds its zero too)
+        const int e0 = D.inc_off[k], es = e0 + D.inc_split[k], e1 = D.inc_off[k + 1];
+        for (int e = e0; e < e1; e += kChunk) {
+          int2 ent[kChunk];
+          double ax[kChunk], ay[kChunk], az[kChunk];
+  #pragma unroll
+          for (int w = 0; w < kChunk; ++w) ent[w] = e + w < e1 ? D.inc[e + w] : make_int2(0, 0);
+  #pragma unroll
+          for (int w = 0; w < kChunk; ++w) {
+            const double* a = D.abf + 3 * (size_t)ent[w].x;
+            ax[w] = a[0];
+            ay[w] = a[1];
+            az[w] = a[2];
+          }
+  #pragma unroll
+          for (int w = 0; w < kChunk; ++w) {
+            if (e + w >= e1) break;
+            if (e + w < es) {
+              fx += ax[w];
+              fy += ay[w];
+              fz += az[w];
+            } else {
+              fx += -ax[w];
+              fy += -ay[w];
+              fz += -az[w];
+            }
+          }
+        }
+        const int nci = D.ci_cnt[k];
+        const double* mine = D.ci_v + (size_t)k * kContacts * 9;
+        // inbox in the reference's order of the pairs in which this particle is second
+        const int nib = min(D.ib_cnt[k], kContacts);
+        unsigned long long ik[kContacts];
+        int ix[kContacts];
+        for (int a = 0; a < nib; ++a) {
+          const unsigned long long key = D.ib_key[(size_t)k * kContacts + a];
+          const int idx = D.ib_idx[(size_t)k * kContacts + a];
+          int b = a - 1;
+          while (b >= 0 && ik[b] > key) {
+            ik[b + 1] = ik[b];
+            ix[b + 1] = ix[b];
+            --b;
+          }
+          ik[b + 1] = key;
+          ix[b + 1] = idx;
+        }
+        if (friction) {
+          for (int c = 0; c < nci; ++c) {
+            fx += mine[9 * c];
+            fy += mine[9 * c + 1];
+            fz += mine[9 * c + 2];
+          }
+          for (int c = 0; c < nib; ++c) {
+            const double* t = D.ci_v + (size_t)ix[c] * 9;
+            fx += -t[0];
+            fy += -t[1];
+            fz += -t[2];
+          }
+        }
+        if (P.rolling) {
+          for (int c = 0; c < nci; ++c) {
+            fx += -mine[9 * c + 3];
+            fy += -mine[9 * c + 4];
+            fz += -mine[9 * c + 5];
+          }
+          for (int c = 0; c < nib; ++c) {
+            const double* t = D.ci_v + (size_t)ix[c] * 9;
+            fx += t[3];
+            fy += t[4];
+            fz += t[5];
+          }
+        }
         for (int c = 0; c < nci; ++c) {
-          fx += mine[9 * c];
-          fy += mine[9 * c + 1];
-          fz += mine[9 * c + 2];
+          fx += mine[9 * c + 6];
+          fy += mine[9 * c + 7];
+          fz += mine[9 * c + 8];
         }
         for (int c = 0; c < nib; ++c) {
           const double* t = D.ci_v + (size_t)ix[c] * 9;
-          fx += -t[0];
-          fy += -t[1];
-          fz += -t[2];
+          fx += -t[6];
+          fy += -t[7];
+          fz += -t[8];
         }
-      }
-      if (P.rolling) {
-        for (int c = 0; c < nci; ++c) {
-          fx += -mine[9 * c + 3];
-          fy += -mine[9 * c + 4];
-          fz += -mine[9 * c + 5];
-        }
-        for (int c = 0; c < nib; ++c) {
-          const double* t = D.ci_v + (size_t)ix[c] * 9;
-          fx += t[3];
-          fy += t[4];
-          fz += t[5];
-        }
-      }
-      for (int c = 0; c < nci; ++c) {
-        fx += mine[9 * c + 6];
-        fy += mine[9 * c + 7];
-        fz += mine[9 * c + 8];
-      }
-      for (int c = 0; c < nib; ++c) {
-        const double* t = D.ci_v + (size_t)ix[c] * 9;
-        fx += -t[6];
-        fy += -t[7];
-        fz += -t[8];
-      }
-      // spherical indenter (dem3d.py:1519-1532)
-      {
-        const double dx = px - tpx, dy = py - tpy, dz = pz - tpz;
-        const double dist = norm3(dx, dy, dz);
-        double nx = 0.0, ny = 0.0, nz = -1.0;
-        if (dist > kEps) {
-          const double dc = fmax(dist, kEps);
-          nx = dx / dc;
-          ny = dy / dc;
-          nz = dz / dc;
-        }
-        const double ov = fmax((P.radius + P.tool_radius) - dist, 0.0);
-        const double vn = ((vx - P.tool_velocity[0]) * nx + (vy - P.tool_velocity[1]) * ny) +
-                          (vz - P.tool_velocity[2]) * nz;
-        const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.contact_k * ov;
-        double mag = fmax(el - P.tool_damping * vn, 0.0);
-        if (!(ov > 0.0)) mag = 0.0;
-        const double tx = mag * nx, ty = mag * ny, tz = mag * nz;
-        acc[0] += tx;
-        acc[1] += ty;
-        acc[2] += tz;
-        fx += tx;
-        fy += ty;
-        fz += tz;
-      }
-      // plane platens (dem3d.py:1534-1580) with Coulomb friction (dem3d.py:1187-1240)
-      for (int side = 0; side < 2; ++side) {
-        if (!(P.platens & (1 << side))) continue;
-        double ov, mag;
-        if (side == 0) {
-          ov = fmax((pz + P.radius) - top_z, 0.0);
-          const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
-          mag = fmax(el + P.platen_c * (vz - P.top_velocity), 0.0);
-          if (!(ov > 0.0)) mag = 0.0;
-          fz += -mag;
-          acc[3] += mag;
-        } else {
-          ov = fmax((bottom_z + P.radius) - pz, 0.0);
-          const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
-          mag = fmax(el - P.platen_c * (vz - P.bottom_velocity), 0.0);
-          if (!(ov > 0.0)) mag = 0.0;
-          fz += mag;
-          acc[4] += -mag;
-        }
-        if (platen_friction) {
-          double* td = (side == 0 ? S.top_tangential : S.bottom_tangential) + 3 * (size_t)k;
-          const bool touch = ov > 0.0;
-          const double ux = touch ? vx : 0.0, uy = touch ? vy : 0.0;
-          const double slip = norm3(ux, uy, 0.0);
-          double tx = td[0], ty = td[1], tz = td[2];
-          if (uh) {
-            tx = tx + ux * P.dt;
-            ty = ty + uy * P.dt;
-            tz = tz + 0.0 * P.dt;
-            if (!touch) tx = ty = tz = 0.0;
-            td[0] = tx;
-            td[1] = ty;
-            td[2] = tz;
+        // spherical indenter (dem3d.py:1519-1532)
+        {
+          const double dx = px - tpx, dy = py - tpy, dz = pz - tpz;
+          const double dist = norm3(dx, dy, dz);
+          double nx = 0.0, ny = 0.0, nz = -1.0;
+          if (dist > kEps) {
+            const double dc = fmax(dist, kEps);
+            nx = dx / dc;
+            ny = dy / dc;
+            nz = dz / dc;
           }
-          const double kk = -P.platen_kt;
-          const double sx = kk * tx, sy = kk * ty, sz = kk * tz;
-          const double sm = norm3(sx, sy, sz);
-          const double lim = cone_limit(P.platen_cone, P.platen_cone_c, sm, mag, slip);
-          const double sc = sm > lim ? lim / fmax(sm, kEps) : 1.0;
-          fx += sx * sc;
-          fy += sy * sc;
-          fz += sz * sc;
+          const double ov = fmax((P.radius + P.tool_radius) - dist, 0.0);
+          const double vn = ((vx - P.tool_velocity[0]) * nx + (vy - P.tool_velocity[1]) * ny) +
+                            (vz - P.tool_velocity[2]) * nz;
+          const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.contact_k * ov;
+          double mag = fmax(el - P.tool_damping * vn, 0.0);
+          if (!(ov > 0.0)) mag = 0.0;
+          const double tx = mag * nx, ty = mag * ny, tz = mag * nz;
+          acc[0] += tx;
+          acc[1] += ty;
+          acc[2] += tz;
+          fx += tx;
+          fy += ty;
+          fz += tz;
         }
+        // plane platens (dem3d.py:1534-1580) with Coulomb friction (dem3d.py:1187-1240)
+        for (int side = 0; side < 2; ++side) {
+          if (!(P.platens & (1 << side))) continue;
+          double ov, mag;
+          if (side == 0) {
+            ov = fmax((pz + P.radius) - top_z, 0.0);
+            const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
+            mag = fmax(el + P.platen_c * (vz - P.top_velocity), 0.0);
+            if (!(ov > 0.0)) mag = 0.0;
+            fz += -mag;
+            acc[3] += mag;
+          } else {
+            ov = fmax((bottom_z + P.radius) - pz, 0.0);
+            const double el = P.hertz ? P.hertz_kn_rigid * pow(ov, 1.5) : P.platen_k * ov;
+            mag = fmax(el - P.platen_c * (vz - P.bottom_velocity), 0.0);
+            if (!(ov > 0.0)) mag = 0.0;
+            fz += mag;
+            acc[4] += -mag;
+          }
+          if (platen_friction) {
+            double* td = (side == 0 ? S.top_tangential : S.bottom_tangential) + 3 * (size_t)k;
+            const bool touch = ov > 0.0;
+            const double ux = touch ? vx : 0.0, uy = touch ? vy : 0.0;
+            const double slip = norm3(ux, uy, 0.0);
+            double tx = td[0], ty = td[1], tz = td[2];
+            if (uh) {
+              tx = tx + ux * P.dt;
+              ty = ty + uy * P.dt;
+              tz = tz + 0.0 * P.dt;
+              if (!touch) tx = ty = tz = 0.0;
+              td[0] = tx;
+              td[1] = ty;
+              td[2] = tz;
+            }
+            const double kk = -P.platen_kt;
+            const double sx = kk * tx, sy = kk * ty, sz = kk * tz;
+            const double sm = norm3(sx, sy, sz);
+            const double lim = cone_limit(P.platen_cone, P.platen_cone_c, sm, mag, slip);
+            const double sc = sm > lim ? lim / fmax(sm, kEps) : 1.0;
+            fx += sx * sc;
+            fy += sy * sc;
+            fz += sz * sc;
+          }
+        }
+        if (P.platens & 4) {
+          // lateral servo platens (dem3d.py:1582-1623)
+          const double r = P.radius;
+          double ov = fmax((lp[0] - px) + r, 0.0);
+          double mg = fmax(P.lateral_k * ov - P.lateral_c * (vx - lvx), 0.0);
+          if (!(ov > 0.0)) mg = 0.0;
+          fx += mg;
+          acc[5] += -mg;
+          ov = fmax((px + r) - lp[1], 0.0);
+          mg = fmax(P.lateral_k * ov + P.lateral_c * (vx - lvx), 0.0);
+          if (!(ov > 0.0)) mg = 0.0;
+          fx -= mg;
+          acc[6] += mg;
+          ov = fmax((lp[2] - py) + r, 0.0);
+          mg = fmax(P.lateral_k * ov - P.lateral_c * (vy - lvy), 0.0);
+          if (!(ov > 0.0)) mg = 0.0;
+          fy += mg;
+          acc[7] += -mg;
+          ov = fmax((py + r) - lp[3], 0.0);
+          mg = fmax(P.lateral_k * ov + P.lateral_c * (vy - lvy), 0.0);
+          if (!(ov > 0.0)) mg = 0.0;
+          fy -= mg;
+          acc[8] += mg;
+        }
+        if (O.mode == 1) {
+          O.force[3 * k] = fx;
+          O.force[3 * k + 1] = fy;
+          O.force[3 * k + 2] = fz;
+          continue;
+        }
+        double ax = fx / P.mass, ay = fy / P.mass, az = fz / P.mass;
+        const bool fixed = S.fixed[k] != 0;
+        if (fixed) ax = ay = az = 0.0;
+        double nvx = vx + ax * P.dt, nvy = vy + ay * P.dt, nvz = vz + az * P.dt;
+        if (fixed) nvx = nvy = nvz = 0.0;
+        double npx = px + nvx * P.dt, npy = py + nvy * P.dt, npz = pz + nvz * P.dt;
+        if (fixed) {
+          npx = S.initial_positions[3 * k];
+          npy = S.initial_positions[3 * k + 1];
+          npz = S.initial_positions[3 * k + 2];
+        }
+        vel[3 * k] = nvx;
+        vel[3 * k + 1] = nvy;
+        vel[3 * k + 2] = nvz;
+        pos[3 * k] = npx;
+        pos[3 * k + 1] = npy;
+        pos[3 * k + 2] = npz;
+        if (!(isfinite(npx) && isfinite(npy) && isfinite(npz) && isfinite(nvx) && isfinite(nvy) && isfinite(nvz)))
+          flags |= kStatusNonfinite;
+        insert_cell(D, q, k, npx, npy, npz, width, flags);  // the next step's cell table
       }
-      if (P.platens & 4) {
-        // lateral servo platens (dem3d.py:1582-1623)
-        const double r = P.radius;
-        double ov = fmax((lp[0] - px) + r, 0.0);
-        double mg = fmax(P.lateral_k * ov - P.lateral_c * (vx - lvx), 0.0);
-        if (!(ov > 0.0)) mg = 0.0;
-        fx += mg;
-        acc[5] += -mg;
-        ov = fmax((px + r) - lp[1], 0.0);
-        mg = fmax(P.lateral_k * ov + P.lateral_c * (vx - lvx), 0.0);
-        if (!(ov > 0.0)) mg = 0.0;
-        fx -= mg;
-        acc[6] += mg;
-        ov = fmax((lp[2] - py) + r, 0.0);
-        mg = fmax(P.lateral_k * ov - P.lateral_c * (vy - lvy), 0.0);
-        if (!(ov > 0.0)) mg = 0.0;
-        fy += mg;
-        acc[7] += -mg;
-        ov = fmax((py + r) - lp[3], 0.0);
-        mg = fmax(P.lateral_k * ov + P.lateral_c * (vy - lvy), 0.0);
-        if (!(ov > 0.0)) mg = 0.0;
-        fy -= mg;
-        acc[8] += mg;
-      }
-      if (O.mode == 1) {
-        O.force[3 * k] = fx;
-        O.force[3 * k + 1] = fy;
-        O.force[3 * k + 2] = fz;
-        continue;
-      }
-      double ax = fx / P.mass, ay = fy / P.mass, az = fz / P.mass;
-      const bool fixed = S.fixed[k] != 0;
-      if (fixed) ax = ay = az = 0.0;
-      double nvx = vx + ax * P.dt, nvy = vy + ay * P.dt, nvz = vz + az * P.dt;
-      if (fixed) nvx = nvy = nvz = 0.0;
-      double npx = px + nvx * P.dt, npy = py + nvy * P.dt, npz = pz + nvz * P.dt;
-      if (fixed) {
-        npx = S.initial_positions[3 * k];
-        npy = S.initial_positions[3 * k + 1];
-        npz = S.initial_positions[3 * k + 2];
-      }
-      vel[3 * k] = nvx;
-      vel[3 * k + 1] = nvy;
-      vel[3 * k + 2] = nvz;
-      pos[3 * k] = npx;
-      pos[3 * k + 1] = npy;
-      pos[3 * k + 2] = npz;
-      if (!(isfinite(npx) && isfinite(npy) && isfinite(npz) && isfinite(nvx) && isfinite(nvy) && isfinite(nvz)))
-        flags |= kStatusNonfinite;
-      insert_cell(D, q, k, npx, npy, npz, width, flags);  // the next step's cell table
+      if (friction)
+        for (int k = gt; k < n; k += gs) hist_max = max(hist_max, min(D.hist_cnt[k], kHistory));
     }
     acc[9] = acc_fp;
     acc[10] = acc_rp;
@@ -906,7 +1378,7 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
     double dv[1] = {diss_launch}, dtot[1];
     block_sum_f64<1>(dv, red, dtot);
     if (tid == 0) {
-      for (int q = 0; q < kPartials; ++q) D.part[(size_t)blockIdx.x * kPartials + q] = tot[q];
+      for (int c = 0; c < kPartials; ++c) D.part[(size_t)blockIdx.x * kPartials + c] = tot[c];
       D.pmin[2 * blockIdx.x] = mm;
       D.pmin[2 * blockIdx.x + 1] = hm;
       D.pdiss[blockIdx.x] = dtot[0];
@@ -1158,7 +1630,8 @@ int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_to
       (rc = dalloc(h, &D.hfill, 2 * (size_t)H)) || (rc = dalloc(h, &D.members, n)) || (rc = dalloc(h, &D.ci_cnt, n)) ||
       (rc = dalloc(h, &D.ci_j, (size_t)n * kContacts)) || (rc = dalloc(h, &D.ci_v, (size_t)n * kContacts * 9)) ||
       (rc = dalloc(h, &D.ib_cnt, n)) || (rc = dalloc(h, &D.ib_key, (size_t)n * kContacts)) ||
-      (rc = dalloc(h, &D.ib_idx, (size_t)n * kContacts)) ||
+      (rc = dalloc(h, &D.ib_idx, (size_t)n * kContacts)) || (rc = dalloc(h, &D.hist_old, n)) ||
+      (rc = dalloc(h, &D.cellmin, n)) ||
       (rc = dalloc(h, &D.hist_cnt, n)) || (rc = dalloc(h, &D.hist_j, (size_t)n * kHistory)) ||
       (rc = dalloc(h, &D.hist_d, (size_t)n * kHistory * 3)) || (rc = dalloc(h, &D.ledger, TDEM_L3_COUNT)) ||
       (rc = dalloc(h, &D.status, 1)))
