@@ -63,6 +63,28 @@ class OracleConfig:
         return min(elastic_dt, damping_dt, travel_dt)
 
 
+def _fma(a, b, c):
+    """Correctly rounded a*b + c (Dekker two-product, Knuth two-sum): numpy has
+    no fused multiply-add."""
+    p = a * b
+    s_ = 134217729.0
+    ca, cb = s_ * a, s_ * b
+    ah = ca - (ca - a)
+    bh = cb - (cb - b)
+    al, bl = a - ah, b - bh
+    e = ((ah * bh - p) + ah * bl + al * bh) + al * bl
+    s = p + c
+    bb = s - p
+    t = (p - (s - bb)) + (c - bb)
+    return s + (t + e)
+
+
+def vnorm2(delta: np.ndarray) -> np.ndarray:
+    """torch.linalg.vector_norm of 2-vectors on the CPU: sqrt(fma(y, y, x*x))."""
+    x, y = delta[..., 0], delta[..., 1]
+    return np.sqrt(_fma(y, y, x * x))
+
+
 def _pinv2x2_batch(m: np.ndarray) -> np.ndarray:
     """Moore-Penrose pseudo-inverse of a batch of 2x2 matrices (SVD based)."""
     return np.linalg.pinv(m)
@@ -132,7 +154,7 @@ class IceDEMOracle:
         iu, ju = np.triu_indices(n, k=1)
         self.pairs = np.stack((iu, ju), axis=1).astype(np.int64)
         delta = self.positions[ju] - self.positions[iu]
-        distances = np.sqrt((delta * delta).sum(axis=1))
+        distances = vnorm2(delta)
         self.initial_normals = delta / distances[:, None]
         self.bonded = distances <= 2 * cfg.radius * math.sqrt(2) * (1 + 1e-10)
         self.bond_indices = self.pairs[self.bonded]
@@ -205,7 +227,7 @@ class IceDEMOracle:
         eps = np.finfo(np.float64).eps
         i, j = self.pairs.T
         delta = self.positions[j] - self.positions[i]
-        distance = np.sqrt((delta * delta).sum(axis=1))
+        distance = vnorm2(delta)
         normal = delta / np.maximum(distance, eps)[:, None]
         normal = np.where((distance > 0)[:, None], normal, self.initial_normals)
         extension = distance - self.rest_lengths
@@ -242,7 +264,7 @@ class IceDEMOracle:
         np.add.at(force, j, -pair_force)
         if self.hull_profile is None:
             tool_delta = self.positions - self.tool_position
-            tool_distance = np.sqrt((tool_delta * tool_delta).sum(axis=1))
+            tool_distance = vnorm2(tool_delta)
             tool_normal = tool_delta / np.maximum(tool_distance, eps)[:, None]
             fallback = np.zeros_like(tool_normal)
             fallback[:, 1] = -1
@@ -326,7 +348,7 @@ class IceDEMOracle:
         """dem.py:603-624."""
         cfg = self.config
         delta = self.positions[self.pairs[:, 1]] - self.positions[self.pairs[:, 0]]
-        dist = np.sqrt((delta * delta).sum(axis=1))
+        dist = vnorm2(delta)
         ext = dist - self.rest_lengths
         overlap = np.maximum(2 * cfg.radius - dist, 0.0)
         if self.pair_coefficients is None:

@@ -13,7 +13,9 @@
 // reductions run in a fixed order, so reruns are bitwise identical.
 //
 // This translation unit is compiled with --fmad=false: the reference runs
-// one torch op per arithmetic step, each rounded separately.
+// one torch op per arithmetic step, each rounded separately. The one fused
+// operation is torch's CPU vector_norm, which sums the squares of a 2-vector
+// as fma(y, y, x*x); distances are computed that way, with fma() explicitly.
 
 #include <cuda_runtime.h>
 
@@ -77,7 +79,7 @@ __device__ inline double2 tool_contact(const Params& P, const Topo& T, double2 p
     const double tx = P.tool_start_x + time * P.tool_vel_x;
     const double ty = P.tool_start_y + time * P.tool_vel_y;
     const double dx = p.x - tx, dy = p.y - ty;
-    const double dist = sqrt(dx * dx + dy * dy);
+    const double dist = sqrt(fma(dy, dy, dx * dx));
     const double dcl = fmax(dist, eps);
     if (dist > 0.0) {
       normal = make_double2(dx / dcl, dy / dcl);
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
       if (!S.alive[p]) continue;
       const int i = T.bi[b], j = T.bj[b];
       const double dx = spos[j].x - spos[i].x, dy = spos[j].y - spos[i].y;
-      const double d = sqrt(dx * dx + dy * dy);
+      const double d = sqrt(fma(dy, dy, dx * dx));
       const double ext = d - T.rest[b];
       const double ts = ext / T.rest[b];
       const double bs = 0.5 * (sshear[i] + sshear[j]);
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
         const int hi = k < j ? j : k;
         const double dx = spos[hi].x - spos[lo].x;
         const double dy = spos[hi].y - spos[lo].y;
-        const double d = sqrt(dx * dx + dy * dy);
+        const double d = sqrt(fma(dy, dy, dx * dx));
         double nx, ny;
         if (d > 0.0) {
           const double dcl = fmax(d, eps);
@@ -303,7 +305,7 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
           ny = dy / dcl;
         } else {
           const double ix = gpos0[hi].x - gpos0[lo].x, iy = gpos0[hi].y - gpos0[lo].y;
-          const double id = sqrt(ix * ix + iy * iy);
+          const double id = sqrt(fma(iy, iy, ix * ix));
           nx = ix / id;
           ny = iy / id;
         }
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
           const int hi = k < j ? j : k;
           const double dx = spos[hi].x - spos[lo].x;
           const double dy = spos[hi].y - spos[lo].y;
-          const double d = sqrt(dx * dx + dy * dy);
+          const double d = sqrt(fma(dy, dy, dx * dx));
           double nx, ny;
           if (d > 0.0) {
             const double dcl = fmax(d, eps);
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(512) icedem_kernel(Params P, Topo T, tdem_iced
             ny = dy / dcl;
           } else {
             const double ix = gpos0[hi].x - gpos0[lo].x, iy = gpos0[hi].y - gpos0[lo].y;
-            const double id = sqrt(ix * ix + iy * iy);
+            const double id = sqrt(fma(iy, iy, ix * ix));
             nx = ix / id;
             ny = iy / id;
           }
@@ -654,7 +656,7 @@ int tdem_icedem_create(const tdem_icedem_config* cfg, const double* x0, tdem_ice
   for (int i = 0; i < n; ++i) {
     for (int j = i + 1; j < n; ++j, ++p) {
       const double dx = x0[2 * j] - x0[2 * i], dy = x0[2 * j + 1] - x0[2 * i + 1];
-      const double d = std::sqrt(dx * dx + dy * dy);
+      const double d = std::sqrt(std::fma(dy, dy, dx * dx));
       if (d <= thr) {
         bi.push_back(i);
         bj.push_back(j);
