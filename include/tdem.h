@@ -530,6 +530,12 @@ typedef struct {
   double wet_drag;           /* C_wet */
   double water_level;
   double cap_denominator;    /* 4 r**3, the spherical-cap volume fraction's denominator */
+  int32_t mindlin;           /* 1: Mindlin-Deresiewicz partial slip replaces the Cundall-Strack cone
+                                (mindlin_partial_slip.py:174-232), for pairs and platens */
+  int32_t pad3;
+  double mindlin_platen_8g;  /* 8 G*, rigid counterpart (platen no-slip stiffness 8 G* a) */
+  double rigid_radius;       /* R*, rigid counterpart */
+  double rigid_4e;           /* 4 E*, rigid counterpart (contact radius a = (3 F R* / (4 E*))^(1/3)) */
 } tdem_icedem3d_config;
 
 /* Constant topology, host arrays, copied at create time. */

@@ -22,8 +22,8 @@ Dekker's product and Knuth's sum.
 Pinning: checked against golden vectors produced by the reference itself
 (``tests/golden/make_golden3d.py``) in ``tests/test_oracle_icedem3d.py``.
 
-Not restated (not built on the CUDA path either): the Mindlin partial-slip
-tangential law and the calibrated Hertz restitution map.
+Not restated (not built on the CUDA path either): the calibrated Hertz
+restitution map.
 """
 
 from __future__ import annotations
@@ -52,6 +52,18 @@ def _fma(a, b, c):
     bb = s - p
     t = (p - (s - bb)) + (c - bb)
     return s + (t + e)
+
+
+def partial_slip_magnitude(delta, fn, mu, kt):
+    """Mindlin-Deresiewicz |F_t| (mindlin_partial_slip.py:155-198)."""
+    tiny = float(np.finfo(np.float64).tiny)
+    delta = np.maximum(delta, 0.0)
+    fn = np.maximum(fn, 0.0)
+    ds = ((3.0 * mu) * fn) / (2.0 * np.maximum(kt, tiny))
+    cap = mu * fn
+    ratio = np.where(ds > 0.0, delta / np.maximum(ds, tiny), 1.0)
+    ratio = np.clip(ratio, 0.0, 1.0)
+    return cap * (1.0 - np.maximum(1.0 - ratio, 0.0) ** 1.5)
 
 
 def vnorm(v):
@@ -465,16 +477,23 @@ class IceDEM3DOracle:
                           if hertz and cfg.tangential_stiffness is None else
                           np.full_like(ov, float(cfg.contact_stiffness if cfg.tangential_stiffness is None
                                                  else cfg.tangential_stiffness)))
-                    raw = kt[:, None] * td
-                    fm = vnorm(raw)
-                    lim = self._cone(fm, cmag, vnorm(vt), float(cfg.friction_coefficient))
-                    scale = np.where(fm > lim, lim / np.maximum(fm, 1e-15), 1.0)
-                    ft = raw * scale[:, None]
+                    if cfg.tangential_model == "mindlin_partial_slip":
+                        dm = vnorm(td)
+                        tiny = float(np.finfo(np.float64).tiny)
+                        fmag = partial_slip_magnitude(dm, cmag, float(cfg.friction_coefficient), kt)
+                        unit = np.where((dm > 0.0)[:, None], td / np.maximum(dm, tiny)[:, None], 0.0)
+                        ft = fmag[:, None] * unit
+                    else:
+                        raw = kt[:, None] * td
+                        fm = vnorm(raw)
+                        lim = self._cone(fm, cmag, vnorm(vt), float(cfg.friction_coefficient))
+                        scale = np.where(fm > lim, lim / np.maximum(fm, 1e-15), 1.0)
+                        ft = raw * scale[:, None]
                     fpow = float((ft * (vel[ci] - vel[cj])).sum())
                     np.add.at(force, ci, ft)
                     np.add.at(force, cj, -ft)
                     if update_history:
-                        nxt = ft / kt[:, None]
+                        nxt = td if cfg.tangential_model == "mindlin_partial_slip" else ft / kt[:, None]
                         for a, b, d in zip(ci.tolist(), cj.tolist(), nxt):
                             self.history[(a, b)] = d.copy()
                 if cfg.rolling_resistance_coefficient > 0.0:
@@ -533,13 +552,20 @@ class IceDEM3DOracle:
                         self.top_tang = tang
                     else:
                         self.bottom_tang = tang
-                k_t = float(cfg.platen_stiffness if cfg.platen_friction_stiffness is None
-                            else cfg.platen_friction_stiffness)
-                spring = (-k_t) * tang
-                sm = vnorm(spring)
-                lim = self._cone(sm, pm, vnorm(u), float(cfg.platen_friction_coefficient))
-                scale = np.where(sm > lim, lim / np.maximum(sm, EPS), 1.0)
-                force = force + spring * scale[:, None]
+                if cfg.tangential_model == "mindlin_partial_slip":
+                    g_rig = float(cfg.young_modulus / (2.0 * ((2.0 - cfg.poisson_ratio) * (1.0 + cfg.poisson_ratio))))
+                    a = np.maximum((3.0 * np.maximum(pm, 0.0)) * c.r_rig / (4.0 * c.e_rig), 0.0) ** (1.0 / 3.0)
+                    dm = vnorm(tang)
+                    fmag = partial_slip_magnitude(dm, pm, float(cfg.platen_friction_coefficient), (8.0 * g_rig) * a)
+                    force = force + (-fmag)[:, None] * (tang / np.maximum(dm, EPS)[:, None])
+                else:
+                    k_t = float(cfg.platen_stiffness if cfg.platen_friction_stiffness is None
+                                else cfg.platen_friction_stiffness)
+                    spring = (-k_t) * tang
+                    sm = vnorm(spring)
+                    lim = self._cone(sm, pm, vnorm(u), float(cfg.platen_friction_coefficient))
+                    scale = np.where(sm > lim, lim / np.maximum(sm, EPS), 1.0)
+                    force = force + spring * scale[:, None]
         self.lateral_reaction[:] = 0.0
         if cfg.lateral_platens:
             k = cfg.lateral_platen_stiffness if cfg.lateral_platen_stiffness is not None else cfg.platen_stiffness

@@ -112,6 +112,8 @@ class IceDEM3DConfigC(C.Structure):
         ("lateral_k", C.c_double), ("lateral_c", C.c_double),
         ("gravity_force", C.c_double), ("buoyancy_force", C.c_double), ("wet_drag", C.c_double),
         ("water_level", C.c_double), ("cap_denominator", C.c_double),
+        ("mindlin", C.c_int32), ("pad3", C.c_int32), ("mindlin_platen_8g", C.c_double),
+        ("rigid_radius", C.c_double), ("rigid_4e", C.c_double),
     ]
 
 

@@ -243,6 +243,47 @@ __device__ __forceinline__ void insert_cell(const Dev& D, int t, int k, double x
   D.pslot[k] = slot;
 }
 
+constexpr double kTiny = 2.2250738585072014e-308;  // smallest normal double
+
+// Mindlin-Deresiewicz partial-slip force magnitude
+// mu F_n [1 - (1 - delta / delta_s)^(3/2)], delta_s = 3 mu F_n / (2 k_t)
+// (mindlin_partial_slip.py:155-198).
+__device__ __forceinline__ double partial_slip_mag(double delta, double fn, double mu, double kt) {
+  delta = fmax(delta, 0.0);
+  fn = fmax(fn, 0.0);
+  const double ds = ((3.0 * mu) * fn) / (2.0 * fmax(kt, kTiny));
+  const double cap = mu * fn;
+  double ratio = ds > 0.0 ? delta / fmax(ds, kTiny) : 1.0;
+  ratio = fmin(fmax(ratio, 0.0), 1.0);
+  return cap * (1.0 - pow(fmax(1.0 - ratio, 0.0), 1.5));
+}
+
+// Platen Coulomb friction force for the spring offset t and normal force mag
+// (dem3d.py:1187-1240): the Cundall-Strack spring capped by the cone, or the
+// Mindlin-Deresiewicz law with k_t = 8 G* a of the rigid counterpart.
+__device__ __forceinline__ void platen_friction_force(const tdem_icedem3d_config& P, const double* t, double mag,
+                                                double slip, double* out) {
+  if (P.mindlin) {
+    const double fn = fmax(mag, 0.0);
+    const double a = pow(fmax(((3.0 * fn) * P.rigid_radius) / P.rigid_4e, 0.0), 1.0 / 3.0);
+    const double dm = norm3(t[0], t[1], t[2]);
+    const double fm = -partial_slip_mag(dm, mag, P.platen_cone_c[0], P.mindlin_platen_8g * a);
+    const double dd = fmax(dm, kEps);
+    out[0] = fm * (t[0] / dd);
+    out[1] = fm * (t[1] / dd);
+    out[2] = fm * (t[2] / dd);
+    return;
+  }
+  const double kk = -P.platen_kt;
+  const double sx = kk * t[0], sy = kk * t[1], sz = kk * t[2];
+  const double sm = norm3(sx, sy, sz);
+  const double lim = cone_limit(P.platen_cone, P.platen_cone_c, sm, mag, slip);
+  const double sc = sm > lim ? lim / fmax(sm, kEps) : 1.0;
+  out[0] = sx * sc;
+  out[1] = sy * sc;
+  out[2] = sz * sc;
+}
+
 struct Out {
   double* force;      // (n,3) or null
   int mode;           // 0: steps; 1: one evaluation
@@ -681,17 +722,38 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
                     tz = tz + vtz * P.dt;
                   }
                   const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
-                  const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
-                  const double fm = norm3(fx, fy, fz);
-                  const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
-                  const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
-                  const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
+                  double Fx, Fy, Fz;
+                  if (P.mindlin) {
+                    // Mindlin-Deresiewicz along the displacement (mindlin_partial_slip.py:201-232)
+                    const double dm = norm3(tx, ty, tz);
+                    const double fmag = partial_slip_mag(dm, mag, P.cone_c[0], kt);
+                    double ux = 0.0, uy = 0.0, uz = 0.0;
+                    if (dm > 0.0) {
+                      const double dd = fmax(dm, kTiny);
+                      ux = tx / dd;
+                      uy = ty / dd;
+                      uz = tz / dd;
+                    }
+                    Fx = fmag * ux;
+                    Fy = fmag * uy;
+                    Fz = fmag * uz;
+                  } else {
+                    const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
+                    const double fm = norm3(fx, fy, fz);
+                    const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
+                    const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
+                    Fx = fx * sc;
+                    Fy = fy * sc;
+                    Fz = fz * sc;
+                  }
                   out[0] = Fx;
                   out[1] = Fy;
                   out[2] = Fz;
                   acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
                   if (uh) {
-                    const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
+                    // the state: the displacement itself (Mindlin) or the cone projection F_t / k_t
+                    const double sx = P.mindlin ? tx : Fx / kt, sy = P.mindlin ? ty : Fy / kt,
+                                 sz = P.mindlin ? tz : Fz / kt;
                     if (h >= 0) {
                       hd[3 * h] = sx;
                       hd[3 * h + 1] = sy;
@@ -850,17 +912,38 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
                     tz = tz + vtz * P.dt;
                   }
                   const double kt = P.hertz_tangential ? P.hertz_kt * sqrt(ov) : P.tangential_k;
-                  const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
-                  const double fm = norm3(fx, fy, fz);
-                  const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
-                  const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
-                  const double Fx = fx * sc, Fy = fy * sc, Fz = fz * sc;
+                  double Fx, Fy, Fz;
+                  if (P.mindlin) {
+                    // Mindlin-Deresiewicz along the displacement (mindlin_partial_slip.py:201-232)
+                    const double dm = norm3(tx, ty, tz);
+                    const double fmag = partial_slip_mag(dm, mag, P.cone_c[0], kt);
+                    double ux = 0.0, uy = 0.0, uz = 0.0;
+                    if (dm > 0.0) {
+                      const double dd = fmax(dm, kTiny);
+                      ux = tx / dd;
+                      uy = ty / dd;
+                      uz = tz / dd;
+                    }
+                    Fx = fmag * ux;
+                    Fy = fmag * uy;
+                    Fz = fmag * uz;
+                  } else {
+                    const double fx = kt * tx, fy = kt * ty, fz = kt * tz;
+                    const double fm = norm3(fx, fy, fz);
+                    const double lim = cone_limit(P.cone, P.cone_c, fm, mag, norm3(vtx, vty, vtz));
+                    const double sc = fm > lim ? lim / fmax(fm, 1e-15) : 1.0;
+                    Fx = fx * sc;
+                    Fy = fy * sc;
+                    Fz = fz * sc;
+                  }
                   out[0] = Fx;
                   out[1] = Fy;
                   out[2] = Fz;
                   acc_fp += (Fx * (vkx - vjx) + Fy * (vky - vjy)) + Fz * (vkz - vjz);
                   if (uh) {
-                    const double sx = Fx / kt, sy = Fy / kt, sz = Fz / kt;
+                    // the state: the displacement itself (Mindlin) or the cone projection F_t / k_t
+                    const double sx = P.mindlin ? tx : Fx / kt, sy = P.mindlin ? ty : Fy / kt,
+                                 sz = P.mindlin ? tz : Fz / kt;
                     if (h >= 0) {
                       hd[3 * h] = sx;
                       hd[3 * h + 1] = sy;
@@ -1078,12 +1161,9 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
                 t[2] = t[2] + 0.0 * P.dt;
                 if (!touch) t[0] = t[1] = t[2] = 0.0;
               }
-              const double kk = -P.platen_kt;
-              const double sx = kk * t[0], sy = kk * t[1], sz = kk * t[2];
-              const double sm = norm3(sx, sy, sz);
-              const double lim = cone_limit(P.platen_cone, P.platen_cone_c, sm, mag, slip);
-              const double sc = sm > lim ? lim / fmax(sm, kEps) : 1.0;
-              f += (w == 0 ? sx : (w == 1 ? sy : sz)) * sc;
+              double fr[3];
+              platen_friction_force(P, t, mag, slip, fr);
+              f += fr[w];
             }
           }
           if ((P.platens & 4) && w < 2) {
@@ -1302,14 +1382,12 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
               td[1] = ty;
               td[2] = tz;
             }
-            const double kk = -P.platen_kt;
-            const double sx = kk * tx, sy = kk * ty, sz = kk * tz;
-            const double sm = norm3(sx, sy, sz);
-            const double lim = cone_limit(P.platen_cone, P.platen_cone_c, sm, mag, slip);
-            const double sc = sm > lim ? lim / fmax(sm, kEps) : 1.0;
-            fx += sx * sc;
-            fy += sy * sc;
-            fz += sz * sc;
+            const double tv[3] = {tx, ty, tz};
+            double fr[3];
+            platen_friction_force(P, tv, mag, slip, fr);
+            fx += fr[0];
+            fy += fr[1];
+            fz += fr[2];
           }
         }
         if (P.platens & 4) {

@@ -22,8 +22,7 @@ Differences from the reference, by design:
 * The pair friction history lives on the device (per particle, at most 64
   partners; more raises ``RuntimeError``), so it is not a Python dict. As in
   the reference, an entry is never dropped and is not part of ``state_dict``.
-* Not built: ``tangential_model="mindlin_partial_slip"`` and
-  ``contact_damping_model="restitution_calibrated"`` (both raise
+* Not built: ``contact_damping_model="restitution_calibrated"`` (raises
   ``NotImplementedError``); the diagnostic accumulators ``_rolling_torque`` and
   ``last_*_platen_friction`` are not kept.
 """
@@ -450,8 +449,6 @@ class IceDEM3D:
         self.device = torch.device(config.device)
         if not torch.cuda.is_available():
             raise ValueError("CUDA requested but unavailable")
-        if config.tangential_model != "cundall_strack":
-            raise NotImplementedError("tangential_model='mindlin_partial_slip' is not built on the CUDA path")
         if config.contact_damping_model == "restitution_calibrated":
             raise NotImplementedError("contact_damping_model='restitution_calibrated' is not built on the CUDA path")
         self.dtype = torch.float64
@@ -636,6 +633,14 @@ class IceDEM3D:
             mode, cc = cfg.cone_law(cfg.platen_friction_coefficient)
             c.platen_cone = mode
             c.platen_cone_c[:] = cc
+        if cfg.tangential_model == "mindlin_partial_slip":
+            # Mindlin-Deresiewicz partial slip (mindlin_partial_slip.py:119-232): the
+            # platen's no-slip stiffness is 8 G* a of the rigid counterpart
+            c.mindlin = 1
+            c.mindlin_platen_8g = 8.0 * hertz_reduced_shear_modulus(cfg.young_modulus, cfg.poisson_ratio,
+                                                                    rigid_counterpart=True)
+            c.rigid_radius = r_rig
+            c.rigid_4e = 4.0 * e_rig
         c.rolling = int(cfg.rolling_resistance_coefficient > 0.0)
         c.roll_mu = cfg.rolling_resistance_coefficient
         c.tool_radius, c.tool_damping = cfg.tool_radius, cfg.contact_damping

@@ -23,6 +23,8 @@ the positions, velocities and bond states one step later:
 * ``dem3d_hertz_friction``: Hertz contacts, Cundall-Strack friction with the
   tanh static/dynamic cone, rolling resistance, gravity, a bottom platen with
   friction, free edges.
+* ``dem3d_mindlin``: Hertz contacts with the Mindlin-Deresiewicz partial-slip
+  law for pairs and for a frictional bottom platen, gravity, free edges.
 * ``dem3d_cylinder``: the ``cylinder_xz`` geometry with Maxwell-Wiechert bonds,
   the creep clock, Weibull strengths, dual-cone friction, an absolute dashpot,
   buoyancy and wet drag, a descending top platen and four lateral platens
@@ -198,6 +200,11 @@ def main() -> None:
                         static_friction_coefficient=0.5, dynamic_friction_coefficient=0.3,
                         gravity=9.81)
     run_case("dem3d_hertz_friction", hertz, 1200, sorted(set([0, 1, 5, 50] + list(range(100, 1201, 100)))))
+    mindlin = DEM3DConfig(nx=6, ny=4, nz=3, contact_model="hertz", young_modulus=2.0e6, poisson_ratio=0.3,
+                          tangential_model="mindlin_partial_slip", friction_coefficient=0.4,
+                          breaking_strain=0.004, shear_breaking_strain=0.008, tool_gap=0.002, fix_x_edges=False,
+                          bottom_platen_enabled=True, platen_friction_coefficient=0.3, gravity=9.81)
+    run_case("dem3d_mindlin", mindlin, 1000, sorted(set([0, 1, 5, 50] + list(range(100, 1001, 100)))))
     cyl = DEM3DConfig(nx=7, ny=3, nz=7, geometry="cylinder_xz", bond_model="maxwell_wiechert",
                       bond_creep_exponent=2, bond_creep_time_s=0.05, bond_strength_weibull_modulus=5.0,
                       bond_strength_seed=3, lateral_platens=True, water_level=0.0, gravity=9.81,

@@ -73,9 +73,10 @@ def test_golden_one_step(m3, name):
     print(name, "one-step worst normwise errors", worst)
 
 
-def test_hertz_friction_trajectory_statistics(m3):
-    """The free-running Hertz / tanh-cone case ends in the reference's regime."""
-    g = P.load("dem3d_hertz_friction")
+@pytest.mark.parametrize("name", [c for c in P.CASES if c not in P.FREE_RUN])
+def test_free_run_statistics(m3, name):
+    """The free-running Hertz cases end in the reference's regime."""
+    g = P.load(name)
     sim = _sim(m3, g)
     sim.run(int(g["steps"]))
     want = int((g["failure_mode"] > 0).sum())
@@ -155,7 +156,8 @@ def test_validation_and_errors(m3):
     with pytest.raises(ValueError):
         m3.DEM3DConfig(device="cpu")
     with pytest.raises(NotImplementedError):
-        m3.IceDEM3D(m3.DEM3DConfig(contact_model="hertz", tangential_model="mindlin_partial_slip"))
+        m3.IceDEM3D(m3.DEM3DConfig(contact_model="hertz", contact_damping_model="restitution_calibrated",
+                                   restitution_coefficient=0.5))
     sim = m3.IceDEM3D(m3.DEM3DConfig(nx=3, ny=3, nz=2, fix_x_edges=False))
     with pytest.raises(ValueError):
         sim.step(torch.zeros(5, 3, dtype=torch.float64, device="cuda"))

@@ -164,7 +164,8 @@ def test_struct_layout_matches_c(tmp_path):
     """The ctypes mirrors of the 3-D C-ABI structs have the C sizes and offsets."""
     from tensordem_gb300 import _lib
     src = tmp_path / "layout.c"
-    fields = ("nbond", "radius", "branch_k", "cone", "cone_c", "tool_start", "water_level", "cap_denominator")
+    fields = ("nbond", "radius", "branch_k", "cone", "cone_c", "tool_start", "water_level", "cap_denominator",
+              "mindlin", "rigid_4e")
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "tdem.h"\nint main(void){\n'
                    'printf("%zu %zu %zu\\n", sizeof(tdem_icedem3d_config), sizeof(tdem_icedem3d_topology),'
                    ' sizeof(tdem_icedem3d_state));\n'
