@@ -605,6 +605,12 @@ int tdem_icedem3d_forces(tdem_icedem3d* h, const tdem_icedem3d_state* st, const 
 int tdem_icedem3d_step(tdem_icedem3d* h, const tdem_icedem3d_state* st, const double* loads,
                        int64_t n_steps, double time, void* stream);
 
+/* How threads map onto particles (results are bitwise the same either way):
+ * several lanes per particle (each owning whole sums), one thread per particle,
+ * or by size (lanes while a 16-lane group fits every particle; the default). */
+enum { TDEM_ICE3D_MAP_AUTO = 0, TDEM_ICE3D_MAP_LANES = 1, TDEM_ICE3D_MAP_PARTICLE = 2 };
+int tdem_icedem3d_set_mapping(tdem_icedem3d* h, int mapping);
+
 /* Ledger of the last call (TDEM_L3_COUNT doubles). Synchronizes `stream`. */
 int tdem_icedem3d_read_ledger(tdem_icedem3d* h, double* out_host, int count, void* stream);
 
@@ -620,6 +626,12 @@ int tdem_icedem3d_set_history(tdem_icedem3d* h, const int32_t* pairs_host, const
 int tdem_icedem3d_read_history(tdem_icedem3d* h, int32_t* pairs_host, double* disp_host, int64_t capacity,
                                int64_t* count, void* stream);
 int tdem_icedem3d_last_error(const tdem_icedem3d* h, char* buf, size_t len);
+
+/* Host-side: the damping ratio zeta whose Hertz + Tsuji dashpot delivers the
+ * requested restitution (contact_damping_model="restitution_calibrated";
+ * replaces contact_calibration.hertz_damping_ratio_for_restitution,
+ * src/tensordem/contact_calibration.py:219-248). No GPU needed. */
+int tdem_hertz_damping_ratio(double restitution, double* zeta_out);
 
 #ifdef __cplusplus
 }

@@ -22,8 +22,9 @@ Dekker's product and Knuth's sum.
 Pinning: checked against golden vectors produced by the reference itself
 (``tests/golden/make_golden3d.py``) in ``tests/test_oracle_icedem3d.py``.
 
-Not restated (not built on the CUDA path either): the calibrated Hertz
-restitution map.
+The calibrated Hertz restitution map (``restitution_calibrated``) is not
+restated here: its damping ratio is given (``zeta=``), pinned to the
+reference's own value recorded with the golden vectors.
 """
 
 from __future__ import annotations
@@ -160,7 +161,7 @@ class IceDEM3DOracle:
     """numpy restatement of ``IceDEM3D`` (dem3d.py:564-1663)."""
 
     def __init__(self, config: Oracle3DConfig, *, dt: float, pinv=None, full_rank=None,
-                 thresholds=None) -> None:
+                 thresholds=None, zeta=None) -> None:
         """``dt`` is the resolved step; ``pinv`` / ``full_rank`` (per particle) and
         the per-bond tensile ``thresholds`` (Weibull scatter) may be given to pin
         the constants the reference draws from LAPACK and from torch's RNG; the
@@ -198,6 +199,8 @@ class IceDEM3DOracle:
         if cfg.restitution_coefficient < 1.0 and cfg.contact_damping_model == "restitution":
             a = -math.log(cfg.restitution_coefficient)
             c.zeta = a / math.sqrt(math.pi ** 2 + a ** 2)
+        elif cfg.restitution_coefficient < 1.0 and cfg.contact_damping_model == "restitution_calibrated":
+            c.zeta = float(zeta)
         self.maxwell = cfg.bond_model == "maxwell_wiechert"
         if self.maxwell:
             shares = [float(f) for f in cfg.bond_delayed_elastic_fraction]
@@ -457,8 +460,10 @@ class IceDEM3DOracle:
                     else np.full_like(ov, cfg.contact_stiffness)
                 if cfg.contact_damping_model == "absolute":
                     gamma = np.full_like(ov, cfg.contact_damping)
-                elif cfg.restitution_coefficient < 1.0:
+                elif cfg.restitution_coefficient < 1.0 and hertz:
                     gamma = (2.0 * c.zeta) * np.sqrt(k_local * m_eff)
+                elif cfg.restitution_coefficient < 1.0:
+                    gamma = (2.0 * c.zeta) * np.sqrt(cfg.contact_stiffness * m_eff)
                 else:
                     gamma = np.zeros_like(ov)
                 cmag = np.maximum(k_local * ov - gamma * vn, 0.0)

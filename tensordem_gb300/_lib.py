@@ -181,6 +181,8 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_icedem3d_set_history": (i32, [vp, vp, vp, C.c_int64, vp]),
         "tdem_icedem3d_read_history": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_icedem3d_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "tdem_icedem3d_set_mapping": (i32, [vp, i32]),
+        "tdem_hertz_damping_ratio": (i32, [dbl, C.POINTER(C.c_double)]),
         "tdem_hm_create": (i32, [C.POINTER(HMConfigC), C.POINTER(vp)]),
         "tdem_hm_destroy": (None, [vp]),
         "tdem_hm_set_state": (i32, [vp, vp, vp, vp, vp, vp, vp, i32, vp]),

@@ -290,6 +290,7 @@ struct Out {
   int uf, uh;         // update_fracture, update_history
   long long n_steps;
   double time;
+  int mapping;        // 0: by size; 1: lanes per particle; 2: one thread per particle
 };
 
 constexpr int kChunk = 8;  // incidence entries whose loads are in flight together
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
   // small instances: several lanes per particle (a 16-lane group fits every
   // particle); large ones: one thread per particle, as lanes would only add
   // idle and repeated FP64 work
-  const bool wide = (long long)n * 16 <= (long long)gs;
+  const bool wide = O.mapping == 1 || (O.mapping == 0 && (long long)n * 16 <= (long long)gs);
   double* pos = S.positions;
   double* vel = S.velocities;
   double time = O.time;
@@ -1521,6 +1522,7 @@ struct tdem_icedem3d {
   tdem_icedem3d_config cfg{};
   Dev dev{};
   int max_grid = 1;  // co-resident blocks of the cooperative launch
+  int mapping = 0;   // TDEM_ICE3D_MAP_*
   std::vector<void*> allocs;
   double* ledger_host = nullptr;
   int* status_host = nullptr;
@@ -1751,7 +1753,7 @@ int tdem_icedem3d_forces(tdem_icedem3d* h, const tdem_icedem3d_state* st, const 
                          int update_fracture, int update_history, double* out_force, void* stream) {
   if (!h) return TDEM_ERR_BADARG;
   if (!out_force) return tdem::fail(&h->err, TDEM_ERR_BADARG, "out_force is required");
-  Out o{out_force, 1, update_fracture ? 1 : 0, update_history ? 1 : 0, 1, time};
+  Out o{out_force, 1, update_fracture ? 1 : 0, update_history ? 1 : 0, 1, time, h->mapping};
   return launch(h, st, loads, o, reinterpret_cast<cudaStream_t>(stream));
 }
 
@@ -1759,8 +1761,16 @@ int tdem_icedem3d_step(tdem_icedem3d* h, const tdem_icedem3d_state* st, const do
                        double time, void* stream) {
   if (!h) return TDEM_ERR_BADARG;
   if (n_steps < 1) return tdem::fail(&h->err, TDEM_ERR_BADARG, "n_steps must be >= 1");
-  Out o{nullptr, 0, 1, 1, (long long)n_steps, time};
+  Out o{nullptr, 0, 1, 1, (long long)n_steps, time, h->mapping};
   return launch(h, st, loads, o, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int tdem_icedem3d_set_mapping(tdem_icedem3d* h, int mapping) {
+  if (!h) return TDEM_ERR_BADARG;
+  if (mapping < TDEM_ICE3D_MAP_AUTO || mapping > TDEM_ICE3D_MAP_PARTICLE)
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "mapping must be TDEM_ICE3D_MAP_AUTO, _LANES or _PARTICLE");
+  h->mapping = mapping;
+  return TDEM_OK;
 }
 
 int tdem_icedem3d_read_ledger(tdem_icedem3d* h, double* out, int count, void* stream) {
@@ -1847,6 +1857,101 @@ int tdem_icedem3d_read_history(tdem_icedem3d* h, int32_t* pairs, double* disp, i
     }
   *count = m;
   if (m > capacity) return tdem::fail(&h->err, TDEM_ERR_CAPACITY, "history buffer too small");
+  return TDEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The universal restitution curve of a Hertz spring with the Tsuji dashpot and
+// its inverse (contact_calibration.py:60-248): the similarity ODE
+// u'' = -max(u^(3/2) + 2 zeta u^(1/4) u', 0), u(0) = 0, u'(0) = sqrt(4/5), is
+// integrated by classical RK4 at dimensionless step 1e-4 (at most 50 time
+// units); the exit rate comes from the cubic Hermite interpolant of the last
+// step, located by bisection; the requested restitution is inverted by a
+// secant iteration from the linear spring-dashpot mapping. Host arithmetic in
+// the reference's operation order, so the damping ratio has its bits.
+// ---------------------------------------------------------------------------
+namespace {
+
+double hertz_accel(double u, double w, double zeta) {
+  if (u <= 0.0) return 0.0;
+  const double f = u * std::sqrt(u) + ((2.0 * zeta) * std::pow(u, 0.25)) * w;
+  return f > 0.0 ? -f : 0.0;
+}
+
+double hermite_exit_rate(double u0, double w0, double u1, double w1, double dt) {
+  auto u_of = [&](double th) {
+    const double t2 = th * th, t3 = t2 * th;
+    return (((2.0 * t3 - 3.0 * t2 + 1.0) * u0 + ((t3 - 2.0 * t2 + th) * dt) * w0) + (-2.0 * t3 + 3.0 * t2) * u1) +
+           ((t3 - t2) * dt) * w1;
+  };
+  auto du_of = [&](double th) {
+    const double t2 = th * th;
+    return (((6.0 * t2 - 6.0 * th) * u0 + ((3.0 * t2 - 4.0 * th + 1.0) * dt) * w0) + (-6.0 * t2 + 6.0 * th) * u1) +
+           ((3.0 * t2 - 2.0 * th) * dt) * w1;
+  };
+  double lo = 0.0, hi = 1.0;
+  for (int it = 0; it < 60; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (u_of(mid) > 0.0) lo = mid;
+    else hi = mid;
+    if (hi - lo < 1e-14) break;
+  }
+  return du_of(0.5 * (lo + hi)) / dt;
+}
+
+double hertz_restitution(double zeta) {
+  if (zeta == 0.0) return 1.0;
+  const double dt = 1.0e-4;
+  const double w0 = std::sqrt(4.0 / 5.0);
+  double u = 0.0, w = w0;
+  bool seen = false;
+  const long n_max = (long)(50.0 / dt) + 1;
+  for (long it = 0; it < n_max; ++it) {
+    const double k1u = w, k1w = hertz_accel(u, w, zeta);
+    const double u2 = u + (0.5 * dt) * k1u, w2 = w + (0.5 * dt) * k1w;
+    const double k2u = w2, k2w = hertz_accel(u2, w2, zeta);
+    const double u3 = u + (0.5 * dt) * k2u, w3 = w + (0.5 * dt) * k2w;
+    const double k3u = w3, k3w = hertz_accel(u3, w3, zeta);
+    const double u4 = u + dt * k3u, w4 = w + dt * k3w;
+    const double k4u = w4, k4w = hertz_accel(u4, w4, zeta);
+    const double un = u + (dt * (((k1u + 2.0 * k2u) + 2.0 * k3u) + k4u)) / 6.0;
+    const double wn = w + (dt * (((k1w + 2.0 * k2w) + 2.0 * k3w) + k4w)) / 6.0;
+    if (u > 0.0) seen = true;
+    if (seen && un <= 0.0 && wn < 0.0)
+      return std::min(1.0, std::max(0.0, std::fabs(hermite_exit_rate(u, w, un, wn, dt)) / w0));
+    u = un;
+    w = wn;
+  }
+  return 0.0;
+}
+
+}  // namespace
+
+int tdem_hertz_damping_ratio(double restitution, double* zeta_out) {
+  if (!zeta_out || !(restitution > 0.0 && restitution <= 1.0)) return TDEM_ERR_BADARG;
+  if (restitution == 1.0) {
+    *zeta_out = 0.0;
+    return TDEM_OK;
+  }
+  const double pi = 3.141592653589793;
+  const double a = -std::log(restitution);
+  double z0 = a / std::sqrt(std::pow(pi, 2.0) + std::pow(a, 2.0));
+  double f0 = hertz_restitution(z0) - restitution;
+  double z1 = f0 > 0.0 ? z0 * 1.118 : z0 * (1.0 - 0.05);
+  double f1 = hertz_restitution(z1) - restitution;
+  for (int it = 0; it < 80; ++it) {
+    if (std::fabs(f1) <= 1.0e-10) break;
+    const double denom = f1 - f0;
+    if (denom == 0.0) break;
+    double z2 = z1 - (f1 * (z1 - z0)) / denom;
+    if (!(0.0 < z2 && z2 < 1.0)) z2 = z0 < z1 ? 0.5 * (z0 + z1) : 0.5 * (z1 + z0);
+    const double f2 = hertz_restitution(z2) - restitution;
+    z0 = z1;
+    f0 = f1;
+    z1 = z2;
+    f1 = f2;
+  }
+  *zeta_out = z1;
   return TDEM_OK;
 }
 

@@ -22,14 +22,14 @@ Differences from the reference, by design:
 * The pair friction history lives on the device (per particle, at most 64
   partners; more raises ``RuntimeError``), so it is not a Python dict. As in
   the reference, an entry is never dropped and is not part of ``state_dict``.
-* Not built: ``contact_damping_model="restitution_calibrated"`` (raises
-  ``NotImplementedError``); the diagnostic accumulators ``_rolling_torque`` and
-  ``last_*_platen_friction`` are not kept.
+* Not kept: the diagnostic accumulators ``_rolling_torque`` and
+  ``last_*_platen_friction``.
 """
 
 from __future__ import annotations
 
 import ctypes as C
+import functools
 import math
 from dataclasses import asdict, dataclass
 from typing import Any
@@ -394,6 +394,19 @@ class MaxwellWiechertBond:
         return float(self.equilibrium_stiffness + sum(self.branch_stiffness))
 
 
+@functools.lru_cache(maxsize=256)
+def hertz_damping_ratio_for_restitution(e_requested: float) -> float:
+    """Damping ratio whose Hertz + Tsuji dashpot delivers the restitution
+    ``e_requested`` (contact_calibration.py:219-248), from the library's host
+    routine ``tdem_hertz_damping_ratio`` (RK4 on the universal impact ODE,
+    secant inversion)."""
+    out = C.c_double()
+    rc = _lib.lib().tdem_hertz_damping_ratio(float(e_requested), C.byref(out))
+    if rc != _lib.TDEM_OK:
+        raise ValueError("restitution must be in (0, 1]")
+    return float(out.value)
+
+
 def weibull_strength_factors(n: int, modulus: float, seed: int) -> torch.Tensor:
     """Per-bond strength factors with median 1 (ice_bond_viscoelastic.py:300-323):
     ``scale * (-log(1 - U))**(1/m)``, ``scale = 1 / ln(2)**(1/m)``, U from a
@@ -449,8 +462,6 @@ class IceDEM3D:
         self.device = torch.device(config.device)
         if not torch.cuda.is_available():
             raise ValueError("CUDA requested but unavailable")
-        if config.contact_damping_model == "restitution_calibrated":
-            raise NotImplementedError("contact_damping_model='restitution_calibrated' is not built on the CUDA path")
         self.dtype = torch.float64
         self.dt = config.dt if config.dt is not None else config.recommended_dt
         if self.dt > config.recommended_dt:
@@ -618,9 +629,12 @@ class IceDEM3D:
         if cfg.contact_damping_model == "absolute":
             c.damping, c.damping_c = 2, cfg.contact_damping
         elif cfg.restitution_coefficient < 1.0:
-            ln_e = math.log(cfg.restitution_coefficient)
-            abs_ln_e = -ln_e
-            zeta = abs_ln_e / math.sqrt(math.pi ** 2 + abs_ln_e ** 2)
+            if cfg.contact_damping_model == "restitution_calibrated":
+                zeta = hertz_damping_ratio_for_restitution(cfg.restitution_coefficient)
+            else:
+                ln_e = math.log(cfg.restitution_coefficient)
+                abs_ln_e = -ln_e
+                zeta = abs_ln_e / math.sqrt(math.pi ** 2 + abs_ln_e ** 2)
             c.damping, c.damping_c = 1, 2.0 * zeta
             c.gamma_mobile = 2.0 * zeta * math.sqrt(cfg.contact_stiffness * (cfg.mass / 2.0))
             c.gamma_pinned = 2.0 * zeta * math.sqrt(cfg.contact_stiffness * cfg.mass)
@@ -872,6 +886,15 @@ class IceDEM3D:
         _lib.check(rc, self._handle.ptr, "tdem_icedem3d_step")
         if self.energy_audit is not None:
             self.energy_audit.observe(self)
+
+    def set_thread_mapping(self, mapping: str) -> None:
+        """``"auto"`` (default), ``"lanes"`` or ``"particle"``: how the kernel maps
+        threads onto particles. Results are bitwise the same; speed differs."""
+        modes = {"auto": 0, "lanes": 1, "particle": 2}
+        if mapping not in modes:
+            raise ValueError("mapping must be 'auto', 'lanes' or 'particle'")
+        rc = _lib.lib().tdem_icedem3d_set_mapping(self._handle.ptr, modes[mapping])
+        _lib.check(rc, self._handle.ptr, "tdem_icedem3d_set_mapping")
 
     def contact_pairs(self) -> torch.Tensor:
         """Overlapping pairs (i < j) found by the last force evaluation (int64, (K,2))."""

@@ -32,7 +32,7 @@ DIAG_KEYS = ("reaction_x", "reaction_y", "reaction_z", "top_platen_reaction_z_N"
 ENERGY_KEYS = ("kinetic_energy_J", "bond_elastic_energy_J", "particle_contact_energy_J",
                "tool_contact_energy_J", "platen_contact_energy_J", "released_bond_energy_J",
                "mechanical_energy_J")
-CASES = ("dem3d_box", "dem3d_hertz_friction", "dem3d_mindlin", "dem3d_cylinder", "dem3d_loads")
+CASES = ("dem3d_box", "dem3d_hertz_friction", "dem3d_mindlin", "dem3d_calibrated", "dem3d_cylinder", "dem3d_loads")
 # Cases whose arithmetic uses no transcendental library function (pow, tanh)
 # replay the whole trajectory to 1e-12 (they come out bit-identical). The
 # Hertz / tanh-cone case does not: torch's CPU pow and tanh are correctly

@@ -25,6 +25,9 @@ the positions, velocities and bond states one step later:
   friction, free edges.
 * ``dem3d_mindlin``: Hertz contacts with the Mindlin-Deresiewicz partial-slip
   law for pairs and for a frictional bottom platen, gravity, free edges.
+* ``dem3d_calibrated``: Hertz contacts with the calibrated restitution
+  dashpot (``contact_damping_model="restitution_calibrated"``, e = 0.5), the
+  reference's damping ratio recorded as ``zeta``; fixed bottom layer, friction.
 * ``dem3d_cylinder``: the ``cylinder_xz`` geometry with Maxwell-Wiechert bonds,
   the creep clock, Weibull strengths, dual-cone friction, an absolute dashpot,
   buoyancy and wet drag, a descending top platen and four lateral platens
@@ -45,6 +48,7 @@ from pathlib import Path
 import numpy as np
 import torch
 
+from tensordem.contact_calibration import hertz_damping_ratio_for_restitution  # reference package
 from tensordem.dem3d import DEM3DConfig, IceDEM3D  # reference package
 
 OUT = Path(__file__).resolve().parent
@@ -78,7 +82,8 @@ def _frame(sim: IceDEM3D, rec: dict, step: int) -> None:
     rec["frame_lateral"].append(list(diag["lateral_platen_reaction"]))
 
 
-def run_case(name: str, cfg: DEM3DConfig, steps: int, frames, *, setup=None, loads_fn=None) -> None:
+def run_case(name: str, cfg: DEM3DConfig, steps: int, frames, *, setup=None, loads_fn=None,
+             extra=None) -> None:
     torch.manual_seed(0)
     sim = IceDEM3D(cfg)
     if setup is not None:
@@ -137,6 +142,7 @@ def run_case(name: str, cfg: DEM3DConfig, steps: int, frames, *, setup=None, loa
         out["bond_breaking_strain"] = _np(sim.bond_breaking_strain)
     if loads_log:
         out["loads"] = np.stack(loads_log)
+    out.update(extra or {})
     np.savez_compressed(OUT / f"{name}.npz", **out)
     broken = int((out["failure_mode"] > 0).sum())
     print(f"{name}: n={len(sim.positions)} bonds={len(sim.pairs)} dt={sim.dt:.6g} broken={broken} "
@@ -205,6 +211,12 @@ def main() -> None:
                           breaking_strain=0.004, shear_breaking_strain=0.008, tool_gap=0.002, fix_x_edges=False,
                           bottom_platen_enabled=True, platen_friction_coefficient=0.3, gravity=9.81)
     run_case("dem3d_mindlin", mindlin, 1000, sorted(set([0, 1, 5, 50] + list(range(100, 1001, 100)))))
+    calibrated = DEM3DConfig(nx=6, ny=4, nz=3, contact_model="hertz", young_modulus=2.0e6, poisson_ratio=0.3,
+                             contact_damping_model="restitution_calibrated", restitution_coefficient=0.5,
+                             friction_coefficient=0.3, breaking_strain=0.004, shear_breaking_strain=0.008,
+                             tool_gap=0.002, fix_bottom=True)
+    run_case("dem3d_calibrated", calibrated, 1000, sorted(set([0, 1, 5, 50] + list(range(100, 1001, 100)))),
+             extra={"zeta": hertz_damping_ratio_for_restitution(0.5)})
     cyl = DEM3DConfig(nx=7, ny=3, nz=7, geometry="cylinder_xz", bond_model="maxwell_wiechert",
                       bond_creep_exponent=2, bond_creep_time_s=0.05, bond_strength_weibull_modulus=5.0,
                       bond_strength_seed=3, lateral_platens=True, water_level=0.0, gravity=9.81,

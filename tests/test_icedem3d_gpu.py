@@ -55,10 +55,12 @@ def _cuda(a):
     return torch.as_tensor(np.asarray(a), device="cuda").clone()
 
 
+@pytest.mark.parametrize("mapping", ["lanes", "particle"])
 @pytest.mark.parametrize("name", P.FREE_RUN)
-def test_golden_trajectory(m3, name):
+def test_golden_trajectory(m3, name, mapping):
     g = P.load(name)
     sim = _sim(m3, g)
+    sim.set_thread_mapping(mapping)
     assert sim.dt == float(g["dt"])
     assert np.array_equal(_np(sim.pairs), g["pairs"])
     assert np.array_equal(_np(sim.initial_positions), g["initial_positions"])
@@ -66,10 +68,13 @@ def test_golden_trajectory(m3, name):
     print(name, "worst normwise errors", worst, "broken", sim.broken_bonds)
 
 
+@pytest.mark.parametrize("mapping", ["lanes", "particle"])
 @pytest.mark.parametrize("name", P.CASES)
-def test_golden_one_step(m3, name):
+def test_golden_one_step(m3, name, mapping):
     g = P.load(name)
-    worst = P.replay_one_step(g, _Loaded(_sim(m3, g)), to_np=_np, to_device=_cuda)
+    sim = _sim(m3, g)
+    sim.set_thread_mapping(mapping)
+    worst = P.replay_one_step(g, _Loaded(sim), to_np=_np, to_device=_cuda)
     print(name, "one-step worst normwise errors", worst)
 
 
@@ -155,9 +160,8 @@ def test_validation_and_errors(m3):
         m3.IceDEM3D(m3.DEM3DConfig(dt=1.0))
     with pytest.raises(ValueError):
         m3.DEM3DConfig(device="cpu")
-    with pytest.raises(NotImplementedError):
-        m3.IceDEM3D(m3.DEM3DConfig(contact_model="hertz", contact_damping_model="restitution_calibrated",
-                                   restitution_coefficient=0.5))
+    with pytest.raises(ValueError):
+        m3.DEM3DConfig(contact_damping_model="restitution_calibrated", restitution_coefficient=0.5)  # linear
     sim = m3.IceDEM3D(m3.DEM3DConfig(nx=3, ny=3, nz=2, fix_x_edges=False))
     with pytest.raises(ValueError):
         sim.step(torch.zeros(5, 3, dtype=torch.float64, device="cuda"))
@@ -188,3 +192,29 @@ def test_cli_restart_workflow(m3, tmp_path):
     assert len(rows) == 1 + 5  # header, steps 0..2, then 3..4 appended
     traj = torch.load(out / "trajectory_3d.pt", map_location="cpu", weights_only=False)
     assert traj["dimension"] == 3 and traj["positions"].shape[1:] == (18, 3)
+
+
+def test_contact_capacity_overflow_raises(m3):
+    """40 particles squeezed into one spot: more than 32 overlapping partners
+    per particle is reported as an error, not written past the lists."""
+    sim = m3.IceDEM3D(m3.DEM3DConfig(nx=5, ny=4, nz=2, fix_x_edges=False))
+    gen = torch.Generator(device="cpu").manual_seed(3)
+    sim.positions = ((torch.rand(40, 3, generator=gen, dtype=torch.float64) - 0.5) * 0.002).to("cuda")
+    with pytest.raises(RuntimeError):
+        sim.forces(update_fracture=False, update_history=False)
+
+
+def test_bench_sizes_agree_across_mappings(m3):
+    """A specimen above the size where the mapping switches: the per-particle
+    and the lane mappings step to identical states."""
+    cfg = m3.DEM3DConfig(nx=40, ny=20, nz=10, breaking_strain=0.004, shear_breaking_strain=0.008,
+                         friction_coefficient=0.3, restitution_coefficient=0.7)
+    a, b = m3.IceDEM3D(cfg), m3.IceDEM3D(cfg)
+    a.set_thread_mapping("particle")
+    b.set_thread_mapping("lanes")
+    a.run(1300)
+    b.run(1300)
+    assert a.broken_bonds > 0
+    for name in ("positions", "velocities", "alive", "failure_energy_J"):
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
+    assert a.friction_history() == b.friction_history()

@@ -37,7 +37,8 @@ def _oracle(g):
     cov.index_add_(0, j, rr)
     o = IceDEM3DOracle(Oracle3DConfig(**cfg), dt=float(g["dt"]), pinv=torch.linalg.pinv(cov).numpy(),
                        full_rank=(torch.linalg.matrix_rank(cov) >= 3).numpy(),
-                       thresholds=g.get("bond_breaking_strain"))
+                       thresholds=g.get("bond_breaking_strain"),
+                       zeta=float(g["zeta"]) if "zeta" in g else None)
     o.lateral_velocity = np.asarray(g["lateral_velocity"], dtype=np.float64)
     return o
 
@@ -178,3 +179,14 @@ def test_struct_layout_matches_c(tmp_path):
     assert sizes == [ctypes.sizeof(_lib.IceDEM3DConfigC), ctypes.sizeof(_lib.IceDEM3DTopologyC),
                      ctypes.sizeof(_lib.IceDEM3DStateC)]
     assert [int(v) for v in out[3:]] == [getattr(_lib.IceDEM3DConfigC, f).offset for f in fields]
+
+
+def test_calibrated_damping_ratio_is_the_references():
+    """The library's host restatement of the Hertz restitution calibration
+    returns the reference's damping ratio bit for bit (contact_calibration.py:219-248)."""
+    from tensordem_gb300.dem3d import hertz_damping_ratio_for_restitution
+    g = P.load("dem3d_calibrated")
+    assert hertz_damping_ratio_for_restitution(0.5) == float(g["zeta"])
+    assert hertz_damping_ratio_for_restitution(1.0) == 0.0
+    # the calibrated dashpot is stiffer than the linear mapping's (e = 0.5 -> zeta 0.2154)
+    assert 0.27 < hertz_damping_ratio_for_restitution(0.5) < 0.30
