@@ -592,70 +592,80 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
     const int* hcnt_p = D.hcnt + p * H;
     double acc_fp = 0.0, acc_rp = 0.0, acc_en = 0.0, acc_nc = 0.0;
     if (wide) {
-      // ---- C1: contact candidates (dem3d.py:825-856, 1374-1381). Each particle
-      // lists its overlapping partners with higher ids in the reference's
-      // pair-list order: neighbour cells in offset order, members ascending.
-      for (int k = gt; k < n; k += gs) {
-        int nci = 0;
-        const int sk = D.pslot[k];
-        if (friction) D.hist_old[k] = min(D.hist_cnt[k], kHistory);
-        if (sk >= 0) {
-          const unsigned long long kk = D.pkey[k];
-          const long long cx = (long long)(kk >> 42) - kCoordHalf;
-          const long long cy = (long long)((kk >> 21) & ((1ull << 21) - 1)) - kCoordHalf;
-          const long long cz = (long long)(kk & ((1ull << 21) - 1)) - kCoordHalf;
-          const double pkx = pos[3 * k], pky = pos[3 * k + 1], pkz = pos[3 * k + 2];
-          // the first particle of this particle's cell orders its pairs in the partners' inboxes
-          int own_min = k;
-          {
-            const int m0 = D.hstart[sk], m1 = m0 + hcnt_p[sk];
-            for (int m = m0; m < m1; ++m) own_min = min(own_min, D.members[m]);
+      // ---- C1: contact candidates (dem3d.py:825-856, 1374-1381). A warp per
+      // particle, lane o < 27 owning neighbour cell o in the reference's offset
+      // order (dx, then dy, then dz); each lane finds its cell's overlapping
+      // members with higher ids, ascending, and an exclusive prefix over the
+      // lanes lays them out in the reference's pair-list order.
+      {
+        const int lane = threadIdx.x & 31;
+        const int o = lane < 27 ? lane : 13;  // lanes 27..31 idle (13 is the own cell)
+        const int dx = o / 9 - 1, dy = (o / 3) % 3 - 1, dz = o % 3 - 1;
+        for (int k = gt >> 5; k < n; k += gs >> 5) {  // warp-uniform
+          const int sk = D.pslot[k];
+          if (lane == 0 && friction) D.hist_old[k] = min(D.hist_cnt[k], kHistory);
+          int sl = -1, cnt = 0, st = 0;
+          double pkx = 0.0, pky = 0.0, pkz = 0.0;
+          if (sk >= 0) {
+            const unsigned long long kk = D.pkey[k];
+            const long long cx = (long long)(kk >> 42) - kCoordHalf;
+            const long long cy = (long long)((kk >> 21) & ((1ull << 21) - 1)) - kCoordHalf;
+            const long long cz = (long long)(kk & ((1ull << 21) - 1)) - kCoordHalf;
+            pkx = pos[3 * k];
+            pky = pos[3 * k + 1];
+            pkz = pos[3 * k + 2];
+            if (lane < 27) {
+              sl = find_cell(hkey_p, D.hmask, pack_cell(cx + dx, cy + dy, cz + dz));
+              if (sl >= 0) {
+                cnt = hcnt_p[sl];
+                st = D.hstart[sl];
+              }
+            }
           }
-          D.cellmin[k] = own_min;
-          for (int dx = -1; dx <= 1; ++dx) {
-            // the nine cells of this dx: lookups, then counts and starts, in flight together
-            int sl[9], cnt[9], st[9];
-            unsigned long long ck[9], first[9];
-            unsigned hs[9];
-  #pragma unroll
-            for (int o = 0; o < 9; ++o) {
-              ck[o] = pack_cell(cx + dx, cy + o / 3 - 1, cz + o % 3 - 1);
-              hs[o] = hash_slot(ck[o], D.hmask);
-              first[o] = hkey_p[hs[o]];
+          // own cell's first particle (the inbox order key of this particle's pairs)
+          if (lane == 13 && sk >= 0) {
+            int own_min = k;
+            for (int m = st; m < st + cnt; ++m) own_min = min(own_min, D.members[m]);
+            D.cellmin[k] = own_min;
+          }
+          // pass 1: count, pass 2: write at the prefix offset
+          int near = 0;
+          for (int pass = 0; pass < 2; ++pass) {
+            int base = 0;
+            if (pass == 1) {
+              int incl = near;
+#pragma unroll
+              for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += y;
+              }
+              base = incl - near;
+              const int total = __shfl_sync(0xffffffffu, incl, 31);
+              if (lane == 0) D.ci_cnt[k] = min(total, kContacts);
+              if (total > kContacts && lane == 0) flags |= kStatusContacts;
+              if (near == 0) continue;
             }
-  #pragma unroll
-            for (int o = 0; o < 9; ++o)  // a collision probes on (rare)
-              sl[o] = first[o] == ck[o] ? (int)hs[o] : (first[o] == kEmpty ? -1 : find_cell(hkey_p, D.hmask, ck[o]));
-  #pragma unroll
-            for (int o = 0; o < 9; ++o) {
-              cnt[o] = sl[o] >= 0 ? hcnt_p[sl[o]] : 0;
-              st[o] = sl[o] >= 0 ? D.hstart[sl[o]] : 0;
-            }
-            for (int o = 0; o < 9; ++o) {
-              // members of the cell ascending: repeated selection (cells hold a few)
-              int last = -1;
-              for (int t = 0; t < cnt[o]; ++t) {
-                int j = INT_MAX;
-                for (int m = st[o]; m < st[o] + cnt[o]; ++m) {
-                  const int x = D.members[m];
-                  if (x > last && x < j) j = x;
-                }
-                last = j;
-                if (j <= k) continue;
-                const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
-                const double ov = fmax(two_r - norm3(ex, ey, ez), 0.0);
-                if (!(ov > 0.0)) continue;
-                if (nci == kContacts) {
-                  flags |= kStatusContacts;
-                  continue;
-                }
-                D.ci_j[(size_t)k * kContacts + nci] = j;
-                ++nci;
+            int w = 0, last = -1;
+            for (int t = 0; t < cnt; ++t) {
+              int j = INT_MAX;
+              for (int m = st; m < st + cnt; ++m) {
+                const int x = D.members[m];
+                if (x > last && x < j) j = x;
+              }
+              last = j;
+              if (j <= k) continue;
+              const double ex = pos[3 * j] - pkx, ey = pos[3 * j + 1] - pky, ez = pos[3 * j + 2] - pkz;
+              const double ov = fmax(two_r - norm3(ex, ey, ez), 0.0);
+              if (!(ov > 0.0)) continue;
+              if (pass == 0) {
+                ++near;
+              } else {
+                if (base + w < kContacts) D.ci_j[(size_t)k * kContacts + base + w] = j;
+                ++w;
               }
             }
           }
         }
-        D.ci_cnt[k] = nci;
       }
       TDEM_GRID_SYNC();
       // ---- C2: one thread per overlapping pair (dem3d.py:1382-1514): normal
@@ -1097,16 +1107,38 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
             ik[b + 1] = key;
             ix[b + 1] = idx;
           }
+          // contact terms, in order; each chunk's loads are in flight together
+          auto own_sum = [&](int off, bool neg) {
+            for (int c0 = 0; c0 < nci; c0 += kChunk) {
+              double val[kChunk];
+#pragma unroll
+              for (int c = 0; c < kChunk; ++c) val[c] = c0 + c < nci ? mine[9 * (c0 + c) + off + w] : 0.0;
+#pragma unroll
+              for (int c = 0; c < kChunk; ++c)
+                if (c0 + c < nci) f += neg ? -val[c] : val[c];
+            }
+          };
+          auto inbox_sum = [&](int off, bool neg) {
+            for (int c0 = 0; c0 < nib; c0 += kChunk) {
+              double val[kChunk];
+#pragma unroll
+              for (int c = 0; c < kChunk; ++c)
+                val[c] = c0 + c < nib ? D.ci_v[(size_t)ix[c0 + c] * 9 + off + w] : 0.0;
+#pragma unroll
+              for (int c = 0; c < kChunk; ++c)
+                if (c0 + c < nib) f += neg ? -val[c] : val[c];
+            }
+          };
           if (friction) {
-            for (int c = 0; c < nci; ++c) f += mine[9 * c + w];
-            for (int c = 0; c < nib; ++c) f += -D.ci_v[(size_t)ix[c] * 9 + w];
+            own_sum(0, false);
+            inbox_sum(0, true);
           }
           if (P.rolling) {
-            for (int c = 0; c < nci; ++c) f += -mine[9 * c + 3 + w];
-            for (int c = 0; c < nib; ++c) f += D.ci_v[(size_t)ix[c] * 9 + 3 + w];
+            own_sum(3, true);
+            inbox_sum(3, false);
           }
-          for (int c = 0; c < nci; ++c) f += mine[9 * c + 6 + w];
-          for (int c = 0; c < nib; ++c) f += -D.ci_v[(size_t)ix[c] * 9 + 6 + w];
+          own_sum(6, false);
+          inbox_sum(6, true);
           // spherical indenter (dem3d.py:1519-1532)
           {
             const double dx = px - tpx, dy = py - tpy, dz = pz - tpz;
