@@ -1482,23 +1482,33 @@ __global__ void __launch_bounds__(kBlock, 1) icedem3d_kernel(tdem_icedem3d_confi
     acc[11] = acc_en;
     acc[12] = acc_nc;
     if (flags) atomicOr(&D.gflags[step & 1], flags);
-    double tot[kPartials];
-    block_sum_f64<kPartials>(acc, red, tot);
-    const double mm = block_min_f64(min_margin, red);
-    const double hm = -block_min_f64(-(double)hist_max, red);
-    double dv[1] = {diss_launch}, dtot[1];
-    block_sum_f64<1>(dv, red, dtot);
-    if (tid == 0) {
-      for (int c = 0; c < kPartials; ++c) D.part[(size_t)blockIdx.x * kPartials + c] = tot[c];
-      D.pmin[2 * blockIdx.x] = mm;
-      D.pmin[2 * blockIdx.x + 1] = hm;
-      D.pdiss[blockIdx.x] = dtot[0];
-    }
+    // per-block ledger partials: only the launch's last evaluation is reported
+    // (margins, history sizes and dissipation accumulate per thread meanwhile)
+    auto write_partials = [&]() {
+      double tot[kPartials];
+      block_sum_f64<kPartials>(acc, red, tot);
+      const double mm = block_min_f64(min_margin, red);
+      const double hm = -block_min_f64(-(double)hist_max, red);
+      double dv[1] = {diss_launch}, dtot[1];
+      block_sum_f64<1>(dv, red, dtot);
+      if (tid == 0) {
+        for (int c = 0; c < kPartials; ++c) D.part[(size_t)blockIdx.x * kPartials + c] = tot[c];
+        D.pmin[2 * blockIdx.x] = mm;
+        D.pmin[2 * blockIdx.x + 1] = hm;
+        D.pdiss[blockIdx.x] = dtot[0];
+      }
+    };
+    const bool final_step = O.mode == 1 || step + 1 == total;
+    if (final_step) write_partials();
     TDEM_GRID_SYNC();
     // every block takes the same exit decision: this parity's flags are final
     // after the barrier and are cleared only two steps later
     const int f = *reinterpret_cast<volatile int*>(&D.gflags[step & 1]);
-    const bool last = O.mode == 1 || f != 0 || step + 1 == total;
+    const bool last = final_step || f != 0;
+    if (last && !final_step) {  // an early exit on a status: its partials too
+      write_partials();
+      TDEM_GRID_SYNC();
+    }
     if (O.mode != 1) {
       if (blockIdx.x == 0 && (P.platens & 4) && tid < 4)
         S.lateral_position[tid] = lp[tid] + S.lateral_velocity[tid] * P.dt;

@@ -173,6 +173,13 @@ def test_validation_and_errors(m3):
     with pytest.raises(FloatingPointError):
         sim.step()
     assert sim.step_count == 1
+    # a multi-step launch stops after the offending step, as step() does
+    other = m3.IceDEM3D(m3.DEM3DConfig(nx=3, ny=3, nz=2, fix_x_edges=False))
+    other.run(3)
+    other.velocities[0, 0] = math.inf
+    with pytest.raises(FloatingPointError):
+        other.run(10)
+    assert other.step_count == 4
 
 
 def test_cli_restart_workflow(m3, tmp_path):
