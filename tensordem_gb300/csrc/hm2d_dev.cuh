@@ -593,15 +593,22 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
   unsigned nmask = 0u;
   Acc<T> fx, fy, tq;
   if (FEAT && P.BMAX > 0) {
+    // the count and every slot word in one round of loads (slots past the
+    // count are allocated, their words unused)
+    unsigned wds[kMaxBondSlots];
+#pragma unroll
+    for (int u = 0; u < kMaxBondSlots; ++u)
+      if (u < P.BMAX) wds[u] = B.bpart[lp][(size_t)u * n + i];
     const int bc = B.bcnt[lp][i];
     if (bc > 0) {
       const T si = B.strain[i];
-      constexpr int KB = 2;  // bond slots whose loads are in flight together
-      for (int s0 = 0; s0 < bc; s0 += KB) {
+      constexpr int KB = 2;  // bond slots whose partner loads are in flight together
+#pragma unroll
+      for (int s0 = 0; s0 < kMaxBondSlots; s0 += KB) {
+        if (s0 >= bc) break;
         BondIn<T> in[KB];
 #pragma unroll
-        for (int u = 0; u < KB; ++u)
-          if (s0 + u < bc) in[u].w = B.bpart[lp][(size_t)(s0 + u) * n + i];
+        for (int u = 0; u < KB; ++u) in[u].w = wds[s0 + u];
 #pragma unroll
         for (int u = 0; u < KB; ++u) {
           if (s0 + u < bc) {
