@@ -307,6 +307,10 @@ class HM2DOracle:
     def contact_exclusions(self):
         return None
 
+    def energy_exclusions(self):
+        """Pair keys without contact energy in the committed state."""
+        return None
+
     def extra_forces(self, pos, vel, omega, force, torque, diss, *, advance):
         return force, torque, diss
 
@@ -345,6 +349,11 @@ class HM2DOracle:
         dist = np.sqrt((d * d).sum(axis=1))
         delta = self.radius[i] + self.radius[j] - dist
         act = delta > 0
+        # the pairs evaluate() gives no contact force hold no contact energy
+        excl = self.energy_exclusions()
+        if excl is not None and len(excl):
+            act &= ~np.isin(i * self.n + j, excl)
+        act &= (self.inv_mass[i] + self.inv_mass[j]) > 0
         if act.any():
             ia, ja, da = i[act], j[act], delta[act]
             reff = self.radius[ia] * self.radius[ja] / (self.radius[ia] + self.radius[ja])
@@ -436,6 +445,10 @@ class BondedHM2DOracle(HM2DOracle):
         # bonds intact after this evaluation's break test (dem.py:251 precedes
         # the pair forces: a bond broken now already acts as a contact)
         return (self.bi * self.n + self.bj)[self._alive_now]
+
+    def energy_exclusions(self):
+        # bonds intact in the committed state (no peeked break test)
+        return (self.bi * self.n + self.bj)[self.alive]
 
     def before_contacts(self, pos, *, advance):
         """Break test at this evaluation's positions (dem.py:243-277)."""

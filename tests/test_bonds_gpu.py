@@ -4,7 +4,8 @@ against the FP64 bonded oracle (oracle/hm2d.py, BondedHM2DOracle).
 Tolerances: FP64 engine - break set, modes and failure evaluations identical,
 state within 1e-9 normwise over 200 steps of cracking; FP32 engine - peak
 indenter load within 1% of the oracle's, ledger within 2% of the work input,
-break count within 10%.
+break count within 10%; before the first break, ledger residual within 3e-6 of
+the work input.
 """
 
 import math
@@ -94,6 +95,9 @@ def test_fp64_bonded_sheet_matches_oracle(hm):
                      ("fracture_released", "fracture_released"), ("dissipated", "dissipated")):
         assert abs(led[k_g] - ref[k_o]) <= 1e-6 * scale, k_g
     assert abs(led["tool_work"] - o.tool_work) <= 1e-6 * scale
+    # the engine's normal elastic energy includes the indenter contact
+    assert abs(led["elastic_normal"] - ref["elastic_normal"] - ref["tool_elastic"]) <= 1e-6 * scale
+    assert abs(led["total"] - ref["total"]) <= 1e-6 * scale
     load = e.load_curve()
     assert load.shape[0] == o.evals - 1
 
@@ -115,6 +119,36 @@ def test_fp32_bonded_sheet_peak_load_within_one_percent(hm):
     assert abs(led["total"] - ref["total"]) <= 0.02 * o.tool_work
     nb_g, nb_o = led["broken"], int((~o.alive).sum())
     assert abs(nb_g - nb_o) <= max(5, 0.1 * nb_o)
+
+
+def test_fp32_ledger_residual_before_the_first_break(hm):
+    """The FP32 engine's ledger residual (energies + dissipated + fracture -
+    tool work) against the FP64 oracle's, before any bond breaks: within 3e-6
+    of the work input at every checkpoint (measured 4e-9 to 1.9e-6, under
+    1e-6 once the work input passes ~2 kJ). FP32 positions resolve ~1e-8 m
+    against indenter overlaps of ~1e-3 m, so the FP32 tool work itself
+    differs by ~3e-6. The FP64 engine's residual equals the oracle's to 1e-12
+    of the work input."""
+    for speed, stops in ((5.0, (100, 200, 300, 400)), (20.0, (60, 100, 130))):
+        cfg64, st, bonds, strength = small_sheet(24, 8, precision=64, steps=600, speed=speed)
+        o = bonded_oracle_for(cfg64, st, bonds, strength)
+        engines = {}
+        for prec in (32, 64):
+            cfg, st_p, b_p, s_p = small_sheet(24, 8, precision=prec, steps=600, speed=speed)
+            engines[prec] = _engine(hm, cfg, st_p, b_p, s_p)
+        done = 0
+        for stop in stops:
+            o.step(stop - done)
+            for e in engines.values():
+                e.step(stop - done)
+            done = stop
+            assert (~o.alive).sum() == 0, "the window must end before the first break"
+            ref, work = o.energies()["total"], o.tool_work
+            r32 = (engines[32].ledger()["total"] - ref) / work
+            r64 = (engines[64].ledger()["total"] - ref) / work
+            print(f"speed {speed} step {stop}: work {work:.1f} J, residual fp32 {r32:.2e}, fp64 {r64:.2e}")
+            assert abs(r64) <= 1e-12, (speed, stop, r64)
+            assert abs(r32) <= 3e-6, (speed, stop, r32)
 
 
 def test_bonded_variants_bit_identical(hm):
