@@ -187,8 +187,8 @@ def _cmd_scale(args: argparse.Namespace) -> None:
                 times.append(e0.elapsed_time(e1) * 1e3)
             times.sort()
             med = times[len(times) // 2]
-            rows.append({"discs": cfg.n, "variant": v, "us_median": med, "us_min": times[0],
-                         "alg_GBs": cfg.n * 80 / (med * 1e-6) / 1e9})
+            rows.append({"discs": cfg.n, "variant": v, "us_median": med, "us_mean": sum(times) / len(times),
+                         "us_min": times[0], "alg_GBs": cfg.n * 80 / (med * 1e-6) / 1e9})
             print(json.dumps(rows[-1]), flush=True)
         del eng
 
