@@ -69,6 +69,60 @@ def test_candidate_pairs_match_brute_force(hm, precision):
     assert len(want) > cfg.n
 
 
+def _edge_configurations():
+    """2-D counterparts of the reference's neighbour-search configurations
+    (tests/test_dem_vectorized_verification.py:94-121): one disc, a touching
+    pair, a pair just outside the reach, an overlapping lattice, a dilute and a
+    clustered random set, a collinear chain. Equal radii r = 1 mm in a 30 mm
+    box; the clustered set is wider than the 3-D original (sigma 4 mm) so no
+    disc has more than the engine's 24 candidate slots."""
+    r, c = 1e-3, 15e-3
+    rng = np.random.default_rng(0)
+    g = np.arange(6, dtype=np.float64)
+    yy, xx = np.meshgrid(g, g, indexing="ij")
+    return {
+        "single": np.array([[c, c]]),
+        "pair_touching": np.array([[c - r, c], [c + r, c]]),
+        "pair_just_outside": np.array([[c - 1.02 * r, c], [c + 1.02 * r, c]]),
+        "dense_lattice_overlapping": np.stack([xx.ravel(), yy.ravel()], 1) * (2 * r * 0.99) + 8e-3,
+        "random_dilute": rng.uniform(2e-3, 28e-3, (40, 2)),
+        "random_clustered": np.clip(c + rng.normal(0.0, 4e-3, (60, 2)), 1.5e-3, 28.5e-3),
+        "collinear_chain": np.stack([3e-3 + np.arange(12) * 1.9 * r, np.full(12, c)], 1),
+    }
+
+
+def _positions_case(pos, r=1e-3, box=30e-3, skin=0.02e-3):
+    from tensordem_gb300.hm2d import HM2DConfig, grid_for_box, rayleigh_dt
+    n = len(pos)
+    ncell, cell = grid_for_box(box, r, skin)
+    radius = np.full(n, r)
+    mass = 2500.0 * math.pi * radius**2 * (2 * radius)
+    cfg = HM2DConfig(n=n, ncx=ncell, ncy=ncell, cell=cell, skin=skin, dt=0.2 * rayleigh_dt(r, 2500.0, 70e9, 0.25),
+                     young=70e9, poisson=0.25, restitution=0.8, mu=0.5, mu_wall=0.5, precision=64,
+                     max_neighbors=24)
+    st = dict(pos=np.ascontiguousarray(pos, dtype=np.float64), vel=np.zeros((n, 2)), omega=np.zeros(n),
+              radius=radius, mass=mass, inertia=0.5 * mass * radius**2)
+    return cfg, st
+
+
+@pytest.mark.parametrize("name", list(_edge_configurations()))
+def test_cell_list_edge_configurations_match_brute_force(hm, name):
+    pos = _edge_configurations()[name]
+    cfg, st = _positions_case(pos)
+    e = _engine(hm, cfg, st)
+    got = {tuple(p) for p in e.pairs().tolist()}
+    bi, bj = brute_force_pairs(st["pos"], 0.0, st["radius"], skin=cfg.skin)
+    want = set(zip(bi.tolist(), bj.tolist()))
+    assert got == want, (name, sorted(got ^ want)[:10])
+    expected_count = {"single": 0, "pair_touching": 1, "pair_just_outside": 0, "dense_lattice_overlapping": 60,
+                      "collinear_chain": 11}
+    if name in expected_count:
+        assert len(want) == expected_count[name]
+    # the engine steps these states without error
+    e.step(5)
+    assert e.ledger()["status"] == 0
+
+
 def test_fp64_single_evaluation_matches_oracle(hm):
     cfg, st = dense_gas(24, seed=4, precision=64)
     # push a few pairs into contact at t = 0
