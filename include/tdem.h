@@ -453,8 +453,9 @@ int tdem_batch_read_bonds(tdem_batch* h, int32_t id, int32_t* pairs, int32_t* st
 /* Batch counters (TDEM_BATCH_I_COUNT int64). Synchronizes `stream`. */
 int tdem_batch_info(tdem_batch* h, int64_t* out, int32_t count, void* stream);
 
-/* Step-kernel variants (block shape, CTAs per SM) and the autotuner that
- * times `steps` real steps of each and keeps the fastest. */
+/* Step-kernel variants (block shape, CTAs per SM, tiles per grab of the
+ * work counter) and the autotuner that times `steps` real steps of each and
+ * keeps the fastest. */
 int tdem_batch_num_variants(void);
 int tdem_batch_set_variant(tdem_batch* h, int variant);
 int tdem_batch_get_variant(const tdem_batch* h);

@@ -137,8 +137,9 @@ __device__ __forceinline__ T warp_sum(T x) {
 
 // PART 0: every tile (read-back); 1: the granular instances' tiles, granular
 // code, no step bookkeeping; 2: the other tiles, full code, and the step
-// bookkeeping (it runs after part 1 in the same stream).
-template <class T, int MODE, int BLOCK, int MINB, int PART>
+// bookkeeping (it runs after part 1 in the same stream). CHUNK: tiles per
+// grab from the step kernel's work counter.
+template <class T, int MODE, int BLOCK, int MINB, int PART, int CHUNK = 8>
 __global__ void __launch_bounds__(BLOCK, MINB)
     batch_kernel(Bufs<T> B, cudaGraphConditionalHandle h_rebuild, cudaGraphConditionalHandle h_loop,
                  int use_cond, int rebuild_every) {
@@ -168,20 +169,21 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   const V4<T>* __restrict__ pos = B.pos[sp];
   const V4<T>* __restrict__ vel = B.vel[sp];
   const uint4* __restrict__ head = B.head[lp];
-  // Tiles are handed out in chunks of kChunk consecutive tiles (step kernel:
+  // Tiles are handed out in chunks of CHUNK consecutive tiles (step kernel:
   // from an atomic counter, so fast and slow tiles balance; read-back: one
   // static chunk per warp). Consecutive tiles mostly belong to one instance,
   // so its parameters are copied once and its ticket is taken once per
   // (chunk, instance) segment. Rows stay per tile: the instance sums do not
-  // depend on which warp took which tile.
-  constexpr int kChunk = 8;
-  const int per = (MODE == kBatch) ? kChunk : (ntiles + nwarps - 1) / nwarps;
+  // depend on which warp took which tile. A warp holds two chunks at a time
+  // (the one it works on and the next), so small batches balance only with
+  // short chunks; large ones take long chunks, which keeps the atomics few.
+  const int per = (MODE == kBatch) ? CHUNK : (ntiles + nwarps - 1) / nwarps;
   const int gw = blockIdx.x * NW + wib;
   int grabs = 0;
   auto grab = [&]() -> int {
     if (MODE == kPeek) return (grabs++ == 0) ? (int)min((long long)gw * per, (long long)ntiles) : ntiles;
     int b = 0;
-    if (lane == 0) b = tbeg + atomicAdd(PART == 1 ? &ctl->tile_next : &ctl->tile_next2, kChunk);
+    if (lane == 0) b = tbeg + atomicAdd(PART == 1 ? &ctl->tile_next : &ctl->tile_next2, CHUNK);
     return __shfl_sync(kFull, b, 0);
   };
   int t = grab();
@@ -553,8 +555,10 @@ namespace {
 
 using namespace tdem::hm;
 
-constexpr int kBatchVariants = 4;
-inline int bvariant_block(int v) { return (v == 1 || v == 3) ? 128 : 256; }
+// Step-kernel shapes: block size, CTAs per SM and tiles per grab. 4 and 5 are
+// 1 and 3 with 2-tile grabs, for batches with few tiles per warp.
+constexpr int kBatchVariants = 6;
+inline int bvariant_block(int v) { return (v == 0 || v == 2) ? 256 : 128; }
 
 template <class T>
 using BatchFn = void (*)(Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int);
@@ -565,6 +569,8 @@ BatchFn<T> batch_fn_part(int variant) {
     case 1: return &batch_kernel<T, kBatch, 128, 4, PART>;
     case 2: return &batch_kernel<T, kBatch, 256, 3, PART>;
     case 3: return &batch_kernel<T, kBatch, 128, 6, PART>;
+    case 4: return &batch_kernel<T, kBatch, 128, 4, PART, 2>;
+    case 5: return &batch_kernel<T, kBatch, 128, 6, PART, 2>;
     default: return &batch_kernel<T, kBatch, 256, 2, PART>;
   }
 }
@@ -576,7 +582,7 @@ BatchFn<T> batch_fn(int variant, int part) {
   return part == 1 ? batch_fn_part<T, 1>(variant) : batch_fn_part<T, 2>(variant);
 }
 
-inline int bvariant_minb(int v) { return v == 0 ? 2 : v == 1 ? 4 : v == 2 ? 3 : 6; }
+inline int bvariant_minb(int v) { return v == 0 ? 2 : (v == 1 || v == 4) ? 4 : v == 2 ? 3 : 6; }
 
 // One device allocation, carved into 256-byte aligned arrays.
 struct Arena {

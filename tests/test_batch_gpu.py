@@ -216,6 +216,29 @@ def test_batch_alone_and_in_mix_are_bit_identical(bt):
     _same(ra, rm)
 
 
+def test_batch_step_variants_bit_identical(bt):
+    """Every step-kernel shape (block size, CTAs per SM, tiles per grab of the
+    work counter) gives the same bits for each instance of a mix: instance
+    sums are formed per tile in tile order, whichever warp took the tile."""
+    from tensordem_gb300 import _lib
+    runs = []
+    for v in range(_lib.lib().tdem_batch_num_variants()):
+        b = _batch(bt, precision=32, every=10)
+        ids = [b.admit(o) for o in _others(bt, 32)]
+        cfg, st = _gas(5)
+        ids.append(b.admit(_inst(bt, cfg, st)))
+        b.variant = v
+        b.step(80)
+        assert b.variant == v
+        runs.append([b.read(i) for i in ids])
+    assert len(runs) == 6
+    for got in runs[1:]:
+        for a, c in zip(runs[0], got):
+            _same(a, c)
+            for k in ("bond_elastic", "fracture_released", "tool_work", "peak_load"):
+                assert a["ledger"][k] == c["ledger"][k], k
+
+
 def test_batch_join_and_retire_keep_results_bit_identical(bt):
     a_cfg, a_st = _gas(1)
     b_cfg, b_st = _gas(2, 20)
