@@ -35,6 +35,29 @@ def test_demo_break_counts_match_reference_runs():
     assert str(P.load("demo_b0.015_s0.03")["break_digest"]) == "111527dd778f1d6f"
 
 
+def test_demo_goldens_match_independent_break_digests():
+    """sha256(failure_mode || failure_time_s)[:16] over all 5,460 pairs of the
+    21x5 demo right after `dem-2d --steps 2000`, as recorded from independent
+    runs of the reference CLI: 111527dd778f1d6f (0.015 / 0.03, 230 breaks)
+    and 5d4913305c94ad8f (0.01 / 0.02, 250 breaks). The fixtures also hold
+    the breaks that one more forces() evaluation at t = 2000 dt commits (two
+    in the 0.01 / 0.02 case); those are left out here."""
+    import hashlib
+    for name, digest, count in (("demo_b0.015_s0.03", "111527dd778f1d6f", 230),
+                                ("demo_b0.01_s0.02", "5d4913305c94ad8f", 250)):
+        g = P.load(name)
+        pairs = 105 * 104 // 2
+        mode = np.zeros(pairs, np.uint8)
+        when = np.full(pairs, -1.0)
+        mode[g["bond_pair_index"]] = g["failure_mode"]
+        when[g["bond_pair_index"]] = g["failure_time_s"]
+        late = (mode > 0) & (when >= float(g["final_time"]))
+        mode[late] = 0
+        when[late] = -1.0
+        assert int((mode > 0).sum()) == count, name
+        assert hashlib.sha256(mode.tobytes() + when.tobytes()).hexdigest()[:16] == digest, name
+
+
 def test_reproducibility_case():
     g = P.load("repro_7x3")
     P.replay(g, _oracle_from(g), to_np=np.asarray)
