@@ -10,13 +10,20 @@ Restated from the reference's
   tests/test_dem2d_fracture_ledger.py:57-94 - a controlled single-bond break
   against 0.5 k xi^2, the k xi^2 scaling of the channel, every break event of
   an indentation re-scored from the pre-step geometry, and a sub-threshold
-  negative control.
+  negative control;
+* scripts/verify_dem2d_energy_ledger.py:82-262, as exercised by
+  tests/test_dem2d_energy_ledger.py:71-146 - a free particle's viscous decay
+  v0 exp(-t/tau) and its dissipation 0.5 m v0^2 (1 - exp(-2t/tau)) with the
+  predicted first-order bookkeeping residual, a bonded harmonic oscillator
+  A cos(omega t) with omega = sqrt(2k/m), and the tool-work residual under
+  time-step refinement.
 
 The inputs and bounds are the reference's own.
 """
 
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass
 from typing import Any, Callable
 
@@ -57,7 +64,7 @@ def indentation(b: Backend, dt_scale: float = 1.0, seconds: float = INDENT_SECON
         + acc["fracture_release_J"]
     scale = abs(acc["tool_work_J"]) + abs(acc["damping_dissipation_J"]) + abs(e1 - e0)
     return dict(sim=sim, steps=steps, accounting=acc, raw=raw, closed=raw - acc["pair_contact_acquired_J"],
-                scale=scale)
+                scale=scale, e_end=e1)
 
 
 def momentum_gap(b: Backend, sim) -> tuple[float, float]:
@@ -194,6 +201,87 @@ def subthreshold(b: Backend) -> dict:
                 released=sim.accounting["fracture_release_J"], acquired=sim.accounting["pair_contact_acquired_J"])
 
 
+def ledger_residual(sim, e0: float) -> float:
+    """E_now - E0 + damping + fracture - tool work - external work - acquired
+    (positive: the ledger missed an energy input)."""
+    acc = sim.accounting
+    return (sim.mechanical_energy()["mechanical_J"] - e0 + acc["damping_dissipation_J"]
+            + acc["fracture_release_J"] - acc["tool_work_J"] - acc["external_work_J"]
+            - acc["pair_contact_acquired_J"])
+
+
+def park(b: Backend, sim) -> None:
+    """Every disc 1 m from the next on the x axis, at rest, free, unbonded."""
+    n = len(b.arr(sim.positions))
+    sim.positions = b.put(sim, np.stack((np.arange(n, dtype=np.float64), np.zeros(n)), axis=1))
+    sim.velocities = b.put(sim, np.zeros((n, 2)))
+    sim.fixed = b.put(sim, np.zeros(n, dtype=bool))
+    sim.alive = b.put(sim, np.zeros(len(b.arr(sim.alive)), dtype=bool))
+
+
+def drag_decay(b: Backend, dt_scale: float = 1.0, v0: float = 0.5, c: float = 2.0, tau_fraction: float = 1.5) -> dict:
+    """Case A: one free disc under linear drag c, nothing else acting."""
+    kw = dict(nx=2, ny=2, drag=c, contact_damping=0.0, tool_speed=1e-9, fix_edges=False)
+    dt0 = b.make(**kw).dt
+    sim = b.make(**kw, dt=dt0 * dt_scale)
+    park(b, sim)
+    vel = b.arr(sim.velocities).copy()
+    vel[0, 0] = v0
+    sim.velocities = b.put(sim, vel)
+    m = sim.config.mass
+    tau = m / c
+    e0 = sim.mechanical_energy()["mechanical_J"]
+    for _ in range(int(round(tau_fraction * tau / sim.dt))):
+        sim.step()
+    t = sim.time
+    v_sim = float(b.arr(sim.velocities)[0, 0])
+    v_ref = v0 * math.exp(-t / tau)
+    d_sim = sim.accounting["damping_dissipation_J"]
+    d_ref = 0.5 * m * v0 ** 2 * (1.0 - math.exp(-2.0 * t / tau))
+    ke_sim = sim.mechanical_energy()["mechanical_J"]
+    ke_ref = 0.5 * m * v_ref ** 2
+    r = ledger_residual(sim, e0)
+    # the ledger samples the dissipated power at the pre-update velocity
+    r_pred = 0.5 * (c / m) * sim.dt * d_ref
+    return dict(v_sim=v_sim, v_ref=v_ref, v_relerr=abs(v_sim - v_ref) / v_ref,
+                ke_relerr=abs(ke_sim - ke_ref) / ke_ref, d_sim=d_sim, d_relerr=abs(d_sim - d_ref) / d_ref,
+                residual=r, r_pred=r_pred, r_pred_relerr=abs(r - r_pred) / abs(r_pred),
+                r_over_d=abs(r) / d_ref)
+
+
+def bonded_oscillator(b: Backend, dt_scale: float = 1.0, k: float = 2000.0, amplitude_ratio: float = 0.005,
+                      periods: float = 3.0) -> dict:
+    """Case B: discs 0 and 1 joined by their bond alone, released from rest at
+    an extension of 0.5% of the rest length; no drag, no damping."""
+    kw = dict(nx=2, ny=2, bond_stiffness=k, contact_stiffness=k, drag=0.0, contact_damping=0.0, tool_speed=1e-9,
+              fix_edges=False, breaking_strain=10.0, shear_breaking_strain=10.0)
+    dt0 = b.make(**kw).dt
+    sim = b.make(**kw, dt=dt0 * dt_scale)
+    m = sim.config.mass
+    rest = 2.0 * sim.config.radius
+    amp = amplitude_ratio * rest
+    alive = np.zeros(len(b.arr(sim.alive)), dtype=bool)
+    alive[_pair_index(b, sim, 0, 1)] = True
+    sim.alive = b.put(sim, alive)
+    sim.fixed = b.put(sim, np.zeros(len(b.arr(sim.fixed)), dtype=bool))
+    pos = b.arr(sim.positions).copy()
+    pos[0] = (-rest / 2 - amp / 2, 0.0)
+    pos[1] = (rest / 2 + amp / 2, 0.0)
+    sim.positions = b.put(sim, pos)
+    sim.velocities = b.put(sim, np.zeros_like(pos))
+    omega = math.sqrt(2.0 * k / m)
+    e0 = sim.mechanical_energy()["mechanical_J"]
+    worst = 0.0
+    for _ in range(int(round(periods * 2.0 * math.pi / omega / sim.dt))):
+        sim.step()
+        p = b.arr(sim.positions)
+        ext = float(np.hypot(*(p[1] - p[0]))) - rest
+        worst = max(worst, abs(ext - amp * math.cos(omega * sim.time)) / amp)
+    acc = sim.accounting
+    return dict(e0=e0, k=k, amp=amp, xi_relerr_max=worst, r_over_e0=abs(ledger_residual(sim, e0)) / e0,
+                damping=acc["damping_dissipation_J"], tool=acc["tool_work_J"], fracture=acc["fracture_release_J"])
+
+
 # -- the assertions, shared by the CPU and GPU test modules ------------------
 
 def check_uniform_load_momentum(b: Backend) -> None:
@@ -259,3 +347,37 @@ def check_subthreshold(b: Backend) -> None:
     d = subthreshold(b)
     assert d["alive"]
     assert d["released"] == 0.0 and d["acquired"] == 0.0
+
+
+LEDGER_TOL = 0.03  # the reference's acceptance for the closed-form ledger cases
+
+
+def check_drag_decay(a: dict, a_half: dict) -> None:
+    assert a["v_sim"] < a["v_ref"] * 1.02
+    assert a["v_relerr"] < LEDGER_TOL and a["ke_relerr"] < LEDGER_TOL and a["d_relerr"] < LEDGER_TOL, a
+    assert a["r_over_d"] < LEDGER_TOL
+    assert a["r_pred"] > 0.0 and a["r_pred_relerr"] < 0.10, a
+    assert 0.4 < a_half["r_over_d"] / a["r_over_d"] < 0.6
+    assert a_half["d_relerr"] < a["d_relerr"]
+    # negative control: without the dissipation channel the identity is open
+    assert a["d_sim"] > 0.0 and a["d_sim"] / max(abs(a["residual"]), 1e-18) > 50.0
+
+
+def check_oscillator(coarse: dict, fine: dict) -> None:
+    assert coarse["r_over_e0"] < LEDGER_TOL
+    for key in ("damping", "tool", "fracture"):
+        assert abs(coarse[key]) <= 1e-12, key
+    assert abs(coarse["e0"] - 0.5 * coarse["k"] * coarse["amp"] ** 2) <= 1e-10 * coarse["e0"]
+    # semi-implicit Euler's phase error at omega dt = 0.11: a trajectory miss,
+    # not a ledger one, and first order in dt
+    assert LEDGER_TOL < coarse["xi_relerr_max"] < 0.10
+    assert 0.35 < fine["xi_relerr_max"] / coarse["xi_relerr_max"] < 0.65
+    assert fine["r_over_e0"] <= coarse["r_over_e0"]
+
+
+def check_tool_channel(run: dict, run_half: dict) -> None:
+    def over_scale(r):
+        return abs(r["closed"]) / max(r["e_end"], r["accounting"]["damping_dissipation_J"], 1e-12)
+    assert run["accounting"]["tool_work_J"] > 0.0
+    assert over_scale(run) < LEDGER_TOL
+    assert 0.2 < over_scale(run_half) / over_scale(run) < 0.7

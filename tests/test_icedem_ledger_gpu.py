@@ -51,8 +51,25 @@ def test_energy_ledger_closes_with_retained_contact_term(indentation):
     lc.check_energy_closure(indentation)
 
 
-def test_energy_residual_is_bookkeeping_not_timestep_error(b, indentation):
-    lc.check_residual_is_bookkeeping(indentation, lc.indentation(b, dt_scale=0.5))
+@pytest.fixture(scope="module")
+def indentation_half(b):
+    return lc.indentation(b, dt_scale=0.5)
+
+
+def test_energy_residual_is_bookkeeping_not_timestep_error(indentation, indentation_half):
+    lc.check_residual_is_bookkeeping(indentation, indentation_half)
+
+
+def test_drag_decay_matches_closed_form(b):
+    lc.check_drag_decay(lc.drag_decay(b), lc.drag_decay(b, dt_scale=0.5))
+
+
+def test_bonded_oscillator_ledger_and_integrator(b):
+    lc.check_oscillator(lc.bonded_oscillator(b), lc.bonded_oscillator(b, dt_scale=0.5))
+
+
+def test_tool_work_residual_shrinks_with_dt(indentation, indentation_half):
+    lc.check_tool_channel(indentation, indentation_half)
 
 
 def test_restart_accepts_checkpoint_without_new_ledger_channel():

@@ -33,8 +33,25 @@ def test_energy_ledger_closes_with_retained_contact_term(indentation):
     lc.check_energy_closure(indentation)
 
 
-def test_energy_residual_is_bookkeeping_not_timestep_error(indentation):
-    lc.check_residual_is_bookkeeping(indentation, lc.indentation(B, dt_scale=0.5))
+@pytest.fixture(scope="module")
+def indentation_half():
+    return lc.indentation(B, dt_scale=0.5)
+
+
+def test_energy_residual_is_bookkeeping_not_timestep_error(indentation, indentation_half):
+    lc.check_residual_is_bookkeeping(indentation, indentation_half)
+
+
+def test_drag_decay_matches_closed_form():
+    lc.check_drag_decay(lc.drag_decay(B), lc.drag_decay(B, dt_scale=0.5))
+
+
+def test_bonded_oscillator_ledger_and_integrator():
+    lc.check_oscillator(lc.bonded_oscillator(B), lc.bonded_oscillator(B, dt_scale=0.5))
+
+
+def test_tool_work_residual_shrinks_with_dt(indentation, indentation_half):
+    lc.check_tool_channel(indentation, indentation_half)
 
 
 def test_controlled_break_matches_closed_form():
