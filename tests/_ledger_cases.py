@@ -16,7 +16,11 @@ Restated from the reference's
   v0 exp(-t/tau) and its dissipation 0.5 m v0^2 (1 - exp(-2t/tau)) with the
   predicted first-order bookkeeping residual, a bonded harmonic oscillator
   A cos(omega t) with omega = sqrt(2k/m), and the tool-work residual under
-  time-step refinement.
+  time-step refinement;
+* tests/test_dem2d_energy_fracture_ledger_negative.py:56-533 - the energy
+  balance gate closes on a clean indentation and rejects a run in which one
+  ledger channel is zeroed, tripled or (for the dormant external-work channel)
+  offset by the tool work, while a sign flip of a dormant channel is vacuous.
 
 The inputs and bounds are the reference's own.
 """
@@ -64,7 +68,7 @@ def indentation(b: Backend, dt_scale: float = 1.0, seconds: float = INDENT_SECON
         + acc["fracture_release_J"]
     scale = abs(acc["tool_work_J"]) + abs(acc["damping_dissipation_J"]) + abs(e1 - e0)
     return dict(sim=sim, steps=steps, accounting=acc, raw=raw, closed=raw - acc["pair_contact_acquired_J"],
-                scale=scale, e_end=e1)
+                scale=scale, e0=e0, e_end=e1)
 
 
 def momentum_gap(b: Backend, sim) -> tuple[float, float]:
@@ -381,3 +385,41 @@ def check_tool_channel(run: dict, run_half: dict) -> None:
     assert run["accounting"]["tool_work_J"] > 0.0
     assert over_scale(run) < LEDGER_TOL
     assert 0.2 < over_scale(run_half) / over_scale(run) < 0.7
+
+
+# signed coefficients of dE - W_tool - W_ext + Q_damping + E_fracture - E_acquired
+BALANCE_SIGNS = {"tool_work_J": -1.0, "external_work_J": -1.0, "damping_dissipation_J": 1.0,
+                 "fracture_release_J": 1.0, "pair_contact_acquired_J": -1.0}
+BALANCE_TOL = 0.005
+
+
+def balance_error(run: dict, acc: dict | None = None) -> float:
+    """The balance gate's relative residual, over |W_tool| + |Q_damping| + |E_fracture|
+    of the same ledger."""
+    acc = run["accounting"] if acc is None else acc
+    r = run["e_end"] - run["e0"] + sum(s * float(acc[k]) for k, s in BALANCE_SIGNS.items())
+    scale = abs(acc["tool_work_J"]) + abs(acc["damping_dissipation_J"]) + abs(acc["fracture_release_J"])
+    return abs(r) / max(scale, 1e-18)
+
+
+def check_balance_gate_and_negative_controls(run: dict) -> None:
+    clean = balance_error(run)
+    assert run["sim"].broken_bonds > 0
+    assert clean < BALANCE_TOL, clean  # positive control
+    faults = [("fracture_release_J", 0.0, 0.0), ("fracture_release_J", 3.0, 0.0),
+              ("pair_contact_acquired_J", 0.0, 0.0), ("pair_contact_acquired_J", 3.0, 0.0),
+              ("tool_work_J", 0.0, 0.0), ("damping_dissipation_J", 0.0, 0.0)]
+    # external work is dormant in this run: fault it additively by the tool work
+    assert run["accounting"]["external_work_J"] == 0.0
+    faults.append(("external_work_J", 1.0, run["accounting"]["tool_work_J"]))
+    for channel, factor, offset in faults:
+        acc = dict(run["accounting"])
+        acc[channel] = acc[channel] * factor + offset
+        assert acc[channel] != run["accounting"][channel], channel  # the fault is not vacuous
+        err = balance_error(run, acc)
+        assert err > BALANCE_TOL and err > clean, (channel, factor, offset, err)
+    # a sign flip of the dormant channel changes nothing: a vacuous control
+    acc = dict(run["accounting"])
+    acc["external_work_J"] *= -1.0
+    assert acc["external_work_J"] == run["accounting"]["external_work_J"]
+    assert balance_error(run, acc) == clean

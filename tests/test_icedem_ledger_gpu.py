@@ -72,6 +72,10 @@ def test_tool_work_residual_shrinks_with_dt(indentation, indentation_half):
     lc.check_tool_channel(indentation, indentation_half)
 
 
+def test_balance_gate_rejects_single_channel_faults(indentation):
+    lc.check_balance_gate_and_negative_controls(indentation)
+
+
 def test_restart_accepts_checkpoint_without_new_ledger_channel():
     from tensordem_gb300 import DEMConfig, IceDEM
     sim = IceDEM(DEMConfig(nx=5, ny=3, tool_speed=0.2))

@@ -54,6 +54,10 @@ def test_tool_work_residual_shrinks_with_dt(indentation, indentation_half):
     lc.check_tool_channel(indentation, indentation_half)
 
 
+def test_balance_gate_rejects_single_channel_faults(indentation):
+    lc.check_balance_gate_and_negative_controls(indentation)
+
+
 def test_controlled_break_matches_closed_form():
     lc.check_controlled_break(B)
 
