@@ -51,3 +51,13 @@ def test_single_process_reduction_is_identity():
     import bench
     assert bench.max_over_ranks(3.5, "cpu") == 3.5
     assert bench.aggregate_rate(1, 100, 10, 2.0) == 500.0
+
+
+def test_cpu_baseline_runs_the_oracle_on_every_requested_core():
+    """The reference arm's sample: slabs of equal disc count, one spawned
+    process per core, all discs counted once."""
+    import bench
+    r = bench.cpu_oracle_rate(2, n_side=32, workers=2)
+    assert r["cores"] == 2 and r["kind"] == "port" and r["value"] > 0
+    assert "1,024-disc case" in r["sample"] and "2 vertical slabs" in r["sample"]
+    assert bench.host_cores() >= 1
