@@ -112,3 +112,18 @@ def test_step_guard_rejects_a_step_above_the_bound():
     base = DEM3DConfig(nx=3, ny=3, nz=3, contact_model="hertz", young_modulus=E_YOUNG, poisson_ratio=NU)
     with pytest.raises(ValueError, match="dt exceeds"):
         IceDEM3D(replace(base, dt=2.0 * base.recommended_dt))
+
+
+def test_pair_damping_mode_contract():
+    """The reference's tests/test_dem3d_pair_contact_damping.py:82-101: the
+    restitution mapping stays the default dashpot convention, unknown modes
+    and two conventions at once are refused, and the absolute mode takes any
+    non-negative damping."""
+    assert DEM3DConfig().contact_damping_model == "restitution"
+    with pytest.raises(ValueError):
+        DEM3DConfig(contact_damping_model="viscous")
+    with pytest.raises(ValueError):
+        DEM3DConfig(contact_damping_model="absolute", restitution_coefficient=0.5)
+    for damping in (0.0, 5.0, 40.0):
+        assert DEM3DConfig(contact_damping_model="absolute", contact_damping=damping).contact_damping_model == \
+            "absolute"
