@@ -42,3 +42,22 @@ def test_library_exports_every_declared_symbol(library):
 def test_version_and_capacity(library):
     assert library.tdem_version() >= 1
     assert library.tdem_icedem_max_discs() >= 105
+
+
+def test_variant_counts(library):
+    """Host-only queries: six single-engine step-kernel variants and six
+    batched shapes (block size, CTAs per SM, tiles per work grab)."""
+    assert library.tdem_hm_num_variants() == 6
+    assert library.tdem_batch_num_variants() == 6
+
+
+def test_restitution_damping_ratio_is_a_host_routine(library):
+    """The calibrated-restitution damping ratio runs on the host (no GPU):
+    e = 1 needs no damping, and lower restitution needs more."""
+    out = ctypes.c_double()
+    ratios = []
+    for e in (0.95, 0.7, 0.5, 0.3):
+        assert library.tdem_hertz_damping_ratio(ctypes.c_double(e), ctypes.byref(out)) == 0
+        ratios.append(out.value)
+    assert all(r > 0.0 for r in ratios)
+    assert ratios == sorted(ratios)
