@@ -1,7 +1,7 @@
 """The reference's 2-D mechanics-invariant and load-interface checks (its
 tests/test_mechanics_invariants.py:15-131 and tests/test_load_interface.py:12-48)
 on the numpy oracle of the reference mode (oracle/icedem.py), with the same
-inputs and bounds: the checker itself obeys them before it checks the CUDA
+inputs and bounds: the oracle itself obeys them before it checks the CUDA
 path (tests/test_icedem_reference_checks_gpu.py runs them there)."""
 
 import numpy as np
