@@ -49,6 +49,7 @@ def _args():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--cpu-sample-steps", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble and served-trace leg")
     return ap.parse_args()
 
 
@@ -227,13 +228,131 @@ def profiled_traffic() -> float | None:
 
 
 def algorithmic_bytes(n: int, head_bytes: int, contact_sides: int) -> int:
-    """Bytes one step must move: state read + write (pos, vel: 2 x 2 x 16 B per
-    disc), the list head (16 B per disc) and the tangential history of every
-    touching contact side (8 B read + 8 B write)."""
+    """Bytes one step must move in this layout: state read + write (pos, vel:
+    2 x 2 x 16 B per disc), the list head (16 B per disc) and the tangential
+    history of every touching contact side (8 B read + 8 B write)."""
     return n * (64 + head_bytes) + 16 * contact_sides
 
 
+def survey_bytes(n: int, k: int, c: int, b: int, r: float) -> float:
+    """The hot-path byte model N*64 + K*4 + C*16 + B*20 + 96*N/R: particle
+    state read and written, one 4-byte candidate index per candidate pair, 16 B
+    of history per active contact, 20 B per bond, and the rebuild's sort
+    traffic (96 B per particle) spread over the rebuild interval R."""
+    return n * 64 + k * 4 + c * 16 + b * 20 + (96.0 * n / r if r > 0 else 0.0)
+
+
+def timed_steps(eng, steps, warmup, flush_l2, stream, dev):
+    """Warm-up steps, then `steps` timed steps: L2 flushed (untimed), the step
+    kernel in its own event bracket, and a list rebuild, when the device says
+    one is due, in a bracket of its own. Returns (step ms, rebuild ms, wall s)."""
+    import torch
+    # the warm-up runs right before the timed steps in the same loop shape: a
+    # first launch after an idle spell takes ~5x longer
+    for _ in range(max(3, warmup)):
+        flush_l2()
+        eng.step_kernel()
+        if eng.rebuild_pending():
+            eng.rebuild()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    rebuild_evs = []
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for e0, e1 in evs:
+        flush_l2()
+        e0.record(stream)
+        eng.step_kernel()
+        e1.record(stream)
+        if eng.rebuild_pending():
+            r0 = torch.cuda.Event(enable_timing=True)
+            r1 = torch.cuda.Event(enable_timing=True)
+            r0.record(stream)
+            eng.rebuild()
+            r1.record(stream)
+            rebuild_evs.append((r0, r1))
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    eng.check()
+    return ([e0.elapsed_time(e1) for e0, e1 in evs], [r0.elapsed_time(r1) for r0, r1 in rebuild_evs], wall)
+
+
+def fp64_rate(seed, steps, warmup, flush_l2, stream, dev) -> dict:
+    """The plain FP64 build of the same kernels on the same workload and loop."""
+    from tensordem_gb300.hm2d import HM2D, granular_gas_case
+    cfg, st = granular_gas_case(N_SIDE, seed=seed, precision=64)
+    eng = HM2D(cfg, device=dev)
+    eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
+    eng.autotune(steps=2)
+    eng.step(2)
+    step_ms, rebuild_ms, _ = timed_steps(eng, steps, warmup, flush_l2, stream, dev)
+    total = sum(step_ms) + sum(rebuild_ms)
+    return {"value": cfg.n * steps / (total / 1e3), "unit": UNIT, "steps": steps, "variant": eng.variant,
+            "step_kernel_us_mean": 1e3 * sum(step_ms) / len(step_ms), "rebuilds": len(rebuild_ms),
+            "note": "precision=64 build of the same kernels (FP64 contacts, sums and ledger), same seeded "
+                    "1,048,576-disc state and the same flushed per-step loop"}
+
+
+BATCH_INSTANCES = 512
+BATCH_STEPS = 1000
+BATCH_SAMPLE = 64
+
+
+def batched_leg(seed: int = 0, *, serve_seconds: float = 20.0, calibrate_seconds: float = 4.0) -> dict:
+    """The metric's second half on this GPU, in this run.
+
+    A seeded ensemble of the 4096-run mix's shape (half bonded-ice
+    indentations, half granular column collapses, N log-uniform 100-20,000,
+    mu U[0.3, 0.7], E log-uniform 1-70 GPa) cut to 512 runs x 1,000 steps: all
+    of them solved in one batched engine (FP32 contacts, FP64 ledger), and a
+    seeded sample of 64 of them solved one by one through the plain FP64
+    single-solve engine (create, upload, steps, read-back each), extrapolated
+    to the 512. Then a short served Poisson trace: requests of the same mix with
+    N log-uniform 500-200,000 and S log-uniform 100-5,000 steps arrive for 20 s
+    at 0.8 of the capacity measured by a 4 s saturated run, under a 150 GB HBM
+    budget; p50 / p95 / p99 time-to-completion."""
+    import numpy as np
+
+    from tensordem_gb300 import ensemble, serve
+    from tensordem_gb300.batch import ensemble_case
+    specs = ensemble_case(BATCH_INSTANCES, seed=seed, steps=BATCH_STEPS)
+    rng = np.random.default_rng(seed + 1)
+    sample = sorted(rng.choice(len(specs), size=BATCH_SAMPLE, replace=False).tolist())
+    rep, ledgers = ensemble.run_batched(specs, precision=32, autotune_steps=2)
+    seq = ensemble.run_sequential_fp64(specs, sample)
+    mean_s = float(np.mean([x["seconds"] for x in seq.values()]))
+    one_by_one = len(specs) / (mean_s * len(specs))
+    agree = ensemble.compare(ledgers, seq)
+    budget = int(150e9)
+    n_min, n_max, s_min, s_max, block = 500, 200_000, 100, 5000, 100
+    capacity = serve.calibrate(seconds=calibrate_seconds, budget_bytes=budget, block=block, seed=seed,
+                               n_min=n_min, n_max=n_max, s_min=s_min, s_max=s_max)
+    trace = serve.make_trace(duration=serve_seconds, capacity=capacity, load=0.8, seed=seed, n_min=n_min,
+                             n_max=n_max, s_min=s_min, s_max=s_max)
+    srv = serve.serve(trace, budget_bytes=budget, block=block, time_limit=serve_seconds * 4 + 30)
+    srv.pop("done")
+    return {
+        "workload": f"{BATCH_INSTANCES} runs x {BATCH_STEPS} steps of the mixed ensemble (half bonded-ice "
+                    "indentations, half granular column collapses; N log-uniform 100-20,000; seed "
+                    f"{seed}); served trace: Poisson arrivals for {serve_seconds:g} s at 0.8 of the measured "
+                    f"capacity, N log-uniform {n_min}-{n_max}, S log-uniform {s_min}-{s_max}, 150 GB budget",
+        "solves_per_s": rep["solves_per_s"],
+        "one_by_one_fp64_solves_per_s": one_by_one,
+        "one_by_one_sample": f"{BATCH_SAMPLE} of the {BATCH_INSTANCES} runs (seeded), mean {mean_s:.4f} s per "
+                             "solve incl. create, upload, steps, read-back; extrapolated",
+        "speedup": rep["solves_per_s"] / one_by_one,
+        "particle_steps_per_s": rep["particle_steps_per_s"],
+        "particles": rep["particles"], "instances_with_status": rep["instances_with_status"],
+        "peak_load_rel_err_max": agree["peak_load_rel_err_max"],
+        "ledger_total_rel_diff_max": agree["ledger_total_rel_diff_max"],
+        "served": {"capacity_particle_steps_per_s": capacity, "requests": srv["requests"],
+                   "completed": srv["completed"], "latency_s": srv["latency_s"],
+                   "queue_wait_s": srv["queue_wait_s"], "particle_steps_per_s": srv["particle_steps_per_s"],
+                   "status_errors": srv["status_errors"]},
+    }
+
+
 def run_ours(a) -> None:
+    import numpy as np
     import torch
 
     from tensordem_gb300.hm2d import HM2D, granular_gas_case
@@ -259,57 +378,45 @@ def run_ours(a) -> None:
         flush_r.sum()
 
     stream = torch.cuda.current_stream(dev)
-    led0 = eng.ledger()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
-    rebuild_evs = []
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    # Each timed step: L2 flushed (untimed), then the step kernel in its own
-    # event bracket. A list rebuild, when the device says one is due, runs in
-    # its own bracket and is added to the total: all of the run's work is timed.
     with ClockSampler(local) as clocks:
-        t0 = time.perf_counter()
-        for e0, e1 in evs:
-            flush_l2()
-            e0.record(stream)
-            eng.step_kernel()
-            e1.record(stream)
-            if eng.rebuild_pending():
-                r0 = torch.cuda.Event(enable_timing=True)
-                r1 = torch.cuda.Event(enable_timing=True)
-                r0.record(stream)
-                eng.rebuild()
-                r1.record(stream)
-                rebuild_evs.append((r0, r1))
-        torch.cuda.synchronize(dev)
-        wall = time.perf_counter() - t0
-    eng.check()
-    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    rebuild_ms = [r0.elapsed_time(r1) for r0, r1 in rebuild_evs]
+        step_ms, rebuild_ms, wall = timed_steps(eng, a.steps, a.warmup, flush_l2, stream, dev)
     kernel_ms = sum(step_ms) / len(step_ms)
     total_ms = sum(step_ms) + sum(rebuild_ms)
     if world > 1:
         total_ms = max_over_ranks(total_ms, dev)
         torch.distributed.barrier()
     led1 = eng.ledger()
-    rebuilds = led1["rebuilds"] - led0["rebuilds"]
     clk = clocks.summary()
     n = cfg.n
     value = aggregate_rate(world, n, a.steps, total_ms / 1e3)
 
-    # contacts touching at the end of the run (for the algorithmic byte count)
+    # candidate pairs K, touching contacts C (with stored history), bonds B
+    # and the rebuild interval R of the run so far, for the byte models
     hist = eng.history()
-    contact_sides = 2 * len(hist)
-    alg = algorithmic_bytes(n, 16, contact_sides)
+    k_pairs = len(eng.pairs())
+    c_contacts = len(hist)
+    r_interval = led1["evals"] / max(1, led1["rebuilds"])
+    alg = algorithmic_bytes(n, 16, 2 * c_contacts)
     peak, peak_kind = measured_peak()
     achieved = alg / (kernel_ms / 1e3) / 1e9
+    traffic = profiled_traffic()
+    sb = survey_bytes(n, k_pairs, c_contacts, 0, r_interval)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profiled_traffic(), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "algorithmic_bytes_per_step": alg}
+                "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_step": alg,
+                "survey_model": {"bytes_per_step": sb, "achieved": sb / (kernel_ms / 1e3) / 1e9,
+                                 "frac": sb / (kernel_ms / 1e3) / 1e9 / peak,
+                                 "N": n, "K": k_pairs, "C": c_contacts, "B": 0, "R": r_interval},
+                "dram": None if traffic is None else {
+                    "bytes_per_launch": traffic, "achieved": traffic / (kernel_ms / 1e3) / 1e9,
+                    "frac": traffic / (kernel_ms / 1e3) / 1e9 / peak,
+                    "note": "DRAM bytes of one ncu-captured launch: the new state stays in L2 during the "
+                            "launch and is written back after it"}}
 
     # end to end through the C ABI with host buffers (rank-local)
-    import numpy as np
     e2e_eng = HM2D(cfg, device=dev)
     e2e_eng.variant = eng.variant
     host = {k: np.ascontiguousarray(v) for k, v in st.items()}
@@ -324,6 +431,7 @@ def run_ours(a) -> None:
     e2e_eng.read_state_host(out_pos, out_vel, out_om)
     e2e_s = time.perf_counter() - t0
     e2e_eng.check()
+    del e2e_eng
     if world > 1:
         e2e_s = max_over_ranks(e2e_s, dev)
     h2d = 8 * n * (2 + 2 + 1 + 1 + 1 + 1)
@@ -333,6 +441,11 @@ def run_ours(a) -> None:
            "note": "one solve through tdem_hm_set_state/step/read_state with host arrays: upload, "
                    f"{a.steps} steps, download; L2 flushed before it"}
 
+    fp64 = fp64_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev)
+    batched = None
+    if rank == 0 and world == 1 and not a.no_batched:
+        del eng
+        batched = batched_leg(0)
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         cpu = cpu_oracle_rate(max(1, a.cpu_sample_steps))
@@ -342,14 +455,14 @@ def run_ours(a) -> None:
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": workload_config(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": a.steps + 12 * len(rebuild_ms),
-                "clocks": clk,
-                "extra": {"variant": eng.variant, "graph": led1["graph"], "autotune_ms_per_10_steps": tuning,
-                          "rebuilds_in_timed_region": rebuilds, "rebuild_ms_total": sum(rebuild_ms),
+                "clocks": clk, "batched": batched,
+                "extra": {"variant": led1["variant"], "graph": led1["graph"], "autotune_ms_per_10_steps": tuning,
+                          "rebuilds_in_timed_region": len(rebuild_ms), "rebuild_ms_total": sum(rebuild_ms),
                           "step_kernel_us_mean": 1e3 * kernel_ms,
                           "step_kernel_us_median": 1e3 * statistics.median(step_ms),
                           "wall_s_timed_loop": wall,
                           "max_neighbors_seen": led1["max_neighbors"],
-                          "touching_contacts_end": len(hist)}}
+                          "touching_contacts_end": c_contacts, "fp64": fp64}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

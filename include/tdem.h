@@ -157,6 +157,28 @@ int tdem_icedem_step(tdem_icedem* h, const tdem_icedem_state* st, const double* 
  * when it stopped on a non-finite state). */
 int tdem_icedem_steps_done(const tdem_icedem* h);
 
+/* Fragments of the state: connected components of the intact bonds given
+ * by the per-pair alive flags (P,) bool (device), isolated discs included.
+ * labels_host[k] (n ints) = the smallest disc id of disc k's fragment.
+ * Replaces the component search of IceDEM.fragments
+ * (src/tensordem/dem.py:462-484). Synchronizes `stream`. */
+int tdem_icedem_fragments(tdem_icedem* h, const void* alive, int32_t* labels_host, void* stream);
+
+/* Stored mechanical energy of the state (positions, velocities (n,2) FP64 and
+ * the per-pair alive flags (P,) bool, device arrays) with the tool at `time`:
+ * out_host[0..4] = kinetic, intact-bond springs (per-bond stiffness when
+ * set), penalty energy of overlapping pairs that are not intact bonds, tool
+ * penalty energy, their sum (J). Replaces IceDEM.mechanical_energy
+ * (src/tensordem/dem.py:603-624) and its per-bond-stiffness form
+ * (src/tensordem/calibrated_dem.py:79-93). Synchronizes `stream`. */
+int tdem_icedem_energy(tdem_icedem* h, const double* positions, const double* velocities, const void* alive,
+                       double time, double* out_host, void* stream);
+
+/* The TDEM_L_COUNT ledger doubles copied into a device buffer, ordered on
+ * `stream` (no synchronization): lets a caller record diagnostics rows on the
+ * device, as the dem-2d command's history does (src/tensordem/cli.py:69-105). */
+int tdem_icedem_ledger_to_device(tdem_icedem* h, double* out_device, void* stream);
+
 /* Ledger transfer (host doubles, up to TDEM_L_COUNT). Synchronizes `stream`. */
 int tdem_icedem_read_ledger(tdem_icedem* h, double* out_host, int count, void* stream);
 int tdem_icedem_write_ledger(tdem_icedem* h, const double* in_host, int count, void* stream);
@@ -319,9 +341,9 @@ int tdem_hm_get_variant(const tdem_hm* h);
 int tdem_hm_autotune(tdem_hm* h, int steps, float* ms_out, void* stream);
 
 /* Allocation-free contact forces. No counterpart in the reference: it exists
- * for callers that cannot allocate device memory, such as code running while
- * another solver's CUDA graph is being captured, real-time coupling loops and
- * plug-ins whose host application owns all device memory.
+ * for callers that cannot allocate device memory, such as plug-ins whose host
+ * application owns and budgets all device memory, and real-time coupling
+ * loops in which an allocation's latency or failure cannot be accepted.
  *
  * One Hertz-Mindlin force evaluation of `cfg->n` discs given in original order
  * as device arrays (positions (n,2), velocities (n,2), omega, radius, mass,
@@ -335,16 +357,39 @@ int tdem_hm_autotune(tdem_hm* h, int steps, float* ms_out, void* stream);
  * process exits. Limits: n <= 16384 discs, grids up to 256 x 256 cells, at
  * most 8 candidate partners per disc; larger inputs are rejected with
  * TDEM_ERR_BADARG (or TDEM_ERR_CAPACITY for a crowded disc) and a message in
- * err_buf (optional, err_len bytes). The first call on a device resolves the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture. All calls share the one array, which keeps the last
- * call's contents (each call clears what must start at zero): calls that
- * overlap on the GPU, on any streams or threads, race. The call synchronizes
- * `stream` to read the evaluation's status. */
+ * err_buf (optional, err_len bytes); the configuration passes the same checks
+ * as tdem_hm_create, and max_bonds and indenter_radius must be 0 (contacts,
+ * walls and gravity only). The first call on a device resolves the array's
+ * device address (cudaGetSymbolAddress) and keeps it for the process: make
+ * that first call before any stream capture, and do not reset the device
+ * (cudaDeviceReset) between calls. All calls share the one array, which keeps
+ * the last call's contents (each call clears what must start at zero): calls
+ * that overlap on the GPU, on any streams or threads, race. The call
+ * synchronizes `stream` to read the evaluation's status. */
 int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos, const double* vel,
                                    const double* omega, const double* radius, const double* mass,
                                    const double* inertia, double* out_force, double* out_torque,
                                    char* err_buf, size_t err_len, void* stream);
+
+/* The Hertz-Mindlin contact law on its own: the per-contact arithmetic of
+ * the step kernel (the same device function) applied to `count` pair states,
+ * in the engine's precision (cfg->precision) with cfg's material (young,
+ * poisson, restitution, mu, dt; the grid fields are not used). Replaces the
+ * reference's contact-law helpers: the Hertz normal force with the Tsuji
+ * dashpot (src/tensordem/scale_ceiling/kernel.py:300-310), the Mindlin
+ * tangential spring with the Coulomb cap and state projection
+ * (src/tensordem/hertz_mindlin.py:118-176) and the history increment
+ * (src/tensordem/contact_tangential.py:377-417).
+ *
+ * in (host, count x 16 doubles per row): overlap delta, unit normal (x, y)
+ * from a to b, r_a, r_b, v_a (x, y), omega_a, v_b (x, y), omega_b, 1/m_a,
+ * 1/m_b, stored history xi (x, y) in a's orientation, 1 unused. out (host,
+ * count x 8 per row): force on a (x, y), n x F_a (the torque on a is r_a
+ * times it), updated history (x, y), dissipated energy of the step, Hertz
+ * energy, spring energy. A pair without overlap (delta <= 0), or of two
+ * clamped discs (1/m_a + 1/m_b = 0), reports zeros: its history resets.
+ * Synchronizes `stream`. */
+int tdem_hm_contact_law(const tdem_hm_config* cfg, int64_t count, const double* in, double* out, void* stream);
 
 /* 1 (default): steps run as one conditional CUDA graph launch; 0: plain launches. */
 int tdem_hm_use_graph(tdem_hm* h, int on);

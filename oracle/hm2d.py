@@ -119,6 +119,44 @@ class HMParams:
         return 2.0 * math.sqrt(5.0 / 6.0) * tsuji_beta(self.restitution)
 
 
+def contact_law(p: HMParams, delta, nrm, ra, rb, inv_ma, inv_mb, vel_a, vel_b, om_a, om_b, xi) -> dict:
+    """The per-contact Hertz-Mindlin law for K active contacts (delta > 0).
+
+    ``nrm`` is the unit normal from a to b (K, 2), ``xi`` the stored
+    tangential history in a's orientation. The relative velocity of the
+    contact points is v_a - v_b + (omega_a r_a + omega_b r_b) t with
+    t = (-n_y, n_x) (granular2d/engine.py:458-482). Returns the force on a,
+    ``cr`` = n x F_a (torque on a = r_a cr, on b = r_b cr), the updated
+    history, the normal force, the elastic part and the two dissipation terms
+    of the step (kernel.py:300-326, hertz_mindlin.py:118-176,
+    contact_tangential.py:377-417, granular2d/engine.py:483-497).
+    """
+    dt = p.dt
+    tng = np.stack((-nrm[:, 1], nrm[:, 0]), axis=1)
+    reff = ra * rb / (ra + rb)
+    meff = 1.0 / (inv_ma + inv_mb)
+    sq = np.sqrt(reff * delta)
+    s_n = 2.0 * p.estar * sq
+    f_el = (2.0 / 3.0) * s_n * delta
+    v_rel = vel_a - vel_b + (om_a * ra + om_b * rb)[:, None] * tng
+    v_n = (v_rel * nrm).sum(axis=1)
+    f_n = np.maximum(f_el + p.damp * np.sqrt(s_n * meff) * v_n, 0.0)
+    v_t = v_rel - v_n[:, None] * nrm
+    xi = xi + v_t * dt
+    xi = xi - (xi * nrm).sum(axis=1)[:, None] * nrm
+    s_t = 8.0 * p.gstar * sq
+    fmag = s_t * np.sqrt((xi * xi).sum(axis=1))
+    cap = p.mu * f_n
+    slip = fmag > cap
+    scale = np.where(slip, cap / np.maximum(fmag, 1e-300), 1.0)
+    slip_loss = float(np.sum(np.where(slip, cap * (fmag - cap) / np.maximum(s_t, 1e-300), 0.0)))
+    xi = xi * scale[:, None]
+    f_a = -f_n[:, None] * nrm - s_t[:, None] * xi
+    cr = nrm[:, 0] * f_a[:, 1] - nrm[:, 1] * f_a[:, 0]
+    return dict(f_a=f_a, cr=cr, xi=xi, f_n=f_n, f_el=f_el, s_t=s_t, sliding=slip, slip_loss=slip_loss,
+                dashpot_loss=float(np.sum((f_n - f_el) * v_n)) * dt)
+
+
 @dataclass
 class ContactState:
     keys: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
@@ -222,33 +260,16 @@ class HM2DOracle:
             xi[hit] = st.xi[at[hit]]
         if len(i):
             nrm = d / dist[:, None]
-            tng = np.stack((-nrm[:, 1], nrm[:, 0]), axis=1)
             ra, rb = self.radius[i], self.radius[j]
-            reff = ra * rb / (ra + rb)
-            meff = 1.0 / (self.inv_mass[i] + self.inv_mass[j])
-            sq = np.sqrt(reff * delta)
-            s_n = 2.0 * p.estar * sq
-            f_el = (2.0 / 3.0) * s_n * delta
-            v_rel = vel[i] - vel[j] + (omega[i] * ra + omega[j] * rb)[:, None] * tng
-            v_n = (v_rel * nrm).sum(axis=1)
-            f_n = np.maximum(f_el + p.damp * np.sqrt(s_n * meff) * v_n, 0.0)
-            v_t = v_rel - v_n[:, None] * nrm
-            xi = xi + v_t * dt
-            xi = xi - (xi * nrm).sum(axis=1)[:, None] * nrm
-            s_t = 8.0 * p.gstar * sq
-            fmag = s_t * np.sqrt((xi * xi).sum(axis=1))
-            cap = p.mu * f_n
-            slip = fmag > cap
-            scale = np.where(slip, cap / np.maximum(fmag, 1e-300), 1.0)
-            diss += float(np.sum(np.where(slip, cap * (fmag - cap) / np.maximum(s_t, 1e-300), 0.0)))
-            xi = xi * scale[:, None]
-            f_a = -f_n[:, None] * nrm - s_t[:, None] * xi
-            cr = nrm[:, 0] * f_a[:, 1] - nrm[:, 1] * f_a[:, 0]
+            c = contact_law(p, delta, nrm, ra, rb, self.inv_mass[i], self.inv_mass[j], vel[i], vel[j],
+                            omega[i], omega[j], xi)
+            xi, f_a, cr = c["xi"], c["f_a"], c["cr"]
+            diss += c["slip_loss"]
             np.add.at(force, i, f_a)
             np.add.at(force, j, -f_a)
             np.add.at(torque, i, ra * cr)
             np.add.at(torque, j, rb * cr)
-            diss += float(np.sum((f_n - f_el) * v_n)) * dt
+            diss += c["dashpot_loss"]
         if advance:
             self.state = ContactState(keys, xi)
         # walls

@@ -1,7 +1,7 @@
 """Time the reference's own 2-D disc engine on this host's CPU (a CPU data
 point beside the 1M-disc settling case; the reference tree must be importable)::
 
-    PYTHONPATH=/root/reference/src python oracle/time_reference2d.py [--discs-side 1024] [--steps 20]
+    PYTHONPATH=<reference>/src python oracle/time_reference2d.py [--discs-side 1024] [--steps 20]
 
 The reference has no 2-D Hertz-Mindlin engine; its closest 2-D cell-list
 engine is ``tensordem.granular2d.DiskSystem`` (linear spring-dashpot,

@@ -1,7 +1,7 @@
 """Time the reference's own 3-D step on this host's CPU (the CPU baseline of
 the 3-D reference mode; the reference tree must be importable)::
 
-    PYTHONPATH=/root/reference/src python oracle/time_reference3d.py
+    PYTHONPATH=<reference>/src python oracle/time_reference3d.py
 
 It builds the reference's ``tensordem.dem3d.IceDEM3D`` on the indentation
 specimens of ``python -m tensordem_gb300 bench-3d`` (breaking strains

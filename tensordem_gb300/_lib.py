@@ -170,6 +170,9 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_icedem_read_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
         "tdem_icedem_write_ledger": (i32, [vp, C.POINTER(C.c_double), i32, vp]),
         "tdem_icedem_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "tdem_icedem_energy": (i32, [vp, vp, vp, vp, dbl, C.POINTER(C.c_double), vp]),
+        "tdem_icedem_fragments": (i32, [vp, vp, vp, vp]),
+        "tdem_icedem_ledger_to_device": (i32, [vp, vp, vp]),
         "tdem_icedem3d_max_particles": (i32, []),
         "tdem_icedem3d_create": (i32, [C.POINTER(IceDEM3DConfigC), C.POINTER(IceDEM3DTopologyC),
                                        C.POINTER(vp)]),
@@ -205,6 +208,7 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_hm_rebuild": (i32, [vp, vp]),
         "tdem_hm_read_history": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_hm_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
+        "tdem_hm_contact_law": (i32, [C.POINTER(HMConfigC), C.c_int64, vp, vp, vp]),
         "tdem_batch_bytes": (i32, [C.POINTER(BatchConfigC), C.POINTER(C.c_int64)]),
         "tdem_batch_create": (i32, [C.POINTER(BatchConfigC), C.POINTER(vp)]),
         "tdem_batch_destroy": (None, [vp]),

@@ -67,15 +67,10 @@ class CalibratedIceDEM(IceDEM):
         super().run(steps)
 
     def mechanical_energy(self) -> dict:
-        """The base record with the bond energy of the per-bond springs."""
+        """The energy record; the kernel sums the bond springs with the
+        per-bond stiffness it holds (calibrated_dem.py:79-93)."""
         self._check()
-        record = super().mechanical_energy()
-        delta = self.positions[self.pairs[:, 1]] - self.positions[self.pairs[:, 0]]
-        extension = torch.linalg.vector_norm(delta, dim=1) - self.rest_lengths
-        corrected = float(0.5 * (self.pair_coefficients[self.alive] * extension[self.alive].square()).sum())
-        record["mechanical_J"] += corrected - record["bond_J"]
-        record["bond_J"] = corrected
-        return record
+        return super().mechanical_energy()
 
     def snapshot(self) -> dict:
         """Restart record, schema ``tensordem.calibrated-restart/1``."""

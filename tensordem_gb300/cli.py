@@ -22,37 +22,105 @@ from __future__ import annotations
 import argparse
 import csv
 import json
+import math
 import sys
 import time
 from dataclasses import asdict
 from pathlib import Path
 
+import numpy as np
 import torch
 
 
 def read_hull_profile(path: Path) -> torch.Tensor:
-    """x,y CSV of local hull vertices in metres (src/tensordem/cli.py:15-39)."""
+    """Hull vertices from a CSV file in metres: a header row with columns named
+    x and y, then one vertex per row (the file the reference's dem-2d command
+    reads, src/tensordem/cli.py:15-39). Raises ValueError on an unreadable
+    file, missing headers, a bad or non-finite number, fewer than two
+    vertices or a zero-length segment."""
     try:
-        with path.open(newline="", encoding="utf-8-sig") as stream:
-            reader = csv.DictReader(stream)
-            if reader.fieldnames is None or not {"x", "y"}.issubset(reader.fieldnames):
-                raise ValueError("hull profile CSV must contain x,y column headers")
-            points = []
-            for line_number, row in enumerate(reader, start=2):
-                try:
-                    points.append((float(row["x"]), float(row["y"])))
-                except (TypeError, ValueError) as exc:
-                    raise ValueError(f"invalid x,y value in hull profile CSV line {line_number}") from exc
+        text = path.read_text(encoding="utf-8-sig")
     except OSError as exc:
         raise ValueError(f"cannot read hull profile CSV: {exc}") from exc
-    if len(points) < 2:
+    table = [(number, row) for number, row in enumerate(csv.reader(text.splitlines()), start=1) if row]
+    if not table or not {"x", "y"} <= set(table[0][1]):
+        raise ValueError("hull profile CSV must contain x,y column headers")
+    ix, iy = table[0][1].index("x"), table[0][1].index("y")
+    vertices = []
+    for number, row in table[1:]:
+        try:
+            vertices.append((float(row[ix]), float(row[iy])))
+        except (IndexError, ValueError) as exc:
+            raise ValueError(f"invalid x,y value in hull profile CSV line {number}") from exc
+    if len(vertices) < 2:
         raise ValueError("hull profile CSV must contain at least two vertices")
-    profile = torch.tensor(points, dtype=torch.float64)
-    if not bool(torch.isfinite(profile).all()):
+    v = np.asarray(vertices, dtype=np.float64)
+    if not np.isfinite(v).all():
         raise ValueError("hull profile coordinates must be finite")
-    if bool((torch.linalg.vector_norm(profile[1:] - profile[:-1], dim=1) <= 1e-12).any()):
+    if (np.hypot(*np.diff(v, axis=0).T) <= 1e-12).any():
         raise ValueError("hull profile must not contain zero-length segments")
-    return profile
+    return torch.from_numpy(v)
+
+
+# history.csv columns (the diagnostics record) and where each comes from in a
+# device-side sample row: the clock, the tool, the reactions, the broken-bond
+# count, the kinetic energy, then ledger slots (impulses x/y, energies).
+_HISTORY = ("time", "tool_x", "tool_y", "reaction_x", "reaction_y", "boundary_reaction_x", "boundary_reaction_y",
+            "broken_bonds", "kinetic_energy", "tool_impulse_on_ice_x_Ns", "tool_impulse_on_ice_y_Ns",
+            "support_impulse_x_Ns", "support_impulse_y_Ns", "drag_impulse_x_Ns", "drag_impulse_y_Ns",
+            "external_impulse_x_Ns", "external_impulse_y_Ns", "fracture_release_J", "pair_contact_acquired_J",
+            "tool_work_J", "damping_dissipation_J", "external_work_J")
+_LEDGER_COLUMNS = (11, 12, 7, 8, 9, 10, 5, 6, 1, 2, 3, 4, 0)  # ledger slots of the last 13 columns
+
+
+class _Samples:
+    """The samples of a dem-2d run recorded on the device: one history row
+    (forces evaluated on the device, ledger copied device to device), the
+    positions, velocities, intact-bond flags and tool position. Nothing is
+    copied to the host until the run ends."""
+
+    def __init__(self, sim, count: int):
+        dev, n = sim.device, len(sim.positions)
+        self.sim = sim
+        self.rows = torch.zeros((count, len(_HISTORY)), dtype=torch.float64, device=dev)
+        self.positions = torch.empty((count, n, 2), dtype=torch.float64, device=dev)
+        self.velocities = torch.empty_like(self.positions)
+        self.bonds = torch.empty((count, int(sim.bonded.sum())), dtype=torch.bool, device=dev)
+        self.tool = torch.empty((count, 2), dtype=torch.float64, device=dev)
+        self.ledger = torch.empty(32, dtype=torch.float64, device=dev)
+        self.columns = torch.tensor(_LEDGER_COLUMNS, dtype=torch.int64, device=dev)
+        self.times: list[float] = []
+
+    def take(self) -> None:
+        from . import _lib
+        sim, k = self.sim, len(self.times)
+        force, reaction = sim.forces()
+        row = self.rows[k]
+        tool = sim.tool_position
+        row[0] = sim.time
+        row[1:3] = tool
+        row[3:5] = reaction
+        row[5:7] = -force[sim.fixed].sum(dim=0)
+        row[7] = (sim.bonded & ~sim.alive).sum()
+        row[8] = 0.5 * sim.config.mass * sim.velocities.square().sum()
+        stream = torch.cuda.current_stream(sim.device).cuda_stream
+        rc = _lib.lib().tdem_icedem_ledger_to_device(sim._handle.ptr, self.ledger.data_ptr(), stream)
+        _lib.check(rc, sim._handle.ptr, "tdem_icedem_ledger_to_device")
+        row[9:] = self.ledger[self.columns]
+        self.positions[k] = sim.positions
+        self.velocities[k] = sim.velocities
+        self.bonds[k] = sim.alive[sim.bonded]
+        self.tool[k] = tool
+        self.times.append(sim.time)
+
+    def write_history(self, path: Path) -> None:
+        count = len(self.times)
+        with path.open("w", newline="", encoding="utf-8") as stream:
+            writer = csv.writer(stream)
+            writer.writerow(_HISTORY)
+            for values in self.rows[:count].cpu().tolist():
+                values[7] = int(values[7])
+                writer.writerow(values)
 
 
 def _cmd_dem_2d(args: argparse.Namespace) -> None:
@@ -61,66 +129,43 @@ def _cmd_dem_2d(args: argparse.Namespace) -> None:
     if args.steps < 1 or args.save_every < 1:
         sys.exit("--steps and --save-every must be positive")
     try:
-        hull_profile = read_hull_profile(args.hull_profile) if args.hull_profile else None
-        hull_speed = (args.hull_velocity_x**2 + args.hull_velocity_y**2) ** 0.5
-        speed_bound = max(args.speed, hull_speed, 1e-12)
-        config = DEMConfig(nx=args.nx, ny=args.ny, dt=args.dt, tool_speed=speed_bound,
-                           breaking_strain=args.breaking_strain,
-                           shear_breaking_strain=args.shear_breaking_strain, device=args.device)
-        if hull_profile is None:
-            simulation = IceDEM(config)
-        else:
-            simulation = IceDEM(config, hull_profile=hull_profile,
-                                hull_start=(args.hull_start_x, args.hull_start_y),
-                                hull_velocity=(args.hull_velocity_x, args.hull_velocity_y))
+        hull = read_hull_profile(args.hull_profile) if args.hull_profile else None
+        # the time-step bound must cover the faster of the tool and the hull
+        speed = max(args.speed, math.hypot(args.hull_velocity_x, args.hull_velocity_y), 1e-12)
+        config = DEMConfig(nx=args.nx, ny=args.ny, dt=args.dt, tool_speed=speed,
+                           breaking_strain=args.breaking_strain, shear_breaking_strain=args.shear_breaking_strain,
+                           device=args.device)
+        placement = {} if hull is None else dict(hull_profile=hull, hull_start=(args.hull_start_x, args.hull_start_y),
+                                                 hull_velocity=(args.hull_velocity_x, args.hull_velocity_y))
+        sim = IceDEM(config, **placement)
     except (ValueError, RuntimeError, TypeError) as exc:
         sys.exit(str(exc))
+    # sample at every multiple of save_every and at the last step; the steps in
+    # between run as one kernel launch each
+    stops = sorted(set(range(0, args.steps + 1, args.save_every)) | {args.steps})
+    samples = _Samples(sim, len(stops))
+    done = 0
+    for stop in stops:
+        if stop > done:
+            sim.run(stop - done)
+            done = stop
+        samples.take()
     args.output.mkdir(parents=True, exist_ok=True)
-    frames, velocities, bonds, tool_positions, times = [], [], [], [], []
-    with (args.output / "history.csv").open("w", newline="", encoding="utf-8") as stream:
-        row = simulation.diagnostics()
-        writer = csv.DictWriter(stream, fieldnames=list(row))
-        writer.writeheader()
-        step = 0
-        while step <= args.steps:
-            if step % args.save_every == 0 or step == args.steps:
-                row = simulation.diagnostics()
-                writer.writerow(row)
-                frames.append(simulation.positions.cpu().clone())
-                velocities.append(simulation.velocities.cpu().clone())
-                bonds.append(simulation.alive[simulation.bonded].cpu().clone())
-                tool_positions.append(simulation.tool_position.cpu().clone())
-                times.append(simulation.time)
-            if step == args.steps:
-                break
-            # advance to the next sample point in one kernel launch
-            nxt = min(args.steps, (step // args.save_every + 1) * args.save_every)
-            simulation.run(nxt - step)
-            step = nxt
-    torch.save({
-        "config": asdict(simulation.config),
-        "dt": simulation.dt,
-        "times": torch.tensor(times, dtype=torch.float64),
-        "positions": torch.stack(frames),
-        "velocities": torch.stack(velocities),
-        "bond_pairs": simulation.pairs[simulation.bonded].cpu(),
-        "bond_alive": torch.stack(bonds),
-        "fixed": simulation.fixed.cpu(),
-        "tool_positions": torch.stack(tool_positions),
-        "hull_profile": None if simulation.hull_profile is None else simulation.hull_profile.cpu(),
-        "hull_velocity": simulation.hull_velocity.cpu(),
-    }, args.output / "trajectory.pt")
-    accounting_data = dict(simulation.accounting)
-    accounting_data["total_bonds"] = int(simulation.bonded.sum().item())
-    accounting_data["broken_bonds"] = simulation.broken_bonds
-    accounting_data["failure_energy_sum_J"] = float(simulation.failure_energy_J.sum().item())
-    accounting_data["total_mass_kg"] = float(simulation.config.mass * len(simulation.positions))
-    accounting_data["dt"] = simulation.dt
-    accounting_data["steps"] = simulation.step_count
-    with (args.output / "accounting.json").open("w", encoding="utf-8") as f:
-        f.write(json.dumps(accounting_data, indent=2, sort_keys=True, allow_nan=False))
-    print(f"done: t={simulation.time:.6f} s, dt={simulation.dt:.6g} s, "
-          f"broken bonds={simulation.broken_bonds}/{int(simulation.bonded.sum().item())}; "
+    samples.write_history(args.output / "history.csv")
+    torch.save({"config": asdict(sim.config), "dt": sim.dt,
+                "times": torch.tensor(samples.times, dtype=torch.float64),
+                "positions": samples.positions.cpu(), "velocities": samples.velocities.cpu(),
+                "bond_pairs": sim.pairs[sim.bonded].cpu(), "bond_alive": samples.bonds.cpu(),
+                "fixed": sim.fixed.cpu(), "tool_positions": samples.tool.cpu(),
+                "hull_profile": None if sim.hull_profile is None else sim.hull_profile.cpu(),
+                "hull_velocity": sim.hull_velocity.cpu()}, args.output / "trajectory.pt")
+    total = int(sim.bonded.sum())
+    record = dict(sim.accounting, total_bonds=total, broken_bonds=sim.broken_bonds,
+                  failure_energy_sum_J=float(sim.failure_energy_J.sum()),
+                  total_mass_kg=float(sim.config.mass * len(sim.positions)), dt=sim.dt, steps=sim.step_count)
+    (args.output / "accounting.json").write_text(json.dumps(record, indent=2, sort_keys=True, allow_nan=False),
+                                                 encoding="utf-8")
+    print(f"done: t={sim.time:.6f} s, dt={sim.dt:.6g} s, broken bonds={sim.broken_bonds}/{total}; "
           f"output: {args.output}")
 
 

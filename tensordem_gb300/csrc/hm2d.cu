@@ -212,11 +212,22 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 
 // Step-kernel variants the autotuner chooses from: 0 = one thread per
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
-// block shapes; 4..5 = bulk-copy staging of own state.
-constexpr int kVariants = 6;
+// block shapes; 4..5 = bulk-copy staging of own state; 6 = neighbour window in
+// shared memory (FP32 engines; an FP64 engine runs variant 1's kernel).
+constexpr int kVariants = 7;
+constexpr int kWindowVariant = 6;
 
 template <class T>
 using StepFn = void (*)(Params<T>, Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int);
+
+// The neighbour-window kernel for FP32 engines; variant 1's kernel for FP64.
+template <class T, int MODE, bool F>
+StepFn<T> window_fn() {
+  if constexpr (sizeof(T) == 4)
+    return &force_kernel_win<T, MODE, F>;
+  else
+    return &force_kernel_pf<T, MODE, 256, 3, F>;
+}
 
 template <class T, bool F>
 StepFn<T> step_fn_feat(int variant, int mode) {
@@ -227,6 +238,7 @@ StepFn<T> step_fn_feat(int variant, int mode) {
       case 3: return &force_kernel_pf<T, kPrime, 256, 2, F>;
       case 4: return &force_kernel_bulk<T, kPrime, 256, 3, F>;
       case 5: return &force_kernel_bulk<T, kPrime, 128, 6, F>;
+      case 6: return window_fn<T, kPrime, F>();
       default: return &force_kernel<T, kPrime, F>;
     }
   }
@@ -236,6 +248,7 @@ StepFn<T> step_fn_feat(int variant, int mode) {
     case 3: return &force_kernel_pf<T, kStep, 256, 2, F>;
     case 4: return &force_kernel_bulk<T, kStep, 256, 3, F>;
     case 5: return &force_kernel_bulk<T, kStep, 128, 6, F>;
+    case 6: return window_fn<T, kStep, F>();
     default: return &force_kernel<T, kStep, F>;
   }
 }
@@ -247,7 +260,17 @@ StepFn<T> step_fn(int variant, int mode, bool feat) {
   return feat ? step_fn_feat<T, true>(variant, mode) : step_fn_feat<T, false>(variant, mode);
 }
 
-inline int variant_block(int variant) { return (variant == 2 || variant == 5) ? 128 : 256; }
+template <class T>
+inline int variant_block(int variant) {
+  if (variant == kWindowVariant) return sizeof(T) == 4 ? kWinThreads : 256;
+  return (variant == 2 || variant == 5) ? 128 : 256;
+}
+
+// Dynamic shared memory of a variant's step kernel.
+template <class T>
+inline size_t variant_smem(int variant) {
+  return (variant == kWindowVariant && sizeof(T) == 4) ? kWinSmem : 0;
+}
 
 template <class T>
 struct Engine final : EngineBase {
@@ -324,9 +347,14 @@ struct Engine final : EngineBase {
     nwarp_slots = nblocks * (kThreads / 32);
     for (int v = 1; v < kVariants; ++v) {
       int per_sm = 0;
-      const int bs = variant_block(v);
+      const int bs = variant_block<T>(v);
+      const size_t smem = variant_smem<T>(v);
+      if (smem > 0)
+        for (int mode : {kPrime, kStep})
+          TDEM_CUDA_TRY(&err, cudaFuncSetAttribute(reinterpret_cast<const void*>(step_fn<T>(v, mode, feat())),
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       TDEM_CUDA_TRY(&err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, reinterpret_cast<const void*>(step_fn<T>(v, kStep, feat())), bs, 0));
+                              &per_sm, reinterpret_cast<const void*>(step_fn<T>(v, kStep, feat())), bs, smem));
       const int need = (int)((n + bs - 1) / bs);
       vgrid[v] = std::max(1, std::min(need, per_sm * sms));
       nwarp_slots = std::max(nwarp_slots, vgrid[v] * (bs / 32));
@@ -420,8 +448,8 @@ struct Engine final : EngineBase {
     cudaKernelNodeParams kp = {};
     kp.func = reinterpret_cast<void*>(step_fn<T>(variant, kStep, feat()));
     kp.gridDim = dim3((unsigned)vgrid[variant]);
-    kp.blockDim = dim3((unsigned)variant_block(variant));
-    kp.sharedMemBytes = 0;
+    kp.blockDim = dim3((unsigned)variant_block<T>(variant));
+    kp.sharedMemBytes = (unsigned)variant_smem<T>(variant);
     kp.kernelParams = args;
     cudaGraphNode_t snode;
     if (P.BMAX > 0) {
@@ -508,7 +536,7 @@ struct Engine final : EngineBase {
 
   int prime(cudaStream_t s) {
     launch_strain(s);
-    step_fn<T>(variant, kPrime, feat())<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
+    step_fn<T>(variant, kPrime, feat())<<<vgrid[variant], variant_block<T>(variant), variant_smem<T>(variant), s>>>(P, B, 0, 0, 0, 1);
     launch_rebuild(s);  // runs only if the prime step tripped the trigger
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     primed = true;
@@ -545,7 +573,7 @@ struct Engine final : EngineBase {
     }
     for (long long k = 0; k < n; ++k) {
       launch_strain(s);
-      step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
+      step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block<T>(variant), variant_smem<T>(variant), s>>>(P, B, 0, 0, 0, 1);
       launch_rebuild(s);
     }
     TDEM_CUDA_TRY(&err, cudaGetLastError());
@@ -675,7 +703,7 @@ struct Engine final : EngineBase {
     if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "step before set_state");
     if (!primed) return prime(s);
     launch_strain(s);
-    step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block(variant), 0, s>>>(P, B, 0, 0, 0, 1);
+    step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block<T>(variant), variant_smem<T>(variant), s>>>(P, B, 0, 0, 0, 1);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     return TDEM_OK;
   }
@@ -892,6 +920,27 @@ struct Engine final : EngineBase {
 
 std::string g_hm_create_error;
 
+// Configuration checks shared by tdem_hm_create and the allocation-free entry
+// point (static messages: no heap use). Null when the configuration is valid.
+const char* hm_config_error(const tdem_hm_config* c) {
+  if (c->n < 1) return "n out of range";
+  if (c->max_neighbors < 1 || c->max_neighbors > kMaxSlots) return "max_neighbors must be in 1..24";
+  if (!(c->inertia_factor > 0.0)) return "inertia_factor must be positive";
+  if (c->max_bonds < 0 || c->max_bonds > kMaxBondSlots) return "max_bonds must be in 0..8";
+  if (c->max_bonds > 0 && (!(c->bond_kn > 0) || !(c->bond_ks >= 0) || !(c->bond_damping >= 0) ||
+                           !(c->breaking_strain > 0) || !(c->shear_breaking_strain > 0)))
+    return "invalid bond stiffness, damping or break strain";
+  if (!(c->indenter_radius >= 0)) return "indenter_radius must be >= 0";
+  // cell ids pack cx | cy << 16, and the key space is (tiles_x * tiles_y) << 10
+  if (c->ncx < 1 || c->ncy < 1 || c->ncx > 32768 || c->ncy > 32768) return "cell grid must be 1..32768 per axis";
+  if (!(c->cell > 0) || !(c->skin >= 0) || !(c->dt > 0) || !(c->young > 0) || !(c->poisson > -1.0) ||
+      !(c->poisson < 0.5) || !(c->restitution > 0) || !(c->restitution <= 1) || !(c->mu >= 0) ||
+      !(c->mu_wall >= 0))
+    return "invalid material, cell or time-step parameter";
+  if (c->precision != 32 && c->precision != 64) return "precision must be 32 or 64";
+  return nullptr;
+}
+
 }  // namespace
 
 struct tdem_hm {
@@ -905,24 +954,7 @@ int tdem_hm_create(const tdem_hm_config* c, tdem_hm** out) {
   std::string* err = &g_hm_create_error;
   if (!c || !out) return tdem::fail(err, TDEM_ERR_BADARG, "null argument");
   *out = nullptr;
-  if (c->n < 1) return tdem::fail(err, TDEM_ERR_BADARG, "n out of range");
-  if (c->max_neighbors < 1 || c->max_neighbors > kMaxSlots)
-    return tdem::fail(err, TDEM_ERR_BADARG, "max_neighbors must be in 1..24");
-  if (!(c->inertia_factor > 0.0)) return tdem::fail(err, TDEM_ERR_BADARG, "inertia_factor must be positive");
-  if (c->max_bonds < 0 || c->max_bonds > kMaxBondSlots)
-    return tdem::fail(err, TDEM_ERR_BADARG, "max_bonds must be in 0..8");
-  if (c->max_bonds > 0 && (!(c->bond_kn > 0) || !(c->bond_ks >= 0) || !(c->bond_damping >= 0) ||
-                           !(c->breaking_strain > 0) || !(c->shear_breaking_strain > 0)))
-    return tdem::fail(err, TDEM_ERR_BADARG, "invalid bond stiffness, damping or break strain");
-  if (!(c->indenter_radius >= 0)) return tdem::fail(err, TDEM_ERR_BADARG, "indenter_radius must be >= 0");
-  if (c->ncx < 1 || c->ncy < 1 || c->ncx > 32768 || c->ncy > 32768)
-    return tdem::fail(err, TDEM_ERR_BADARG, "cell grid must be 1..32768 per axis");
-  if (!(c->cell > 0) || !(c->skin >= 0) || !(c->dt > 0) || !(c->young > 0) || !(c->poisson > -1.0) ||
-      !(c->poisson < 0.5) || !(c->restitution > 0) || !(c->restitution <= 1) || !(c->mu >= 0) ||
-      !(c->mu_wall >= 0))
-    return tdem::fail(err, TDEM_ERR_BADARG, "invalid material, cell or time-step parameter");
-  if (c->precision != 32 && c->precision != 64)
-    return tdem::fail(err, TDEM_ERR_BADARG, "precision must be 32 or 64");
+  if (const char* why = hm_config_error(c)) return tdem::fail(err, TDEM_ERR_BADARG, why);
   auto* h = new tdem_hm();
   int rc;
   if (c->precision == 32) {
@@ -1054,6 +1086,83 @@ int tdem_hm_use_graph(tdem_hm* h, int on) {
   return h->e->use_graph(on);
 }
 
+}  // extern "C"
+
+namespace {
+
+// The per-contact law of the step kernel (contact_law, with the effective
+// radius and mass formed as pair_force forms them) on rows of pair states:
+// in row k (16 doubles): overlap delta, unit normal (x, y) from a to b, r_a,
+// r_b, a's vx, vy, omega, b's vx, vy, omega, 1/m_a, 1/m_b, history xi (x, y)
+// in a's orientation, one unused; out row k (8 doubles): force on a (x, y),
+// n x F_a, updated history (x, y), dissipated energy, Hertz and tangential
+// spring energies. A pair without overlap, or of two clamped discs, reports
+// zeros (its history resets).
+template <class T>
+__global__ void contact_law_kernel(Params<T> P, long long count, const double* in, double* out) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const double* r = in + 16 * k;
+  double* o = out + 8 * k;
+  const T delta = (T)r[0], nx = (T)r[1], ny = (T)r[2], ra = (T)r[3], rb = (T)r[4];
+  const V4<T> va{(T)r[5], (T)r[6], (T)r[7], (T)r[11]}, vb{(T)r[8], (T)r[9], (T)r[10], (T)r[12]};
+  if (!(delta > T(0)) || !(va.w + vb.w > T(0))) {
+    for (int q = 0; q < 8; ++q) o[q] = 0.0;
+    return;
+  }
+  T reff, meff;
+  pair_effective<T>(ra, rb, va.w, vb.w, reff, meff);
+  const PairOut<T> c = contact_law<T>(P, delta, nx, ny, reff, meff, ra, rb, va, vb, V2<T>{(T)r[13], (T)r[14]});
+  o[0] = (double)c.fx;
+  o[1] = (double)c.fy;
+  o[2] = (double)c.cr;
+  o[3] = (double)c.xi.x;
+  o[4] = (double)c.xi.y;
+  o[5] = (double)c.diss;
+  o[6] = (double)c.un;
+  o[7] = (double)c.ut;
+}
+
+template <class T>
+int contact_law_run(const tdem_hm_config& cfg, long long count, const double* in, double* out, cudaStream_t s) {
+  Params<T> P{};
+  make_params<T>(cfg, 1, P);
+  double *din = nullptr, *dout = nullptr;
+  cudaError_t e = cudaMalloc(&din, (size_t)count * 16 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&dout, (size_t)count * 8 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, (size_t)count * 16 * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    contact_law_kernel<T><<<(unsigned)((count + 127) / 128), 128, 0, s>>>(P, count, din, dout);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, (size_t)count * 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(din);
+  cudaFree(dout);
+  return e == cudaSuccess ? TDEM_OK : TDEM_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tdem_hm_contact_law(const tdem_hm_config* cfg, int64_t count, const double* in, double* out, void* stream) {
+  g_hm_create_error.clear();
+  if (!cfg || (count > 0 && (!in || !out)) || count < 0)
+    return tdem::fail(&g_hm_create_error, TDEM_ERR_BADARG, "null argument or negative count");
+  if (!(cfg->dt > 0) || !(cfg->young > 0) || !(cfg->poisson > -1.0) || !(cfg->poisson < 0.5) ||
+      !(cfg->restitution > 0) || !(cfg->restitution <= 1) || !(cfg->mu >= 0))
+    return tdem::fail(&g_hm_create_error, TDEM_ERR_BADARG, "invalid material or time-step parameter");
+  if (cfg->precision != 32 && cfg->precision != 64)
+    return tdem::fail(&g_hm_create_error, TDEM_ERR_BADARG, "precision must be 32 or 64");
+  if (count == 0) return TDEM_OK;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int rc = cfg->precision == 32 ? contact_law_run<float>(*cfg, (long long)count, in, out, s)
+                                      : contact_law_run<double>(*cfg, (long long)count, in, out, s);
+  if (rc) return tdem::fail(&g_hm_create_error, rc, "CUDA error in the contact-law evaluation");
+  return TDEM_OK;
+}
+
 int tdem_hm_last_error(const tdem_hm* h, char* buf, size_t len) {
   if (!buf || len == 0) return TDEM_ERR_BADARG;
   const std::string& e = h ? h->e->err : g_hm_create_error;
@@ -1068,13 +1177,13 @@ int tdem_hm_last_error(const tdem_hm* h, char* buf, size_t len) {
 // ===========================================================================
 // Allocation-free contact-force evaluation
 //
-// For callers that must not allocate device memory: code that runs while
-// another solver's CUDA graph is being captured (a cudaMalloc there breaks
-// the capture), host callbacks and real-time coupling loops where an
-// allocation's latency or failure is not acceptable, and plug-ins whose host
-// application owns all device memory. The scratch lives in one file-scope
-// device array that every GPU loading this library holds until the process
-// exits.
+// For callers that must not allocate device memory: plug-ins whose host
+// application owns and budgets all device memory, and real-time coupling
+// loops where an allocation's latency or failure is not acceptable. The
+// scratch lives in one file-scope device array that every GPU loading this
+// library holds until the process exits. Its device address is resolved on a
+// device's first call and kept for the process (a device reset in between
+// would leave it stale).
 // ===========================================================================
 namespace {
 
@@ -1123,8 +1232,14 @@ __global__ void noalloc_clear_kernel(Ctl* ctl, int* cell_count, int* cell_fill, 
 __global__ void noalloc_status_kernel(const Ctl* ctl, int* status_out) { *status_out = ctl->status; }
 
 // Error text into the caller's buffer, without touching the heap.
-int noalloc_fail(char* buf, size_t len, int code, const char* fmt, long long a = 0, long long b = 0) {
-  if (buf && len) snprintf(buf, len, fmt, a, b);
+int noalloc_fail(char* buf, size_t len, int code, const char* fmt, long long a = 0, long long b = 0,
+                 const char* text = nullptr) {
+  if (buf && len) {
+    if (text)
+      snprintf(buf, len, fmt, text);
+    else
+      snprintf(buf, len, fmt, a, b);
+  }
   return code;
 }
 
@@ -1145,18 +1260,23 @@ int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos,
     return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG,
                         "the allocation-free path holds at most %lld discs per call, got %lld",
                         (long long)kNoAllocMaxDiscs, (long long)cfg->n);
-  if (cfg->ncx < 1 || cfg->ncy < 1 || !(cfg->cell > 0) || !(cfg->inertia_factor > 0) || !(cfg->young > 0) ||
-      !(cfg->restitution > 0) || !(cfg->restitution <= 1) || !(cfg->poisson > -1.0) || !(cfg->poisson < 0.5))
-    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG, "invalid cell grid or material");
+  // the engine's own configuration checks (grid, material, skin, dt, friction)
+  if (const char* why = hm_config_error(cfg)) return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG, "%s", 0, 0, why);
+  if (cfg->max_bonds != 0 || cfg->indenter_radius != 0.0)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG,
+                        "the allocation-free path evaluates contacts, walls and gravity only: max_bonds and "
+                        "indenter_radius must be 0");
+  // the key count in 64-bit before any index arithmetic depends on it
+  const long long keys = (long long)((cfg->ncx + 31) / 32) * (long long)((cfg->ncy + 31) / 32) * 1024LL;
+  if (keys > kNoAllocMaxKeys)
+    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG,
+                        "the allocation-free path holds cell grids up to 256 x 256 cells; this grid is %lld x %lld",
+                        (long long)cfg->ncx, (long long)cfg->ncy);
   Params<float> P{};
   make_params<float>(*cfg, kNoAllocSlots, P);
   P.BMAX = 0;  // contacts, walls and gravity only: no bond slots live in the scratch
   P.irad = 0.0f;
   P.load_cap = 0;
-  if (P.nkeys > kNoAllocMaxKeys)
-    return noalloc_fail(err_buf, err_len, TDEM_ERR_BADARG,
-                        "the allocation-free path holds cell grids up to 256 x 256 cells; this grid is %lld x %lld",
-                        (long long)cfg->ncx, (long long)cfg->ncy);
   // device address of the scratch array, resolved once per device
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)

@@ -57,39 +57,65 @@ __device__ __forceinline__ Geo<T> pair_geo(const Params<T>& P, const V4<T>& a, c
   return g;
 }
 
+// Effective radius r_a r_b / (r_a + r_b) and effective mass 1 / (1/m_a + 1/m_b).
+// FP32: reciprocals instead of divides (rcp_rn then a product: <= 1 ulp);
+// _rn products are never fused, so every kernel computes the same bits.
+template <class T>
+__device__ __forceinline__ void pair_effective(T ra, T rb, T inv_ma, T inv_mb, T& reff, T& meff) {
+  if constexpr (sizeof(T) == 4) {
+    reff = __fmul_rn(__fmul_rn(ra, rb), __frcp_rn(ra + rb));
+    meff = __frcp_rn(inv_ma + inv_mb);
+  } else {
+    reff = ra * rb / (ra + rb);
+    meff = T(1) / (inv_ma + inv_mb);
+  }
+}
+
+template <class T>
+__device__ __forceinline__ PairOut<T> contact_law(const Params<T>& P, T delta, T nx, T ny, T reff, T meff, T ra,
+                                                  T rb, const V4<T>& va, const V4<T>& vb, V2<T> xi);
+
 // One active contact (g.d2 < g.rs^2): force on a, torque lever term, history.
 template <class T>
 __device__ __forceinline__ PairOut<T> pair_force(const Params<T>& P, const Geo<T>& g, const V4<T>& pa,
                                                  const V4<T>& va, const V4<T>& pb, const V4<T>& vb,
                                                  V2<T> xi) {
-  PairOut<T> o;
-  o.active = true;
   if (!(va.w + vb.w > T(0))) {  // two clamped discs exchange no force
+    PairOut<T> o;
+    o.active = true;
     o.fx = o.fy = o.cr = o.diss = o.un = o.ut = T(0);
     o.xi = V2<T>{T(0), T(0)};
     return o;
   }
   const T d = dev_sqrt(g.d2);  // IEEE: the overlap rs - d is a small difference
   const T delta = g.rs - d;
-  // FP32: reciprocals instead of divides (rcp_rn then a product: <= 1 ulp);
-  // _rn products are never fused, so every kernel computes the same bits
   T nx, ny, reff, meff;
   if constexpr (sizeof(T) == 4) {
     const T inv_d = __frcp_rn(d);
     nx = __fmul_rn(g.dx, inv_d);
     ny = __fmul_rn(g.dy, inv_d);
-    reff = __fmul_rn(__fmul_rn(pa.z, pb.z), __frcp_rn(g.rs));
-    meff = __frcp_rn(va.w + vb.w);
   } else {
     nx = g.dx / d;
     ny = g.dy / d;
-    reff = pa.z * pb.z / g.rs;
-    meff = T(1) / (va.w + vb.w);
   }
+  pair_effective<T>(pa.z, pb.z, va.w, vb.w, reff, meff);
+  return contact_law<T>(P, delta, nx, ny, reff, meff, pa.z, pb.z, va, vb, xi);
+}
+
+// The contact law proper, from the overlap delta > 0 and the unit normal n
+// from a to b: Hertz normal force with the Tsuji dashpot, clamped at zero;
+// the tangential history incremented by the tangential relative velocity of
+// the contact points and rotated into the current tangent plane; the Mindlin
+// spring S_t xi capped at mu F_n with the state projected onto the cone.
+template <class T>
+__device__ __forceinline__ PairOut<T> contact_law(const Params<T>& P, T delta, T nx, T ny, T reff, T meff, T ra,
+                                                  T rb, const V4<T>& va, const V4<T>& vb, V2<T> xi) {
+  PairOut<T> o;
+  o.active = true;
   const T sq = dev_sqrt(reff * delta);
   const T sn = P.estar2 * sq;
   const T fel = (T(2) / T(3)) * sn * delta;
-  const T wsum = va.z * pa.z + vb.z * pb.z;
+  const T wsum = va.z * ra + vb.z * rb;
   const T vrx = (va.x - vb.x) - wsum * ny;
   const T vry = (va.y - vb.y) + wsum * nx;
   const T vn = vrx * nx + vry * ny;
@@ -200,10 +226,34 @@ __device__ __forceinline__ double block_sum_t(T x) {
 // evaluation (history, integrated state, ledger); kPeek only reports the
 // integer-time velocity, force and energies.
 // ---------------------------------------------------------------------------
+// Where a particle reads its partners' state. GlobalFetch: the current
+// buffers in HBM (through L2). WindowFetch: a shared-memory copy of a window
+// of sorted indices [lo, hi) when the partner lies in it, else HBM; the copy
+// holds the same values, so results are bit-identical either way.
+template <class T>
+struct GlobalFetch {
+  const V4<T>* __restrict__ pos;
+  const V4<T>* __restrict__ vel;
+  __device__ __forceinline__ V4<T> p(int j) const { return pos[j]; }
+  __device__ __forceinline__ V4<T> v(int j) const { return vel[j]; }
+};
+
+template <class T>
+struct WindowFetch {
+  const V4<T>* __restrict__ pos;   // HBM
+  const V4<T>* __restrict__ vel;
+  const V4<T>* spos;               // shared-memory rings: index j sits at (j - off) & mask
+  const V4<T>* svel;
+  int lo, hi, off, mask;
+  __device__ __forceinline__ bool in(int j) const { return (unsigned)(j - lo) < (unsigned)(hi - lo); }
+  __device__ __forceinline__ V4<T> p(int j) const { return in(j) ? spos[(j - off) & mask] : pos[j]; }
+  __device__ __forceinline__ V4<T> v(int j) const { return in(j) ? svel[(j - off) & mask] : vel[j]; }
+};
+
 // One candidate slot of particle i (partner j at position q): contact test,
 // history update in place, force and torque accumulation.
-template <class T, int MODE>
-__device__ __forceinline__ void do_slot(const Params<T>& P, const V4<T>* __restrict__ vel,
+template <class T, int MODE, class F>
+__device__ __forceinline__ void do_slot(const Params<T>& P, const F& fetch,
                                         V2<T>* __restrict__ hist, int i, int j, int s, size_t slot,
                                         const V4<T>& p, const V4<T>& v, const V4<T>& q, unsigned mask,
                                         unsigned& nmask, Acc<T>& fx, Acc<T>& fy, Acc<T>& tq, T& diss, T& un,
@@ -218,7 +268,7 @@ __device__ __forceinline__ void do_slot(const Params<T>& P, const V4<T>* __restr
     if (COMMIT && stored) hist[slot] = V2<T>{T(0), T(0)};  // contact opened: reset
     return;
   }
-  const V4<T> w = vel[j];
+  const V4<T> w = fetch.v(j);
   const V4<T>& va = owner ? v : w;
   const V4<T>& vb = owner ? w : v;
   const V2<T> xi0 = stored ? hist[slot] : V2<T>{T(0), T(0)};
@@ -567,25 +617,23 @@ __device__ __forceinline__ void indenter_contact(const Params<T>& P, long long e
 // walls, and (committing modes) the velocity-Verlet update into the other
 // buffers. p, v, hd are the particle's own loads (already issued).
 // Positions of the first three partners of a list head, issued together.
-template <class T>
-__device__ __forceinline__ void load_head_partners(const V4<T>* __restrict__ pos, const uint4& hd, V4<T>& q0,
-                                                   V4<T>& q1, V4<T>& q2) {
+template <class T, class F>
+__device__ __forceinline__ void load_head_partners(const F& fetch, const uint4& hd, V4<T>& q0, V4<T>& q1,
+                                                   V4<T>& q2) {
   const int cnt = (int)(hd.x & 0xFFu);
-  if (cnt > 0) q0 = pos[hd.y];
-  if (cnt > 1) q1 = pos[hd.z];
-  if (cnt > 2) q2 = pos[hd.w];
+  if (cnt > 0) q0 = fetch.p((int)hd.y);
+  if (cnt > 1) q1 = fetch.p((int)hd.z);
+  if (cnt > 2) q2 = fetch.p((int)hd.w);
 }
 
 // process_particle with the first three partners' positions already loaded.
-template <class T, int MODE, bool FEAT>
-__device__ __forceinline__ void process_particle_q(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i,
-                                                   const V4<T>& p, const V4<T>& v, const uint4& hd,
+template <class T, int MODE, bool FEAT, class F>
+__device__ __forceinline__ void process_particle_q(const Params<T>& P, const Bufs<T>& B, const F& fetch, int sp,
+                                                   int lp, int i, const V4<T>& p, const V4<T>& v, const uint4& hd,
                                                    const V4<T>& q0, const V4<T>& q1, const V4<T>& q2, int primed,
                                                    long long eval, ThreadLedger<T>& L) {
   constexpr bool COMMIT = MODE != kPeek;
   const int n = P.n;
-  const V4<T>* __restrict__ pos = B.pos[sp];
-  const V4<T>* __restrict__ vel = B.vel[sp];
   const unsigned* __restrict__ tail = B.nbr[lp];
   V2<T>* __restrict__ hist = B.hist[lp];
   const int cnt = (int)(hd.x & 0xFFu);
@@ -614,8 +662,8 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
           if (s0 + u < bc) {
             const size_t k = (size_t)(s0 + u) * n + i;
             const int j = (int)(in[u].w & kBondIdx);
-            in[u].q = pos[j];
-            in[u].wv = vel[j];
+            in[u].q = fetch.p(j);
+            in[u].wv = fetch.v(j);
             in[u].sj = B.strain[j];
             in[u].rs = B.bref[lp][k];
             in[u].us = B.bus[lp][k];
@@ -630,18 +678,18 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
     }
   }
   if (cnt > 0)
-    do_slot<T, MODE>(P, vel, hist, i, (int)hd.y, 0, (size_t)i, p, v, q0, mask, nmask, fx, fy, tq, L.diss, L.un,
+    do_slot<T, MODE>(P, fetch, hist, i, (int)hd.y, 0, (size_t)i, p, v, q0, mask, nmask, fx, fy, tq, L.diss, L.un,
                      L.ut, primed);
   if (cnt > 1)
-    do_slot<T, MODE>(P, vel, hist, i, (int)hd.z, 1, (size_t)n + i, p, v, q1, mask, nmask, fx, fy, tq, L.diss,
+    do_slot<T, MODE>(P, fetch, hist, i, (int)hd.z, 1, (size_t)n + i, p, v, q1, mask, nmask, fx, fy, tq, L.diss,
                      L.un, L.ut, primed);
   if (cnt > 2)
-    do_slot<T, MODE>(P, vel, hist, i, (int)hd.w, 2, (size_t)2 * n + i, p, v, q2, mask, nmask, fx, fy, tq, L.diss,
+    do_slot<T, MODE>(P, fetch, hist, i, (int)hd.w, 2, (size_t)2 * n + i, p, v, q2, mask, nmask, fx, fy, tq, L.diss,
                      L.un, L.ut, primed);
   for (int s = kHeadSlots; s < cnt; ++s) {
     const int j = (int)tail[(size_t)(s - kHeadSlots) * n + i];
-    const V4<T> q = pos[j];
-    do_slot<T, MODE>(P, vel, hist, i, j, s, (size_t)s * n + i, p, v, q, mask, nmask, fx, fy, tq, L.diss, L.un,
+    const V4<T> q = fetch.p(j);
+    do_slot<T, MODE>(P, fetch, hist, i, j, s, (size_t)s * n + i, p, v, q, mask, nmask, fx, fy, tq, L.diss, L.un,
                      L.ut, primed);
   }
   if (COMMIT && nmask != mask) B.head[lp][i].x = (hd.x & 0xFFu) | (nmask << 8);
@@ -711,8 +759,9 @@ __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<
                                                  const V4<T>& p, const V4<T>& v, const uint4& hd, int primed,
                                                  long long eval, ThreadLedger<T>& L) {
   V4<T> q0{}, q1{}, q2{};
-  load_head_partners<T>(B.pos[sp], hd, q0, q1, q2);
-  process_particle_q<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, q0, q1, q2, primed, eval, L);
+  const GlobalFetch<T> fetch{B.pos[sp], B.vel[sp]};
+  load_head_partners<T>(fetch, hd, q0, q1, q2);
+  process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, eval, L);
 }
 
 // Control fields a step kernel reads once at its start. disp and target are
@@ -917,13 +966,134 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
   commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
+// Neighbour-window variant (FP32). Each CTA (one per SM) owns a contiguous
+// range of sorted particles and walks it two ring blocks (2 x 256 particles)
+// per iteration. Positions and velocities of a sliding window of sorted
+// indices, the iteration's blocks plus kWinHalo blocks on either side, sit in
+// a shared-memory ring of kWinSlots blocks; one thread streams blocks in ahead
+// of use with cp.async.bulk (each completing on its own mbarrier, up to
+// kWinAhead blocks past the window), and the list heads of the CTA's own
+// blocks likewise into a ring of kWinHeads blocks. After the Morton sort a
+// disc's partners are nearby in index, so partner gathers read shared memory;
+// the few partners outside the window (across a tile row of the cell key)
+// read HBM. Waits are bounded; a CTA whose wait runs out sets kStatusTimeout,
+// drains its copies in flight (bounded) and stops.
+constexpr long long kWaitBudget = 2000000000LL;  // ~1 s of SM clock per wait
+constexpr int kWinBlock = 256;     // particles per ring block
+constexpr int kWinSlots = 16;      // ring blocks (4096 particles)
+constexpr int kWinHalo = 3;        // halo blocks on either side of an iteration
+constexpr int kWinAhead = 6;       // blocks streamed past the window
+constexpr int kWinHeads = 8;       // head-ring blocks
+constexpr int kWinThreads = 2 * kWinBlock;
+constexpr size_t kWinSmem = (size_t)kWinSlots * kWinBlock * 2 * sizeof(V4<float>) +
+                            (size_t)kWinHeads * kWinBlock * sizeof(uint4) + (kWinSlots + kWinHeads) * 8;
+
+template <class T, int MODE, bool FEAT>
+__global__ void __launch_bounds__(kWinThreads, 1) force_kernel_win(Params<T> P, Bufs<T> B,
+                                                                   cudaGraphConditionalHandle h_rebuild,
+                                                                   cudaGraphConditionalHandle h_loop, int use_cond,
+                                                                   int primed) {
+  static_assert(MODE != kPeek && sizeof(T) == 4, "the window variant steps FP32 engines");
+  extern __shared__ __align__(128) unsigned char win_smem[];
+  V4<T>* spos = reinterpret_cast<V4<T>*>(win_smem);
+  V4<T>* svel = spos + kWinSlots * kWinBlock;
+  uint4* shead = reinterpret_cast<uint4*>(svel + kWinSlots * kWinBlock);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(shead + kWinHeads * kWinBlock);  // [slots] pos/vel, [heads] head
+  const StepCtl c = load_step_ctl(B.ctl);
+  const int sp = c.sp, lp = c.lp;
+  const int n = P.n;
+  const int nblk = (n + kWinBlock - 1) / kWinBlock;
+  const int b0 = (int)(((long long)blockIdx.x * nblk) / gridDim.x);
+  const int b1 = (int)(((long long)(blockIdx.x + 1) * nblk) / gridDim.x);
+  const int first = max(0, b0 - kWinHalo);          // first ring block this CTA loads
+  const int last = min(nblk - 1, b1 - 1 + kWinHalo);  // last one
+  const int tid = threadIdx.x;
+  ThreadLedger<T> L;
+  if (tid == 0) {
+    for (int q = 0; q < kWinSlots + kWinHeads; ++q) bulk::mbar_init(&bar[q], 1);
+    bulk::fence_mbar_init();
+  }
+  __syncthreads();
+  int next_pv = first, next_hd = b0;  // next blocks to issue (thread 0)
+  auto issue_upto = [&](int k) {      // iteration at blocks k, k + 1
+    const int pv_end = min(last, k + 1 + kWinHalo + kWinAhead);
+    for (; next_pv <= pv_end; ++next_pv) {
+      const int r = next_pv - first, slot = r & (kWinSlots - 1);
+      const int cnt = min(kWinBlock, n - next_pv * kWinBlock);
+      const uint32_t bytes = (uint32_t)(cnt * sizeof(V4<T>));
+      bulk::mbar_arrive_expect_tx(&bar[slot], 2 * bytes);
+      bulk::copy_g2s(spos + slot * kWinBlock, B.pos[sp] + (size_t)next_pv * kWinBlock, bytes, &bar[slot]);
+      bulk::copy_g2s(svel + slot * kWinBlock, B.vel[sp] + (size_t)next_pv * kWinBlock, bytes, &bar[slot]);
+    }
+    const int hd_end = min(b1 - 1, k + kWinHeads - 1);
+    for (; next_hd <= hd_end; ++next_hd) {
+      const int r = next_hd - b0, slot = r & (kWinHeads - 1);
+      const int cnt = min(kWinBlock, n - next_hd * kWinBlock);
+      const uint32_t bytes = (uint32_t)(cnt * sizeof(uint4));
+      bulk::mbar_arrive_expect_tx(&bar[kWinSlots + slot], bytes);
+      bulk::copy_g2s(shead + slot * kWinBlock, B.head[lp] + (size_t)next_hd * kWinBlock, bytes,
+                     &bar[kWinSlots + slot]);
+    }
+  };
+  if (tid == 0 && b0 < b1) issue_upto(b0);
+  int waited_pv = first - 1;  // highest ring block this thread has seen complete
+  int waited_hd = b0 - 1;     // highest head block this thread has seen complete
+  bool ok = true;
+  for (int k = b0; k < b1; k += 2) {
+    // the window's new blocks and this iteration's heads
+    const int need = min(last, k + 1 + kWinHalo);
+    while (ok && waited_pv < need) {
+      const int r = waited_pv + 1 - first;
+      ok = bulk::mbar_wait_bounded(&bar[r & (kWinSlots - 1)], (uint32_t)((r >> 4) & 1), kWaitBudget);
+      if (ok) ++waited_pv;
+    }
+    while (ok && waited_hd < min(k + 1, b1 - 1)) {
+      const int r = waited_hd + 1 - b0;
+      ok = bulk::mbar_wait_bounded(&bar[kWinSlots + (r & (kWinHeads - 1))], (uint32_t)((r >> 3) & 1), kWaitBudget);
+      if (ok) ++waited_hd;
+    }
+    if (__syncthreads_or(!ok)) break;
+    const int blk = k + (tid >= kWinBlock ? 1 : 0);
+    const int i = blk * kWinBlock + (tid & (kWinBlock - 1));
+    if (blk < b1 && i < n) {
+      const int off = first * kWinBlock;
+      // resident: ring blocks max(first, k - halo) .. min(last, k + 1 + halo)
+      const WindowFetch<T> fetch{B.pos[sp], B.vel[sp], spos, svel, max(first, k - kWinHalo) * kWinBlock,
+                                 min(n, min(last + 1, k + 2 + kWinHalo) * kWinBlock), off,
+                                 kWinSlots * kWinBlock - 1};
+      const V4<T> p = spos[(i - off) & fetch.mask];
+      const V4<T> v = svel[(i - off) & fetch.mask];
+      const uint4 hd = shead[((blk - b0) & (kWinHeads - 1)) * kWinBlock + (tid & (kWinBlock - 1))];
+      V4<T> q0{}, q1{}, q2{};
+      load_head_partners<T>(fetch, hd, q0, q1, q2);
+      process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, c.evals, L);
+    }
+    __syncthreads();  // every thread is done with the slots the next copies overwrite
+    if (tid == 0) issue_upto(k + 2);
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicOr(&B.ctl->status, (int)kStatusTimeout);
+      // drain the copies in flight before the CTA's shared memory is released
+      for (int b = waited_pv + 1; b < next_pv; ++b) {
+        const int r = b - first;
+        bulk::mbar_wait_bounded(&bar[r & (kWinSlots - 1)], (uint32_t)((r >> 4) & 1), kWaitBudget);
+      }
+      for (int b = waited_hd + 1; b < next_hd; ++b) {
+        const int r = b - b0;
+        bulk::mbar_wait_bounded(&bar[kWinSlots + (r & (kWinHeads - 1))], (uint32_t)((r >> 3) & 1), kWaitBudget);
+      }
+    }
+    __syncthreads();
+  }
+  commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
+}
+
 // Bulk-copy variant: each block streams its tiles of own-particle state
 // (position, velocity, list head: 48 B per particle in FP32) from HBM into
 // shared memory with cp.async.bulk, double-buffered on two mbarriers, so the
 // next tile is in flight while the current one is computed. Partner state is
 // gathered from global memory (mostly L2 hits thanks to the cell sort).
-constexpr long long kWaitBudget = 2000000000LL;  // ~1 s of SM clock per wait
-
 template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
 __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bufs<T> B,
                                                                  cudaGraphConditionalHandle h_rebuild,

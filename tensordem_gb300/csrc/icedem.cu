@@ -147,6 +147,123 @@ __device__ inline double2 tool_contact(const Params& P, const Topo& T, double2 p
   return f;
 }
 
+// Distance from a disc centre to the tool at `time`: the circle's centre, or
+// the nearest point of the hull polyline (the first nearest segment wins).
+__device__ inline double tool_distance(const Params& P, const Topo& T, double2 p, double time) {
+  if (P.hull_m == 0) {
+    const double dx = p.x - (P.tool_start_x + time * P.tool_vel_x);
+    const double dy = p.y - (P.tool_start_y + time * P.tool_vel_y);
+    return sqrt(fma(dy, dy, dx * dx));
+  }
+  const double ox = P.hull_start_x + time * P.hull_vel_x;
+  const double oy = P.hull_start_y + time * P.hull_vel_y;
+  double best = 0.0;
+  for (int m = 0; m + 1 < P.hull_m; ++m) {
+    const double ax = T.hull[m].x + ox, ay = T.hull[m].y + oy;
+    const double sx = (T.hull[m + 1].x + ox) - ax, sy = (T.hull[m + 1].y + oy) - ay;
+    double frac = ((p.x - ax) * sx + (p.y - ay) * sy) / (sx * sx + sy * sy);
+    frac = fmin(fmax(frac, 0.0), 1.0);
+    const double dx = p.x - (ax + frac * sx), dy = p.y - (ay + frac * sy);
+    const double d = sqrt(fma(dy, dy, dx * dx));
+    if (m == 0 || d < best) best = d;
+  }
+  return best;
+}
+
+// Stored mechanical energy of a state (the reference's mechanical_energy,
+// dem.py:603-624): kinetic, the springs of the intact bonds (per-bond
+// stiffness when set), the penalty energy of every overlapping pair that is not
+// an intact bond, and the tool's penalty energy. One CTA; every sum in a fixed
+// order. out: kinetic, bond, pair contact, tool contact, total (J).
+__global__ void __launch_bounds__(512) icedem_energy_kernel(Params P, Topo T, const double2* __restrict__ pos,
+                                                            const double2* __restrict__ vel,
+                                                            const bool* __restrict__ alive, double time,
+                                                            double* __restrict__ out) {
+  __shared__ double red[4 * 16];
+  const int n = P.n, tid = threadIdx.x, nt = blockDim.x;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};  // sum |v|^2, bond, sum overlap^2 (pairs), (tool)
+  for (int k = tid; k < n; k += nt) {
+    const double2 v = vel[k];
+    acc[0] += v.x * v.x + v.y * v.y;
+    const double ov = fmax(P.radius + P.tool_radius - tool_distance(P, T, pos[k], time), 0.0);
+    acc[3] += ov * ov;
+  }
+  for (int b = tid; b < P.nbond; b += nt) {
+    if (!alive[T.bpair[b]]) continue;
+    const double2 a = pos[T.bi[b]], c = pos[T.bj[b]];
+    const double dx = c.x - a.x, dy = c.y - a.y;
+    const double ext = sqrt(fma(dy, dy, dx * dx)) - T.rest[b];
+    acc[1] += 0.5 * (T.kcoef ? T.kcoef[b] : P.kb) * (ext * ext);
+  }
+  // every pair (i < j) closer than two radii that is not an intact bond; the
+  // row of disc i starts at pair index i n - i (i + 1) / 2
+  const double reach = 2.0 * P.radius;
+  for (int i = tid; i < n; i += nt) {
+    const double2 a = pos[i];
+    const long long row = (long long)i * n - (long long)i * (i + 1) / 2 - (i + 1);
+    for (int j = i + 1; j < n; ++j) {
+      const double2 c = pos[j];
+      const double dx = c.x - a.x, dy = c.y - a.y;
+      if (fabs(dx) >= reach || fabs(dy) >= reach) continue;
+      const double ov = fmax(reach - sqrt(fma(dy, dy, dx * dx)), 0.0);
+      if (ov > 0.0 && !alive[row + j]) acc[2] += ov * ov;
+    }
+  }
+  double tot[4];
+  block_sum_f64<4>(acc, red, tot);
+  if (tid == 0) {
+    const double kinetic = 0.5 * P.mass * tot[0];
+    const double pair = 0.5 * P.kc * tot[2];
+    const double tool = 0.5 * P.kc * tot[3];
+    out[0] = kinetic;
+    out[1] = tot[1];
+    out[2] = pair;
+    out[3] = tool;
+    out[4] = kinetic + tot[1] + pair + tool;
+  }
+}
+
+// Fragments: connected components of the intact bonds (isolated discs are
+// components of their own), each disc labelled with the smallest disc id of
+// its component. One CTA, parents in shared memory: every intact bond hooks
+// the larger of its two roots under the smaller (atomicMin keeps parents
+// decreasing, so a root is always its component's smallest id), then every
+// parent pointer is jumped to its root; rounds repeat until no bond joins two
+// roots. A component of n discs needs at most n rounds; `*rounds_out` gets the
+// count, or -1 if the bound was reached.
+__global__ void __launch_bounds__(512) icedem_fragment_kernel(Params P, Topo T, const bool* __restrict__ alive,
+                                                              int* __restrict__ label, int* __restrict__ rounds_out) {
+  extern __shared__ int par[];
+  const int n = P.n, tid = threadIdx.x, nt = blockDim.x;
+  for (int k = tid; k < n; k += nt) par[k] = k;
+  __syncthreads();
+  int rounds = 0;
+  bool joined = true;
+  while (joined && rounds <= n) {
+    bool any = false;
+    for (int b = tid; b < P.nbond; b += nt) {
+      if (!alive[T.bpair[b]]) continue;
+      int ra = T.bi[b], rb = T.bj[b];
+      while (par[ra] != ra) ra = par[ra];
+      while (par[rb] != rb) rb = par[rb];
+      if (ra != rb) {
+        atomicMin(&par[max(ra, rb)], min(ra, rb));
+        any = true;
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < n; k += nt) {
+      int r = par[k];
+      while (par[r] != r) r = par[r];
+      par[k] = r;
+    }
+    joined = __syncthreads_or(any) != 0;
+    ++rounds;
+  }
+  for (int k = tid; k < n; k += nt) label[k] = par[k];
+  if (tid == 0) *rounds_out = joined ? -1 : rounds;
+}
+
 // ---------------------------------------------------------------------------
 // The fused step kernel. mode 0: n_steps full steps; mode 1: one force
 // evaluation (dem.py:226-345) written to out_force / out_reaction.
@@ -512,6 +629,8 @@ struct tdem_icedem {
   double2* hull = nullptr;
   double* kcoef = nullptr;  // per-bond stiffness, null unless set
   double* ledger = nullptr;
+  double* energy = nullptr;  // 5 doubles: the energy kernel's output
+  void* scratch = nullptr;   // fragment labels (kMaxDiscs ints) and a round count
   tdem::icedem::Mailbox* mbox = nullptr;
   tdem::icedem::Mailbox* mbox_host = nullptr;
   double* ledger_host = nullptr;
@@ -597,6 +716,8 @@ void tdem_icedem_destroy(tdem_icedem* h) {
   cudaFree(h->hull);
   cudaFree(h->kcoef);
   cudaFree(h->ledger);
+  cudaFree(h->energy);
+  cudaFree(h->scratch);
   cudaFree(h->mbox);
   cudaFreeHost(h->mbox_host);
   cudaFreeHost(h->ledger_host);
@@ -715,6 +836,8 @@ int tdem_icedem_create(const tdem_icedem_config* cfg, const double* x0, tdem_ice
     return rc;
   }
   cudaError_t e = cudaMalloc(&h->mbox, sizeof(Mailbox));
+  if (e == cudaSuccess) e = cudaMalloc(&h->energy, 5 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->scratch, (kMaxDiscs + 1) * sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(h->mbox, 0, sizeof(Mailbox));
   if (e == cudaSuccess) e = cudaMallocHost(&h->mbox_host, sizeof(Mailbox));
   if (e == cudaSuccess) e = cudaMallocHost(&h->ledger_host, TDEM_L_COUNT * sizeof(double));
@@ -802,6 +925,46 @@ int tdem_icedem_step(tdem_icedem* h, const tdem_icedem_state* st, const double* 
 
 int tdem_icedem_steps_done(const tdem_icedem* h) { return h ? h->mbox_host->steps_done : -1; }
 
+int tdem_icedem_fragments(tdem_icedem* h, const void* alive, int32_t* labels_host, void* stream) {
+  using namespace tdem::icedem;
+  if (!h) return TDEM_ERR_BADARG;
+  if (!alive || !labels_host) return tdem::fail(&h->err, TDEM_ERR_BADARG, "null argument");
+  Topo T{h->bi, h->bj, h->bpair, h->rest, h->ref, h->inc_off, h->inc_bond, h->inc_other, h->pinv, h->hull,
+         h->kcoef};
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int* dlabel = reinterpret_cast<int*>(h->scratch);
+  int* drounds = dlabel + kMaxDiscs;
+  icedem_fragment_kernel<<<1, h->threads, (size_t)h->n * sizeof(int), s>>>(h->P, T, static_cast<const bool*>(alive),
+                                                                          dlabel, drounds);
+  TDEM_CUDA_TRY(&h->err, cudaGetLastError());
+  int rounds = 0;
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(labels_host, dlabel, (size_t)h->n * sizeof(int), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(&rounds, drounds, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
+  if (rounds < 0) return tdem::fail(&h->err, TDEM_ERR_CUDA, "fragment labelling did not converge");
+  return TDEM_OK;
+}
+
+int tdem_icedem_energy(tdem_icedem* h, const double* positions, const double* velocities, const void* alive,
+                       double time, double* out_host, void* stream) {
+  using namespace tdem::icedem;
+  if (!h) return TDEM_ERR_BADARG;
+  if (!positions || !velocities || !alive || !out_host)
+    return tdem::fail(&h->err, TDEM_ERR_BADARG, "null argument");
+  Topo T{h->bi, h->bj, h->bpair, h->rest, h->ref, h->inc_off, h->inc_bond, h->inc_other, h->pinv, h->hull,
+         h->kcoef};
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  icedem_energy_kernel<<<1, h->threads, 0, s>>>(h->P, T, reinterpret_cast<const double2*>(positions),
+                                                reinterpret_cast<const double2*>(velocities),
+                                                static_cast<const bool*>(alive), time, h->energy);
+  TDEM_CUDA_TRY(&h->err, cudaGetLastError());
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(out_host, h->energy, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
+  return TDEM_OK;
+}
+
+
+
 int tdem_icedem_read_ledger(tdem_icedem* h, double* out, int count, void* stream) {
   if (!h || !out || count < 0 || count > TDEM_L_COUNT) return TDEM_ERR_BADARG;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -809,6 +972,14 @@ int tdem_icedem_read_ledger(tdem_icedem* h, double* out, int count, void* stream
                                          cudaMemcpyDeviceToHost, s));
   TDEM_CUDA_TRY(&h->err, cudaStreamSynchronize(s));
   std::memcpy(out, h->ledger_host, count * sizeof(double));
+  return TDEM_OK;
+}
+
+int tdem_icedem_ledger_to_device(tdem_icedem* h, double* out_device, void* stream) {
+  if (!h || !out_device) return TDEM_ERR_BADARG;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  TDEM_CUDA_TRY(&h->err, cudaMemcpyAsync(out_device, h->ledger, TDEM_L_COUNT * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, s));
   return TDEM_OK;
 }
 

@@ -37,9 +37,23 @@ _IMPULSE_KEYS = ("external_impulse_Ns", "support_impulse_Ns", "drag_impulse_Ns",
                  "tool_impulse_on_ice_Ns")
 
 
+# Configuration checks: (fields, predicate, message template). The messages
+# are the reference's, which callers match on (src/tensordem/dem.py:37-55).
+_CONFIG_RULES = (
+    (("nx", "ny"), lambda v: not isinstance(v, bool) and isinstance(v, int) and v >= 2,
+     "{} must be an integer >= 2"),
+    (("radius", "thickness", "density", "bond_stiffness", "contact_stiffness", "breaking_strain",
+      "shear_breaking_strain", "tool_radius", "tool_speed"), lambda v: math.isfinite(v) and v > 0,
+     "{} must be finite and positive"),
+    (("contact_damping", "drag", "tool_gap"), lambda v: math.isfinite(v) and v >= 0,
+     "{} must be finite and nonnegative"),
+    (("dt",), lambda v: v is None or (math.isfinite(v) and v > 0), "{} must be finite and positive"),
+)
+
+
 @dataclass(frozen=True)
 class DEMConfig:
-    """Configuration of the 2-D bonded-disc lattice (dem.py:17-72)."""
+    """Configuration of the 2-D bonded-disc lattice (fields and defaults of dem.py:17-35)."""
 
     nx: int = 21
     ny: int = 5
@@ -60,36 +74,136 @@ class DEMConfig:
     fix_edges: bool = True
 
     def __post_init__(self) -> None:
-        for name in ("nx", "ny"):
-            value = getattr(self, name)
-            if isinstance(value, bool) or not isinstance(value, int) or value < 2:
-                raise ValueError(f"{name} must be an integer >= 2")
-        for name in ("radius", "thickness", "density", "bond_stiffness", "contact_stiffness",
-                     "breaking_strain", "shear_breaking_strain", "tool_radius", "tool_speed"):
-            value = getattr(self, name)
-            if not math.isfinite(value) or value <= 0:
-                raise ValueError(f"{name} must be finite and positive")
-        for name in ("contact_damping", "drag", "tool_gap"):
-            value = getattr(self, name)
-            if not math.isfinite(value) or value < 0:
-                raise ValueError(f"{name} must be finite and nonnegative")
-        if self.dt is not None and (not math.isfinite(self.dt) or self.dt <= 0):
-            raise ValueError("dt must be finite and positive")
+        for fields, ok, message in _CONFIG_RULES:
+            for name in fields:
+                if not ok(getattr(self, name)):
+                    raise ValueError(message.format(name))
 
     @property
     def mass(self) -> float:
+        """Disc mass rho pi r^2 t (kg)."""
         return self.density * math.pi * self.radius**2 * self.thickness
 
     @property
     def recommended_dt(self) -> float:
-        # dem.py:61-72: bounds all N-1 possible pair contacts plus the tool.
-        neighbors = self.nx * self.ny - 1
-        stiffness = (2 * neighbors + 1) * max(self.bond_stiffness, self.contact_stiffness)
-        damping = (2 * neighbors + 1) * self.contact_damping + self.drag
-        elastic_dt = 0.2 * math.sqrt(self.mass / stiffness)
-        damping_dt = 0.2 * self.mass / damping if damping else math.inf
-        travel_dt = 0.1 * self.radius / self.tool_speed
-        return min(elastic_dt, damping_dt, travel_dt)
+        """The reference's conservative step (dem.py:61-72): the smallest of an
+        elastic bound that assumes every other disc may touch (2 (N - 1) + 1
+        springs at the stiffer constant), the matching damping bound, and a
+        tenth of a radius of tool travel."""
+        springs = 2 * (self.nx * self.ny - 1) + 1
+        k_max = springs * max(self.bond_stiffness, self.contact_stiffness)
+        c_sum = springs * self.contact_damping + self.drag
+        bounds = [0.2 * math.sqrt(self.mass / k_max), 0.1 * self.radius / self.tool_speed]
+        if c_sum:
+            bounds.insert(1, 0.2 * self.mass / c_sum)
+        return min(bounds)
+
+
+def _square_lattice(config: DEMConfig, device) -> dict:
+    """The reference's lattice (dem.py:105-131): nx x ny discs on a square grid
+    of spacing 2r centred on x = 0, row by row from y = 0; every pair (i < j)
+    in upper-triangle order with its initial distance and unit normal; the two
+    end columns fixed when ``fix_edges``. Distances use torch's vector norm,
+    as the reference does."""
+    nx, ny, spacing = config.nx, config.ny, 2 * config.radius
+    column = torch.arange(nx, dtype=torch.float64, device=device).repeat(ny)
+    row = torch.arange(ny, dtype=torch.float64, device=device).repeat_interleave(nx)
+    positions = torch.stack((column - (nx - 1) / 2, row), dim=1) * spacing
+    count = nx * ny
+    pairs = torch.triu_indices(count, count, offset=1, device=device).T
+    chord = positions[pairs[:, 1]] - positions[pairs[:, 0]]
+    length = torch.linalg.vector_norm(chord, dim=1)
+    edge = (column == 0) | (column == nx - 1)
+    return dict(positions=positions, pairs=pairs, length=length, normal=chord / length[:, None],
+                fixed=edge if config.fix_edges else torch.zeros_like(edge))
+
+
+def _check_hull(profile, start, velocity, device):
+    """Validated hull placement and polyline (dem.py:146-170 semantics)."""
+    start = torch.tensor(start, dtype=torch.float64, device=device)
+    velocity = torch.tensor(velocity, dtype=torch.float64, device=device)
+    if not bool(torch.isfinite(start).all() and torch.isfinite(velocity).all()):
+        raise ValueError("hull_start and hull_velocity must be finite")
+    if profile is None:
+        return None, start, velocity
+    if not isinstance(profile, torch.Tensor):
+        raise TypeError("hull_profile must be a torch.Tensor with shape (M, 2)")
+    if profile.ndim != 2 or profile.shape[1] != 2 or profile.shape[0] < 2:
+        raise ValueError("hull_profile must have shape (M, 2), M >= 2")
+    profile = profile.to(device=device, dtype=torch.float64).clone()
+    if not bool(torch.isfinite(profile).all()):
+        raise ValueError("hull_profile must contain only finite values")
+    seg = torch.linalg.vector_norm(profile[1:] - profile[:-1], dim=1)
+    if bool((seg <= torch.finfo(torch.float64).eps).any()):
+        raise ValueError("hull_profile must not contain zero-length segments")
+    return profile, start, velocity
+
+
+_RESTART_KEYS = frozenset({
+    "schema", "config", "dt_s", "time_s", "step_count", "positions_m", "velocities_m_s", "initial_positions_m",
+    "fixed", "alive", "failure_mode", "failure_time_s", "failure_extension_m", "failure_energy_J",
+    "tool_start_m", "tool_velocity_m_s", "hull_profile_m", "hull_start_m", "hull_velocity_m_s", "accounting",
+    "last_step"})
+
+
+def _restart_array(values, kind, device):
+    """A restart list as a device tensor of its kind, or None if it is not one:
+    "f64" finite float64, "bool" a list of Python bools, "mode" uint8."""
+    if kind == "bool":
+        if not isinstance(values, list) or any(type(v) is not bool for v in values):
+            return None
+        return torch.tensor(values, dtype=torch.bool, device=device)
+    t = torch.as_tensor(values, dtype=torch.uint8 if kind == "mode" else torch.float64, device=device)
+    if kind == "f64" and not bool(torch.isfinite(t).all()):
+        return None
+    return t
+
+
+def _intact(sim):
+    return sim.failure_mode == 0
+
+
+# Restored arrays in restore order (later checks see earlier fields already
+# restored): snapshot key, IceDEM attribute, kind, [(check(sim, value), message)].
+_RESTART_ARRAYS = (
+    ("positions_m", "positions", "f64", ()),
+    ("velocities_m_s", "velocities", "f64", ()),
+    ("initial_positions_m", "initial_positions", "f64",
+     ((lambda sim, v: torch.equal(v, sim.initial_positions), "reference lattice mismatch"),)),
+    ("tool_start_m", "tool_start", "f64", ()),
+    ("tool_velocity_m_s", "tool_velocity", "f64", ()),
+    ("fixed", "fixed", "bool", ((lambda sim, v: torch.equal(v, sim.fixed), "fixed boundary mismatch"),)),
+    ("alive", "alive", "bool", ((lambda sim, v: not bool((v & ~sim.bonded).any()), "nonbonded pair cannot be alive"),)),
+    ("failure_mode", "failure_mode", "mode",
+     ((lambda sim, v: not bool((v > 3).any()) and not bool((v[~sim.bonded] != 0).any()),
+       "invalid restart failure modes"),
+      (lambda sim, v: torch.equal(v > 0, sim.bonded & ~sim.alive), "failure ledger inconsistent with bond state"))),
+    ("failure_time_s", "failure_time_s", "f64",
+     ((lambda sim, v: not bool((v[~_intact(sim)] < 0).any()), "failed bond has invalid failure time"),
+      (lambda sim, v: not bool((v[_intact(sim)] != -1).any()), "intact bond has failure time"))),
+    ("failure_extension_m", "failure_extension_m", "f64", ()),
+    ("failure_energy_J", "failure_energy_J", "f64",
+     ((lambda sim, v: not bool((v < 0).any()), "negative restart failure energy"),
+      (lambda sim, v: not bool((v[_intact(sim)] != 0).any()), "intact bond has failure energy"))),
+)
+
+
+def _restart_accounting(accounting) -> dict:
+    """The restart's accounting dict, checked against the ledger's channels;
+    channels added after a checkpoint was written restore as zero."""
+    expected = set(_ENERGY_KEYS) | set(_IMPULSE_KEYS)
+    if not isinstance(accounting, dict) or set(accounting) - expected or \
+            (expected - set(accounting)) - ADDITIVE_ACCOUNTING_KEYS:
+        raise ValueError("restart accounting fields mismatch")
+    out = {key: 0.0 for key in expected - set(accounting)}
+    for key, value in accounting.items():
+        t = torch.as_tensor(value, dtype=torch.float64)
+        if tuple(t.shape) != ((2,) if "impulse" in key else ()) or not bool(torch.isfinite(t).all()):
+            raise ValueError("invalid restart accounting")
+        if key == "fracture_release_J" and value < 0:
+            raise ValueError("negative fracture release")
+        out[key] = copy.deepcopy(value)
+    return out
 
 
 class _Handle:
@@ -130,60 +244,42 @@ class IceDEM:
             raise ValueError("tensordem_gb300.IceDEM runs on CUDA devices only")
         if not torch.cuda.is_available():
             raise ValueError("CUDA requested but unavailable")
-        self.dt = config.dt if config.dt is not None else config.recommended_dt
-        if self.dt > config.recommended_dt:
-            raise ValueError(f"dt exceeds conservative limit {config.recommended_dt:.6g} s")
+        limit = config.recommended_dt
+        self.dt = limit if config.dt is None else config.dt
+        if self.dt > limit:
+            raise ValueError(f"dt exceeds conservative limit {limit:.6g} s")
         dev = self.device
-        x = torch.arange(config.nx, dtype=torch.float64, device=dev)
-        y = torch.arange(config.ny, dtype=torch.float64, device=dev)
-        yy, xx = torch.meshgrid(y, x, indexing="ij")
-        self.positions = torch.stack((xx.flatten() - (config.nx - 1) / 2, yy.flatten()), dim=1) \
-            * (2 * config.radius)
+        self.hull_profile, self.hull_start, self.hull_velocity = _check_hull(hull_profile, hull_start,
+                                                                             hull_velocity, dev)
+        lattice = _square_lattice(config, dev)
+        self.positions = lattice["positions"]
         self.initial_positions = self.positions.clone()
         self.velocities = torch.zeros_like(self.positions)
-        n = len(self.positions)
-        self.fixed = torch.zeros(n, dtype=torch.bool, device=dev)
-        if config.fix_edges:
-            self.fixed = (xx.flatten() == 0) | (xx.flatten() == config.nx - 1)
-        self.pairs = torch.triu_indices(n, n, offset=1, device=dev).T
-        delta = self.positions[self.pairs[:, 1]] - self.positions[self.pairs[:, 0]]
-        distances = torch.linalg.vector_norm(delta, dim=1)
-        self.initial_normals = delta / distances[:, None]
-        self.bonded = distances <= 2 * config.radius * math.sqrt(2) * (1 + 1e-10)
+        self.fixed = lattice["fixed"]
+        self.pairs = lattice["pairs"]
+        self.rest_lengths = lattice["length"]
+        self.initial_normals = lattice["normal"]
+        top = (config.ny - 1) * 2 * config.radius + config.radius
+        self.tool_start = torch.tensor([0.0, top + config.tool_radius + config.tool_gap], dtype=torch.float64,
+                                       device=dev)
+        self.tool_velocity = torch.tensor([0.0, -config.tool_speed], dtype=torch.float64, device=dev)
+        # the native engine builds the bond topology (bonds: pairs at most
+        # 2 r sqrt(2) apart); the Python side mirrors its pair list as a mask
+        self._build_native()
+        npair = len(self.pairs)
+        self.bonded = torch.zeros(npair, dtype=torch.bool, device=dev)
+        self.bonded[self._bond_pair_index.to(dev)] = True
         self.bond_indices = self.pairs[self.bonded]
         self.reference_bond_vectors = (self.initial_positions[self.bond_indices[:, 1]]
                                        - self.initial_positions[self.bond_indices[:, 0]])
-        self.rest_lengths = distances.clone()
         self.alive = self.bonded.clone()
-        p = len(self.pairs)
-        self.failure_mode = torch.zeros(p, dtype=torch.uint8, device=dev)
-        self.failure_time_s = torch.full((p,), -1.0, dtype=torch.float64, device=dev)
-        self.failure_extension_m = torch.zeros(p, dtype=torch.float64, device=dev)
-        self.failure_energy_J = torch.zeros(p, dtype=torch.float64, device=dev)
+        self.failure_mode = torch.zeros(npair, dtype=torch.uint8, device=dev)
+        self.failure_time_s = torch.full((npair,), -1.0, dtype=torch.float64, device=dev)
+        self.failure_extension_m = torch.zeros(npair, dtype=torch.float64, device=dev)
+        self.failure_energy_J = torch.zeros(npair, dtype=torch.float64, device=dev)
         self.time = 0.0
         self.step_count = 0
         self._last_step: dict | None = {}
-        self.tool_start = torch.tensor(
-            [0.0, (config.ny - 1) * 2 * config.radius + config.radius + config.tool_radius
-             + config.tool_gap], dtype=torch.float64, device=dev)
-        self.tool_velocity = torch.tensor([0.0, -config.tool_speed], dtype=torch.float64, device=dev)
-        self.hull_profile = None
-        self.hull_start = torch.tensor(hull_start, dtype=torch.float64, device=dev)
-        self.hull_velocity = torch.tensor(hull_velocity, dtype=torch.float64, device=dev)
-        if not bool(torch.isfinite(self.hull_start).all() and torch.isfinite(self.hull_velocity).all()):
-            raise ValueError("hull_start and hull_velocity must be finite")
-        if hull_profile is not None:
-            if not isinstance(hull_profile, torch.Tensor):
-                raise TypeError("hull_profile must be a torch.Tensor with shape (M, 2)")
-            if hull_profile.ndim != 2 or hull_profile.shape[1] != 2 or hull_profile.shape[0] < 2:
-                raise ValueError("hull_profile must have shape (M, 2), M >= 2")
-            self.hull_profile = hull_profile.to(device=dev, dtype=torch.float64).clone()
-            if not bool(torch.isfinite(self.hull_profile).all()):
-                raise ValueError("hull_profile must contain only finite values")
-            if bool((torch.linalg.vector_norm(self.hull_profile[1:] - self.hull_profile[:-1], dim=1)
-                     <= torch.finfo(self.hull_profile.dtype).eps).any()):
-                raise ValueError("hull_profile must not contain zero-length segments")
-        self._build_native()
 
     # ------------------------------------------------------------------ native
     def _build_native(self) -> None:
@@ -194,27 +290,21 @@ class IceDEM:
         c.bond_stiffness, c.contact_stiffness = cfg.bond_stiffness, cfg.contact_stiffness
         c.breaking_strain, c.shear_breaking_strain = cfg.breaking_strain, cfg.shear_breaking_strain
         c.contact_damping, c.drag, c.tool_radius, c.dt = cfg.contact_damping, cfg.drag, cfg.tool_radius, self.dt
-        ts, tv = self.tool_start.tolist(), self.tool_velocity.tolist()
-        c.tool_start[0], c.tool_start[1] = ts
-        c.tool_velocity[0], c.tool_velocity[1] = tv
-        hs, hv = self.hull_start.tolist(), self.hull_velocity.tolist()
-        c.hull_start[0], c.hull_start[1] = hs
-        c.hull_velocity[0], c.hull_velocity[1] = hv
+        c.tool_start[0], c.tool_start[1] = self.tool_start.tolist()
+        c.tool_velocity[0], c.tool_velocity[1] = self.tool_velocity.tolist()
+        c.hull_start[0], c.hull_start[1] = self.hull_start.tolist()
+        c.hull_velocity[0], c.hull_velocity[1] = self.hull_velocity.tolist()
         self._hull_host = None
+        c.hull_vertices = 0
         if self.hull_profile is not None:
             self._hull_host = self.hull_profile.cpu().contiguous()
             c.hull_vertices = self._hull_host.shape[0]
             c.hull_profile_host = C.cast(self._hull_host.data_ptr(), C.POINTER(C.c_double))
-        else:
-            c.hull_vertices = 0
         self._handle = _Handle(c, self.initial_positions.cpu())
         nb = _lib.lib().tdem_icedem_num_bonds(self._handle.ptr)
-        native = torch.empty(nb, dtype=torch.int64)
-        _lib.lib().tdem_icedem_bond_pairs(self._handle.ptr,
-                                          C.cast(native.data_ptr(), C.POINTER(C.c_int64)))
-        expect = torch.nonzero(self.bonded).flatten().cpu()
-        if not torch.equal(native, expect):
-            raise RuntimeError("native bond topology disagrees with the lattice bond mask")
+        index = torch.empty(nb, dtype=torch.int64)
+        _lib.lib().tdem_icedem_bond_pairs(self._handle.ptr, C.cast(index.data_ptr(), C.POINTER(C.c_int64)))
+        self._bond_pair_index = index
 
     def _tensor(self, name: str, dtype: torch.dtype, shape: tuple) -> torch.Tensor:
         t = getattr(self, name)
@@ -411,49 +501,40 @@ class IceDEM:
                     thickness_m=self.config.thickness)
 
     def fracture_events(self) -> list[dict]:
-        """Deterministic per-bond failure records in SI units (dem.py:437-460)."""
-        labels = {1: "tensile", 2: "shear", 3: "mixed"}
-        mode = self.failure_mode.cpu()
-        idx = torch.nonzero(mode > 0, as_tuple=False).flatten().tolist()
-        pairs = self.pairs.cpu()
-        pos = self.positions.cpu()
-        t = self.failure_time_s.cpu()
-        ext = self.failure_extension_m.cpu()
-        en = self.failure_energy_J.cpu()
-        events = []
-        for p in idx:
-            i, j = pairs[p].tolist()
-            events.append({
-                "pair_index": p, "particle_i": i, "particle_j": j,
-                "time_s": float(t[p]), "mode": labels[int(mode[p])],
-                "midpoint_m": ((pos[i] + pos[j]) * 0.5).tolist(),
-                "extension_at_failure_m": float(ext[p]),
-                "released_spring_energy_J": float(en[p]),
-            })
-        return events
+        """Per-bond failure records in SI units, in pair order (the records of
+        dem.py:437-460). The broken bonds, their endpoints, midpoints and
+        failure data are gathered on the device and copied once."""
+        broken = torch.nonzero(self.failure_mode > 0).flatten()
+        ends = self.pairs[broken]
+        mid = 0.5 * (self.positions[ends[:, 0]] + self.positions[ends[:, 1]])
+        ints = torch.cat((broken[:, None], ends, self.failure_mode[broken, None].long()), dim=1).cpu().tolist()
+        reals = torch.stack((self.failure_time_s[broken], mid[:, 0], mid[:, 1], self.failure_extension_m[broken],
+                             self.failure_energy_J[broken]), dim=1).cpu().tolist()
+        names = {1: "tensile", 2: "shear", 3: "mixed"}
+        return [{"pair_index": p, "particle_i": i, "particle_j": j, "time_s": t, "mode": names[m],
+                 "midpoint_m": [mx, my], "extension_at_failure_m": e, "released_spring_energy_J": w}
+                for (p, i, j, m), (t, mx, my, e, w) in zip(ints, reals)]
 
     def fragments(self) -> list[dict]:
         """Connected components of the surviving bonds, isolated discs included,
-        ordered by their smallest particle id (the output of dem.py:462-484):
-        particle ids, mass, centroid and mean velocity per fragment."""
-        from scipy.sparse import coo_matrix
-        from scipy.sparse.csgraph import connected_components
-
+        ordered by their smallest disc id (the output of dem.py:462-484): disc
+        ids, mass, centroid and mean velocity of each. The components come from
+        a union-find kernel over the intact bonds (``tdem_icedem_fragments``);
+        the per-fragment means are device reductions."""
         n = len(self.positions)
-        ij = self.pairs[self.alive].cpu().numpy().reshape(-1, 2)
-        graph = coo_matrix((np.ones(len(ij)), (ij[:, 0], ij[:, 1])), shape=(n, n))
-        _, label = connected_components(graph, directed=False)
-        pos = self.positions.cpu()
-        vel = self.velocities.cpu()
-        members: dict[int, list[int]] = {}
-        for i, c in enumerate(label.tolist()):  # ascending i: member lists come out sorted
-            members.setdefault(c, []).append(i)
-        result = []
-        for ids in sorted(members.values(), key=lambda m: m[0]):
-            result.append(dict(particle_ids=ids, mass_kg=len(ids) * self.config.mass,
-                               centroid_m=pos[ids].mean(0).tolist(),
-                               mean_velocity_m_s=vel[ids].mean(0).tolist()))
-        return result
+        labels = np.empty(n, dtype=np.int32)
+        alive = self._tensor("alive", torch.bool, (len(self.pairs),))
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        rc = _lib.lib().tdem_icedem_fragments(self._handle.ptr, alive.data_ptr(), labels.ctypes.data, stream)
+        _lib.check(rc, self._handle.ptr, "tdem_icedem_fragments")
+        roots, inverse, counts = torch.unique(torch.from_numpy(labels).to(self.device, torch.int64),
+                                              return_inverse=True, return_counts=True)
+        sums = torch.zeros((len(roots), 4), dtype=torch.float64, device=self.device)
+        sums.index_add_(0, inverse, torch.cat((self.positions, self.velocities), dim=1))
+        means = (sums / counts[:, None]).cpu().tolist()
+        members = np.split(np.argsort(labels, kind="stable"), np.cumsum(counts.cpu().numpy())[:-1])
+        return [dict(particle_ids=ids.tolist(), mass_kg=len(ids) * self.config.mass, centroid_m=m[:2],
+                     mean_velocity_m_s=m[2:]) for ids, m in zip(members, means)]
 
     def snapshot(self) -> dict:
         """Complete JSON restart (schema tensordem.restart/1, dem.py:486-502)."""
@@ -472,122 +553,60 @@ class IceDEM:
 
     @classmethod
     def from_snapshot(cls, state: dict, *, device: str | None = None) -> "IceDEM":
-        """Fail closed on missing fields, incompatible topology or nonfinite data (dem.py:504-601)."""
+        """Restore a tensordem.restart/1 record; fail closed (ValueError) on a
+        missing or unknown field, an incompatible lattice or a non-finite or
+        inconsistent value (the checks of dem.py:504-601, driven by the field
+        table ``_RESTART_ARRAYS``)."""
         if not isinstance(state, dict) or state.get("schema") != "tensordem.restart/1":
             raise ValueError("unsupported DEM restart schema")
-        required = {"schema", "config", "dt_s", "time_s", "step_count", "positions_m",
-                    "velocities_m_s", "initial_positions_m", "fixed", "alive", "failure_mode",
-                    "failure_time_s", "failure_extension_m", "failure_energy_J", "tool_start_m",
-                    "tool_velocity_m_s", "hull_profile_m", "hull_start_m", "hull_velocity_m_s",
-                    "accounting", "last_step"}
-        if set(state) != required:
+        if set(state) != _RESTART_KEYS:
             raise ValueError("restart fields missing or unknown")
         cfg = dict(state["config"])
         if device is not None:
             cfg["device"] = device
         if str(cfg.get("device", "cuda")).startswith("cpu"):
             cfg["device"] = "cuda"
-        config = DEMConfig(**cfg)
         hull = state["hull_profile_m"]
-        result = cls(config, hull_profile=None if hull is None else torch.tensor(hull, dtype=torch.float64),
-                     hull_start=state["hull_start_m"], hull_velocity=state["hull_velocity_m_s"])
-        if state["dt_s"] != result.dt or not math.isfinite(state["time_s"]) or state["time_s"] < 0:
+        sim = cls(DEMConfig(**cfg), hull_profile=None if hull is None else torch.tensor(hull, dtype=torch.float64),
+                  hull_start=state["hull_start_m"], hull_velocity=state["hull_velocity_m_s"])
+        t, count = state["time_s"], state["step_count"]
+        if state["dt_s"] != sim.dt or not math.isfinite(t) or t < 0:
             raise ValueError("invalid restart time or timestep")
-        count = state["step_count"]
         if isinstance(count, bool) or not isinstance(count, int) or count < 0:
             raise ValueError("invalid restart step_count")
-        if abs(state["time_s"] - count * result.dt) > 1e-10 * max(1.0, state["time_s"]):
+        if abs(t - count * sim.dt) > 1e-10 * max(1.0, t):
             raise ValueError("restart time inconsistent with step count")
-        for key, attribute in (("positions_m", "positions"), ("velocities_m_s", "velocities"),
-                               ("initial_positions_m", "initial_positions"),
-                               ("tool_start_m", "tool_start"), ("tool_velocity_m_s", "tool_velocity")):
-            original = getattr(result, attribute)
-            tensor = torch.tensor(state[key], dtype=torch.float64, device=result.device)
-            if tensor.shape != original.shape or not bool(torch.isfinite(tensor).all()):
+        for key, attr, kind, checks in _RESTART_ARRAYS:
+            value = _restart_array(state[key], kind, sim.device)
+            if value is None or value.shape != getattr(sim, attr).shape:
                 raise ValueError(f"invalid restart {key}")
-            if attribute == "initial_positions" and not torch.equal(tensor, original):
-                raise ValueError("reference lattice mismatch")
-            setattr(result, attribute, tensor)
-        for key in ("fixed", "alive"):
-            values = state[key]
-            if not isinstance(values, list) or any(type(v) is not bool for v in values):
-                raise ValueError(f"invalid boolean restart {key}")
-            tensor = torch.tensor(values, dtype=torch.bool, device=result.device)
-            if tensor.shape != getattr(result, key).shape:
-                raise ValueError(f"invalid restart {key} shape")
-            if key == "alive" and bool((tensor & ~result.bonded).any()):
-                raise ValueError("nonbonded pair cannot be alive")
-            if key == "fixed" and not torch.equal(tensor, result.fixed):
-                raise ValueError("fixed boundary mismatch")
-            setattr(result, key, tensor)
-        for key in ("failure_mode", "failure_time_s", "failure_extension_m", "failure_energy_J"):
-            dtype = torch.uint8 if key == "failure_mode" else torch.float64
-            tensor = torch.as_tensor(state[key], dtype=dtype, device=result.device)
-            if tensor.shape != getattr(result, key).shape:
-                raise ValueError(f"invalid restart {key} shape")
-            if key == "failure_mode":
-                if bool((tensor > 3).any()) or bool((tensor[~result.bonded] != 0).any()):
-                    raise ValueError("invalid restart failure modes")
-                if not torch.equal(tensor > 0, result.bonded & ~result.alive):
-                    raise ValueError("failure ledger inconsistent with bond state")
-            else:
-                if not bool(torch.isfinite(tensor).all()):
-                    raise ValueError(f"nonfinite restart {key}")
-                if key == "failure_time_s" and bool((tensor[result.failure_mode > 0] < 0).any()):
-                    raise ValueError("failed bond has invalid failure time")
-                if key == "failure_time_s" and bool((tensor[result.failure_mode == 0] != -1).any()):
-                    raise ValueError("intact bond has failure time")
-                if key == "failure_energy_J" and bool((tensor < 0).any()):
-                    raise ValueError("negative restart failure energy")
-                if key == "failure_energy_J" and bool((tensor[result.failure_mode == 0] != 0).any()):
-                    raise ValueError("intact bond has failure energy")
-            setattr(result, key, tensor)
-        if not torch.equal(result.positions[result.fixed], result.initial_positions[result.fixed]) or \
-                bool((result.velocities[result.fixed] != 0).any()):
+            for check, message in checks:
+                if not check(sim, value):
+                    raise ValueError(message)
+            setattr(sim, attr, value)
+        pinned = sim.fixed
+        if not torch.equal(sim.positions[pinned], sim.initial_positions[pinned]) or \
+                bool((sim.velocities[pinned] != 0).any()):
             raise ValueError("fixed particle state mismatch")
-        accounting = state["accounting"]
-        expected = set(_ENERGY_KEYS) | set(_IMPULSE_KEYS)
-        missing = expected - set(accounting)
-        if missing - ADDITIVE_ACCOUNTING_KEYS:
-            raise ValueError("restart accounting fields mismatch")
-        if set(accounting) - expected:
-            raise ValueError("restart accounting fields mismatch")
-        for key, value in accounting.items():
-            tensor = torch.as_tensor(value, dtype=torch.float64)
-            expected_shape = (2,) if "impulse" in key else ()
-            if tuple(tensor.shape) != expected_shape or not bool(torch.isfinite(tensor).all()):
-                raise ValueError("invalid restart accounting")
-            if key == "fracture_release_J" and value < 0:
-                raise ValueError("negative fracture release")
+        sim.accounting = _restart_accounting(state["accounting"])
         json.dumps(state["last_step"], allow_nan=False)
-        acc = copy.deepcopy(accounting)
-        for key in missing:
-            acc[key] = 0.0
-        result.accounting = acc
-        result.last_step = copy.deepcopy(state["last_step"])
-        result.time, result.step_count = state["time_s"], count
-        return result
+        sim.last_step = copy.deepcopy(state["last_step"])
+        sim.time, sim.step_count = t, count
+        return sim
 
     @torch.no_grad()
     def mechanical_energy(self) -> dict:
-        """Actual current spring/contact potential; does not advance failure (dem.py:603-624)."""
-        delta = self.positions[self.pairs[:, 1]] - self.positions[self.pairs[:, 0]]
-        distances = torch.linalg.vector_norm(delta, dim=1)
-        extension = distances - self.rest_lengths
-        overlap = (2 * self.config.radius - distances).clamp_min(0)
-        bond = 0.5 * self.config.bond_stiffness * extension[self.alive].square().sum()
-        contact = 0.5 * self.config.contact_stiffness * overlap[~self.alive].square().sum()
-        if self.hull_profile is None:
-            distance = torch.linalg.vector_norm(self.positions - self.tool_position, dim=1)
-        else:
-            vertices = self.hull_profile + self.tool_position
-            segments = vertices[1:] - vertices[:-1]
-            rel = self.positions[:, None] - vertices[None, :-1]
-            fraction = ((rel * segments).sum(2) / segments.square().sum(1)).clamp(0, 1)
-            nearest = vertices[None, :-1] + fraction[:, :, None] * segments
-            distance = torch.linalg.vector_norm(self.positions[:, None] - nearest, dim=2).min(1).values
-        tool_overlap = (self.config.radius + self.config.tool_radius - distance).clamp_min(0)
-        tool = 0.5 * self.config.contact_stiffness * tool_overlap.square().sum()
-        kinetic = 0.5 * self.config.mass * self.velocities.square().sum()
-        return dict(kinetic_J=float(kinetic), bond_J=float(bond), pair_contact_J=float(contact),
-                    tool_contact_J=float(tool), mechanical_J=float(kinetic + bond + contact + tool))
+        """Stored energy of the current state without advancing failure
+        (the record of dem.py:603-624), summed on the device by
+        ``tdem_icedem_energy``: kinetic, intact-bond springs, penalty energy
+        of overlapping pairs that are not intact bonds, tool penalty energy."""
+        pos, vel = self._tensor("positions", torch.float64, tuple(self.initial_positions.shape)), \
+            self._tensor("velocities", torch.float64, tuple(self.initial_positions.shape))
+        alive = self._tensor("alive", torch.bool, (len(self.pairs),))
+        out = (C.c_double * 5)()
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        rc = _lib.lib().tdem_icedem_energy(self._handle.ptr, pos.data_ptr(), vel.data_ptr(), alive.data_ptr(),
+                                           float(self.time), out, stream)
+        _lib.check(rc, self._handle.ptr, "tdem_icedem_energy")
+        return dict(kinetic_J=out[0], bond_J=out[1], pair_contact_J=out[2], tool_contact_J=out[3],
+                    mechanical_J=out[4])

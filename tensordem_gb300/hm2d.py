@@ -371,6 +371,27 @@ class HM2D:
         return out[:min(int(count.value), cap)].copy()
 
 
+def contact_law(config: HM2DConfig, rows) -> np.ndarray:
+    """The engine's per-contact Hertz-Mindlin law on a batch of pair states.
+
+    ``rows`` is (K, 16): overlap delta, unit normal (x, y) from a to b, r_a,
+    r_b, v_a (x, y), omega_a, v_b (x, y), omega_b, 1/m_a, 1/m_b, the stored
+    tangential history (x, y) in a's orientation and one unused column.
+    Returns (K, 8): force on a (x, y), n x F_a, the updated history (x, y),
+    the step's dissipated energy, the Hertz and the spring energy; zeros for a
+    pair without overlap (its history resets). Runs the step kernel's own device function
+    in ``config.precision`` with ``config``'s material and time step
+    (include/tdem.h, ``tdem_hm_contact_law``).
+    """
+    a = np.ascontiguousarray(np.asarray(rows, dtype=np.float64).reshape(-1, 16))
+    out = np.empty((len(a), 8))
+    lib = _lib.lib()
+    rc = lib.tdem_hm_contact_law(C.byref(config.to_c()), len(a), a.ctypes.data, out.ctypes.data,
+                                 torch.cuda.current_stream().cuda_stream)
+    _lib.check(rc, None, "tdem_hm_contact_law")
+    return out
+
+
 def ice_sheet_case(nx: int = 2048, ny: int = 512, *, radius: float = 0.05, density: float = 900.0,
                    young: float = 5e9, poisson: float = 0.3, mu: float = 0.3, restitution: float = 0.5,
                    bond_damping: float = 0.05, breaking_strain: float = 0.01,

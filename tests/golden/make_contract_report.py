@@ -2,7 +2,7 @@
 
 Run where the reference source tree is available::
 
-    PYTHONPATH=/root/reference/src python tests/golden/make_contract_report.py
+    PYTHONPATH=<reference>/src python tests/golden/make_contract_report.py
 
 It imports ``tensordem.binding_contract`` (src/tensordem/binding_contract.py)
 and runs its ``verify()`` on ``tensordem_gb300.IceDEM`` and

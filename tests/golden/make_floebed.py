@@ -2,7 +2,7 @@
 
 Run where the reference source tree is available::
 
-    PYTHONPATH=/root/reference/src python tests/golden/make_floebed.py
+    PYTHONPATH=<reference>/src python tests/golden/make_floebed.py
 
 It imports ``tensordem.scale_ceiling.kernel.FloeBed``
 (src/tensordem/scale_ceiling/kernel.py:155-455: Hertz normal force with the

@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is mounted::
 
-    PYTHONPATH=/root/reference/src python tests/golden/make_golden.py
+    PYTHONPATH=<reference>/src python tests/golden/make_golden.py
 
 It imports the reference ``tensordem.dem.IceDEM`` (``src/tensordem/dem.py``),
 runs it on CPU in float64 with one torch thread (as its CLI does,

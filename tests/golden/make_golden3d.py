@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is mounted::
 
-    PYTHONPATH=/root/reference/src python tests/golden/make_golden3d.py
+    PYTHONPATH=<reference>/src python tests/golden/make_golden3d.py
 
 It imports the reference ``tensordem.dem3d.IceDEM3D`` (``src/tensordem/dem3d.py``),
 runs it on CPU in float64 with one torch thread (as its CLI does,
