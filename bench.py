@@ -276,10 +276,14 @@ def timed_steps(eng, steps, warmup, flush_l2, stream, dev):
     return ([e0.elapsed_time(e1) for e0, e1 in evs], [r0.elapsed_time(r1) for r0, r1 in rebuild_evs], wall)
 
 
-def fp64_rate(seed, steps, warmup, flush_l2, stream, dev) -> dict:
-    """The plain FP64 build of the same kernels on the same workload and loop."""
+def form_rate(seed, steps, warmup, flush_l2, stream, dev, *, precision=64, sum_precision=32) -> dict:
+    """Another numeric form of the same kernels on the same workload and loop:
+    the plain FP64 build, or the FP32 build with FP64 per-particle sums."""
+    from dataclasses import replace
+
     from tensordem_gb300.hm2d import HM2D, granular_gas_case
-    cfg, st = granular_gas_case(N_SIDE, seed=seed, precision=64)
+    cfg, st = granular_gas_case(N_SIDE, seed=seed, precision=precision)
+    cfg = replace(cfg, sum_precision=sum_precision)
     eng = HM2D(cfg, device=dev)
     eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
     eng.autotune(steps=2)
@@ -288,8 +292,9 @@ def fp64_rate(seed, steps, warmup, flush_l2, stream, dev) -> dict:
     total = sum(step_ms) + sum(rebuild_ms)
     return {"value": cfg.n * steps / (total / 1e3), "unit": UNIT, "steps": steps, "variant": eng.variant,
             "step_kernel_us_mean": 1e3 * sum(step_ms) / len(step_ms), "rebuilds": len(rebuild_ms),
-            "note": "precision=64 build of the same kernels (FP64 contacts, sums and ledger), same seeded "
-                    "1,048,576-disc state and the same flushed per-step loop"}
+            "note": ("precision=64 build of the same kernels (FP64 contacts, sums and ledger)" if precision == 64
+                     else "FP32 contacts with FP64 per-particle force/torque sums") +
+                    ", same seeded 1,048,576-disc state and the same flushed per-step loop"}
 
 
 BATCH_INSTANCES = 512
@@ -441,7 +446,8 @@ def run_ours(a) -> None:
            "note": "one solve through tdem_hm_set_state/step/read_state with host arrays: upload, "
                    f"{a.steps} steps, download; L2 flushed before it"}
 
-    fp64 = fp64_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev)
+    fp64 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=64)
+    sums64 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=32, sum_precision=64)
     batched = None
     if rank == 0 and world == 1 and not a.no_batched:
         del eng
@@ -462,7 +468,7 @@ def run_ours(a) -> None:
                           "step_kernel_us_median": 1e3 * statistics.median(step_ms),
                           "wall_s_timed_loop": wall,
                           "max_neighbors_seen": led1["max_neighbors"],
-                          "touching_contacts_end": c_contacts, "fp64": fp64}}
+                          "touching_contacts_end": c_contacts, "fp64": fp64, "fp32_fp64_sums": sums64}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -221,6 +221,9 @@ typedef struct {
   double indenter_velocity[2]; /* m/s */
   double indenter_radius;      /* m */
   int32_t load_capacity;  /* evaluations whose indenter reaction is recorded */
+  int32_t sum_precision;  /* FP32 engines: 64 sums each particle's force and
+                             torque terms in FP64; 0 or 32: compensated FP32
+                             (float-float) sums. FP64 engines sum in FP64. */
 } tdem_hm_config;
 
 /* Ledger slots of tdem_hm_read_ledger (J unless noted). */

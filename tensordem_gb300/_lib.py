@@ -76,7 +76,7 @@ class HMConfigC(C.Structure):
         ("bond_damping", C.c_double), ("breaking_strain", C.c_double),
         ("shear_breaking_strain", C.c_double), ("indenter_center", C.c_double * 2),
         ("indenter_velocity", C.c_double * 2), ("indenter_radius", C.c_double),
-        ("load_capacity", C.c_int32),
+        ("load_capacity", C.c_int32), ("sum_precision", C.c_int32),
     ]
 
 

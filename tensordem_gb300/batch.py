@@ -147,9 +147,11 @@ class Batch:
 
     def step(self, n: int) -> None:
         """Advance every live instance by n steps (asynchronous)."""
+        from . import ops
+        if not hasattr(self, "_anchor"):
+            self._anchor = torch.zeros(1, device=self.device)  # the device of the torch op
         with torch.cuda.device(self.device):
-            rc = self._lib.tdem_batch_step(self._h, int(n), self._stream())
-        _lib.check(rc, self._h, "tdem_batch_step")
+            ops.batch_step(self._h.value, int(n), self._anchor)
 
     def read(self, iid: int, state: bool = True) -> dict:
         """Integer-time state (host FP64, local order) and ledger of one instance."""

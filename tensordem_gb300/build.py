@@ -71,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                 print(msg, file=sys.stderr)
     objs = [BUILD / (s.stem + ".o") for s in sources()]
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

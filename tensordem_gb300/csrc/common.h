@@ -4,9 +4,13 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "../../include/tdem.h"
 
@@ -16,6 +20,28 @@ namespace tdem {
 inline int fail(std::string* err, int code, const std::string& msg) {
   if (err) *err = msg;
   return code;
+}
+
+// Host memcpy split over up to 8 threads for large copies (the staging of
+// host arrays through pinned buffers is bound by one core's copy rate).
+inline void parallel_copy(void* dst, const void* src, size_t bytes) {
+  constexpr size_t kChunk = size_t(4) << 20;
+  const size_t parts = std::min<size_t>(8, bytes / kChunk);
+  if (parts < 2) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  const size_t step = (bytes / parts + 63) & ~size_t(63);
+  std::vector<std::thread> workers;
+  for (size_t k = 1; k < parts; ++k) {
+    const size_t a = k * step;
+    if (a >= bytes) break;
+    workers.emplace_back([=] {
+      std::memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, std::min(step, bytes - a));
+    });
+  }
+  std::memcpy(dst, src, std::min(step, bytes));
+  for (auto& w : workers) w.join();
 }
 
 #define TDEM_CUDA_TRY(err_str, expr)                                                   \

@@ -218,7 +218,8 @@ constexpr int kVariants = 7;
 constexpr int kWindowVariant = 6;
 
 template <class T>
-using StepFn = void (*)(Params<T>, Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int);
+using StepFn = void (*)(Params<T>, Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int,
+                        StepHint);
 
 // The neighbour-window kernel for FP32 engines; variant 1's kernel for FP64.
 template <class T, int MODE, bool F>
@@ -227,6 +228,13 @@ StepFn<T> window_fn() {
     return &force_kernel_win<T, MODE, F>;
   else
     return &force_kernel_pf<T, MODE, 256, 3, F>;
+}
+
+// The FP64-sum form of an FP32 engine: every variant runs the grid-stride
+// kernel with double per-particle sums.
+template <class T, bool F>
+StepFn<T> step_fn_sum64(int mode) {
+  return mode == kPrime ? &force_kernel_pf<T, kPrime, 256, 3, F, true> : &force_kernel_pf<T, kStep, 256, 3, F, true>;
 }
 
 template <class T, bool F>
@@ -256,7 +264,8 @@ StepFn<T> step_fn_feat(int variant, int mode) {
 // FEAT kernels carry the bonded-particle model and the indenter; the plain
 // granular kernels compile without them (fewer registers).
 template <class T>
-StepFn<T> step_fn(int variant, int mode, bool feat) {
+StepFn<T> step_fn(int variant, int mode, bool feat, bool sum64 = false) {
+  if (sum64) return feat ? step_fn_sum64<T, true>(mode) : step_fn_sum64<T, false>(mode);
   return feat ? step_fn_feat<T, true>(variant, mode) : step_fn_feat<T, false>(variant, mode);
 }
 
@@ -300,6 +309,13 @@ struct Engine final : EngineBase {
   double* host_stage = nullptr;   // pinned
   size_t stage_elems = 0;
   Ctl* host_ctl = nullptr;        // pinned mirror
+  // The device's buffer parities and evaluation count as last read by the
+  // host, kept current across plain step launches and explicit rebuilds;
+  // invalid after anything that changes them on the device unseen.
+  bool sum64 = false;  // FP32 engine with double per-particle sums
+  bool mirror_ok = false;
+  int m_sp = 0, m_lp = 0;
+  long long m_evals = 0;
   double* host_part = nullptr;    // pinned peek partials
   double* host_diss = nullptr;    // pinned committed partials
   double* host_frac = nullptr;    // pinned committed fracture partials
@@ -324,6 +340,14 @@ struct Engine final : EngineBase {
     graph = graph1 = nullptr;
   }
 
+  // host_ctl was just read from the device with nothing enqueued after it
+  void refresh_mirror() {
+    m_sp = host_ctl->sp;
+    m_lp = host_ctl->lp;
+    m_evals = host_ctl->evals;
+    mirror_ok = true;
+  }
+
   template <class U>
   int alloc(U** p, size_t count) {
     void* q = nullptr;
@@ -336,6 +360,7 @@ struct Engine final : EngineBase {
 
   int init(const tdem_hm_config& c) {
     make_params<T>(c, c.max_neighbors, P);
+    sum64 = sizeof(T) == 4 && c.sum_precision == 64;
     const size_t n = (size_t)c.n, W = (size_t)c.max_neighbors;
     nblocks = (int)((n + kThreads - 1) / kThreads);
     scan_blocks = (P.nkeys + kScanChunk - 1) / kScanChunk;
@@ -347,14 +372,14 @@ struct Engine final : EngineBase {
     nwarp_slots = nblocks * (kThreads / 32);
     for (int v = 1; v < kVariants; ++v) {
       int per_sm = 0;
-      const int bs = variant_block<T>(v);
-      const size_t smem = variant_smem<T>(v);
+      const int bs = block_of(v);
+      const size_t smem = smem_of(v);
       if (smem > 0)
         for (int mode : {kPrime, kStep})
-          TDEM_CUDA_TRY(&err, cudaFuncSetAttribute(reinterpret_cast<const void*>(step_fn<T>(v, mode, feat())),
+          TDEM_CUDA_TRY(&err, cudaFuncSetAttribute(reinterpret_cast<const void*>(step_fn<T>(v, mode, feat(), sum64)),
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       TDEM_CUDA_TRY(&err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &per_sm, reinterpret_cast<const void*>(step_fn<T>(v, kStep, feat())), bs, smem));
+                              &per_sm, reinterpret_cast<const void*>(step_fn<T>(v, kStep, feat(), sum64)), bs, smem));
       const int need = (int)((n + bs - 1) / bs);
       vgrid[v] = std::max(1, std::min(need, per_sm * sms));
       nwarp_slots = std::max(nwarp_slots, vgrid[v] * (bs / 32));
@@ -397,6 +422,9 @@ struct Engine final : EngineBase {
   }
 
   bool feat() const { return P.BMAX > 0 || P.irad > T(0); }
+  // launch shape of a variant's step kernel (the FP64-sum form has one shape)
+  int block_of(int v) const { return sum64 ? 256 : variant_block<T>(v); }
+  size_t smem_of(int v) const { return sum64 ? 0 : variant_smem<T>(v); }
   dim3 grid_n() const { return dim3((unsigned)nblocks); }
   dim3 grid_keys() const { return dim3((unsigned)((P.nkeys + kThreads - 1) / kThreads)); }
 
@@ -413,7 +441,7 @@ struct Engine final : EngineBase {
       size_t off = 0;
       for (int k = 0; k < 6; ++k) {
         if (!src[k]) return tdem::fail(&err, TDEM_ERR_BADARG, "set_state: null host array");
-        std::memcpy(host_stage + off, src[k], len[k] * sizeof(double));
+        tdem::parallel_copy(host_stage + off, src[k], len[k] * sizeof(double));
         d[k] = stage + off;
         off += len[k];
       }
@@ -425,6 +453,7 @@ struct Engine final : EngineBase {
         d[k] = src[k];
       }
     }
+    mirror_ok = false;
     Ctl zero{};
     zero.rebuild_pending = 1;
     TDEM_CUDA_TRY(&err, cudaMemcpyAsync(B.ctl, &zero, sizeof(Ctl), cudaMemcpyHostToDevice, s));
@@ -444,12 +473,13 @@ struct Engine final : EngineBase {
   int add_step_and_rebuild(cudaGraph_t g, const cudaGraphNode_t* dep, size_t ndep,
                            cudaGraphConditionalHandle h, cudaGraphConditionalHandle hl, int cond_bits) {
     int prim = 1;
-    void* args[] = {&P, &B, &h, &hl, &cond_bits, &prim};
+    StepHint nohint{};
+    void* args[] = {&P, &B, &h, &hl, &cond_bits, &prim, &nohint};
     cudaKernelNodeParams kp = {};
-    kp.func = reinterpret_cast<void*>(step_fn<T>(variant, kStep, feat()));
+    kp.func = reinterpret_cast<void*>(step_fn<T>(variant, kStep, feat(), sum64));
     kp.gridDim = dim3((unsigned)vgrid[variant]);
-    kp.blockDim = dim3((unsigned)variant_block<T>(variant));
-    kp.sharedMemBytes = (unsigned)variant_smem<T>(variant);
+    kp.blockDim = dim3((unsigned)block_of(variant));
+    kp.sharedMemBytes = (unsigned)smem_of(variant);
     kp.kernelParams = args;
     cudaGraphNode_t snode;
     if (P.BMAX > 0) {
@@ -535,8 +565,9 @@ struct Engine final : EngineBase {
   }
 
   int prime(cudaStream_t s) {
+    mirror_ok = false;
     launch_strain(s);
-    step_fn<T>(variant, kPrime, feat())<<<vgrid[variant], variant_block<T>(variant), variant_smem<T>(variant), s>>>(P, B, 0, 0, 0, 1);
+    step_fn<T>(variant, kPrime, feat(), sum64)<<<vgrid[variant], block_of(variant), smem_of(variant), s>>>(P, B, 0, 0, 0, 1, StepHint{});
     launch_rebuild(s);  // runs only if the prime step tripped the trigger
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     primed = true;
@@ -546,6 +577,7 @@ struct Engine final : EngineBase {
   int step(long long n, cudaStream_t s) override {
     if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "step before set_state");
     if (n <= 0) return TDEM_OK;
+    mirror_ok = false;  // rebuild decisions inside the step graph are the device's
     if (!primed) {
       int rc = prime(s);
       if (rc) return rc;
@@ -573,7 +605,7 @@ struct Engine final : EngineBase {
     }
     for (long long k = 0; k < n; ++k) {
       launch_strain(s);
-      step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block<T>(variant), variant_smem<T>(variant), s>>>(P, B, 0, 0, 0, 1);
+      step_fn<T>(variant, kStep, feat(), sum64)<<<vgrid[variant], block_of(variant), smem_of(variant), s>>>(P, B, 0, 0, 0, 1, StepHint{});
       launch_rebuild(s);
     }
     TDEM_CUDA_TRY(&err, cudaGetLastError());
@@ -582,10 +614,15 @@ struct Engine final : EngineBase {
 
   int peek(cudaStream_t s) {
     launch_strain(s);
-    if (feat())
-      force_kernel<T, kPeek, true><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, primed ? 1 : 0);
+    const int pr = primed ? 1 : 0;
+    if (sum64 && feat())
+      force_kernel<T, kPeek, true, true><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, pr, StepHint{});
+    else if (sum64)
+      force_kernel<T, kPeek, false, true><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, pr, StepHint{});
+    else if (feat())
+      force_kernel<T, kPeek, true><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, pr, StepHint{});
     else
-      force_kernel<T, kPeek, false><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, primed ? 1 : 0);
+      force_kernel<T, kPeek, false><<<grid_n(), kThreads, 0, s>>>(P, B, 0, 0, 0, pr, StepHint{});
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     return TDEM_OK;
   }
@@ -602,11 +639,11 @@ struct Engine final : EngineBase {
       TDEM_CUDA_TRY(&err, cudaGetLastError());
       TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_stage, stage, 8 * n * sizeof(double), cudaMemcpyDeviceToHost, s));
       TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
-      if (pos) std::memcpy(pos, host_stage, 2 * n * sizeof(double));
-      if (vel) std::memcpy(vel, host_stage + 2 * n, 2 * n * sizeof(double));
-      if (omega) std::memcpy(omega, host_stage + 4 * n, n * sizeof(double));
-      if (force) std::memcpy(force, host_stage + 5 * n, 2 * n * sizeof(double));
-      if (torque) std::memcpy(torque, host_stage + 7 * n, n * sizeof(double));
+      if (pos) tdem::parallel_copy(pos, host_stage, 2 * n * sizeof(double));
+      if (vel) tdem::parallel_copy(vel, host_stage + 2 * n, 2 * n * sizeof(double));
+      if (omega) tdem::parallel_copy(omega, host_stage + 4 * n, n * sizeof(double));
+      if (force) tdem::parallel_copy(force, host_stage + 5 * n, 2 * n * sizeof(double));
+      if (torque) tdem::parallel_copy(torque, host_stage + 7 * n, n * sizeof(double));
       return TDEM_OK;
     }
     unpack_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B, pos, vel, omega, force, torque);
@@ -663,6 +700,7 @@ struct Engine final : EngineBase {
   int status(cudaStream_t s) override {
     TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_ctl, B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
+    refresh_mirror();
     const int st = host_ctl->status;
     if (st & kStatusNonfinite) return tdem::fail(&err, TDEM_ERR_NONFINITE, "non-finite particle state; reduce dt");
     if (st & kStatusCapacity)
@@ -703,14 +741,20 @@ struct Engine final : EngineBase {
     if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "step before set_state");
     if (!primed) return prime(s);
     launch_strain(s);
-    step_fn<T>(variant, kStep, feat())<<<vgrid[variant], variant_block<T>(variant), variant_smem<T>(variant), s>>>(P, B, 0, 0, 0, 1);
+    const StepHint hint = mirror_ok ? StepHint{1, m_sp, m_lp, m_evals} : StepHint{};
+    step_fn<T>(variant, kStep, feat(), sum64)<<<vgrid[variant], block_of(variant), smem_of(variant), s>>>(
+        P, B, 0, 0, 0, 1, hint);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
+    // the launch's last block flips the state buffers and counts the evaluation
+    m_sp ^= 1;
+    ++m_evals;
     return TDEM_OK;
   }
 
   int rebuild_pending(cudaStream_t s) override {
     TDEM_CUDA_TRY(&err, cudaMemcpyAsync(host_ctl, B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     TDEM_CUDA_TRY(&err, cudaStreamSynchronize(s));
+    refresh_mirror();
     return host_ctl->rebuild_pending ? 1 : 0;
   }
 
@@ -752,6 +796,7 @@ struct Engine final : EngineBase {
     TDEM_CUDA_TRY(&err, e);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
     // bonded pairs leave the contact candidates: rebuild the list now
+    mirror_ok = false;
     request_rebuild_kernel<<<1, 1, 0, s>>>(B.ctl);
     launch_rebuild(s);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
@@ -857,6 +902,7 @@ struct Engine final : EngineBase {
   // the fastest. Per-particle arithmetic is identical in all variants.
   int autotune(int steps, cudaStream_t s, float* ms_out) override {
     if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "autotune before set_state");
+    mirror_ok = false;
     cudaEvent_t e0, e1;
     TDEM_CUDA_TRY(&err, cudaEventCreate(&e0));
     TDEM_CUDA_TRY(&err, cudaEventCreate(&e1));
@@ -888,6 +934,9 @@ struct Engine final : EngineBase {
     request_rebuild_kernel<<<1, 1, 0, s>>>(B.ctl);
     launch_rebuild(s);
     TDEM_CUDA_TRY(&err, cudaGetLastError());
+    // a requested rebuild always ends by swapping both buffer sets
+    m_sp ^= 1;
+    m_lp ^= 1;
     return TDEM_OK;
   }
 
@@ -938,6 +987,8 @@ const char* hm_config_error(const tdem_hm_config* c) {
       !(c->mu_wall >= 0))
     return "invalid material, cell or time-step parameter";
   if (c->precision != 32 && c->precision != 64) return "precision must be 32 or 64";
+  if (c->sum_precision != 0 && c->sum_precision != 32 && c->sum_precision != 64)
+    return "sum_precision must be 0, 32 or 64";
   return nullptr;
 }
 
@@ -1332,7 +1383,7 @@ int tdem_hm_contact_forces_noalloc(const tdem_hm_config* cfg, const double* pos,
                                                                                B.cell_fill, P.nkeys);
   pack_kernel<float><<<nb, kThreads, 0, s>>>(P, B, pos, vel, omega, radius, mass, inertia);
   launch_rebuild_seq<float>(P, B, s);
-  force_kernel<float, kPeek, false><<<nb, kThreads, 0, s>>>(P, B, 0, 0, 0, 0);
+  force_kernel<float, kPeek, false><<<nb, kThreads, 0, s>>>(P, B, 0, 0, 0, 0, StepHint{});
   unpack_kernel<float><<<nb, kThreads, 0, s>>>(P, B, nullptr, nullptr, nullptr, out_force, out_torque);
   noalloc_status_kernel<<<1, 1, 0, s>>>(B.ctl, status_dev);
   cudaError_t e = cudaGetLastError();

@@ -111,10 +111,12 @@ struct Ctl {
   int sp;                  // current pos/vel/hist buffer
   int lp;                  // current list / cell / orig / wall-history buffer
   unsigned ticket;         // completed blocks of the running step kernel
-  unsigned vmax2_bits;     // max |v|^2 of the running step (float bits)
-  float disp;              // displacement bound since the last rebuild
   int rebuild_pending;     // a rebuild must run before the next evaluation
-  int status;              // Status bits
+  // max |v|^2 of the running step (float bits) and the Status bits: one
+  // aligned 8-byte pair, so a step's last block reads both in one load
+  alignas(8) unsigned vmax2_bits;
+  int status;
+  float disp;              // displacement bound since the last rebuild
   int rebuilds;
   int max_cnt;             // largest candidate count of the last rebuild
   int tile_next2;          // batched engine: chunk counter of the second step launch
@@ -229,6 +231,26 @@ struct Acc<float> {
     lo += err;
   }
   __device__ __forceinline__ float get() const { return hi + lo; }
+};
+
+// Plain FP64 sum of the engine's terms (the FP64-sum form of an FP32
+// engine): every add in double, rounded to the engine's type once at the end.
+template <class T>
+struct AccD {
+  double s = 0.0;
+  __device__ __forceinline__ void add(T x) { s += (double)x; }
+  __device__ __forceinline__ T get() const { return (T)s; }
+};
+
+// The per-particle accumulator: float-float / double (S64 false), or double
+// sums for an FP32 engine (S64 true).
+template <class T, bool S64>
+struct AccSel {
+  using type = Acc<T>;
+};
+template <class T>
+struct AccSel<T, true> {
+  using type = AccD<T>;
 };
 
 __device__ __forceinline__ unsigned spread5(unsigned v) {

@@ -147,10 +147,10 @@ __device__ __forceinline__ PairOut<T> contact_law(const Params<T>& P, T delta, T
 }
 
 // Planar wall with inward normal (nwx, nwy) at distance `gap` from the centre.
-template <class T, bool COMMIT>
+template <class T, bool COMMIT, class A>
 __device__ __forceinline__ void wall_contact(const Params<T>& P, T nwx, T nwy, T gap, const V4<T>& p,
-                                             const V4<T>& v, V2<T>* slot, Acc<T>& fx, Acc<T>& fy,
-                                             Acc<T>& tq, T& diss, T& un, T& ut, bool peek_old_xi) {
+                                             const V4<T>& v, V2<T>* slot, A& fx, A& fy,
+                                             A& tq, T& diss, T& un, T& ut, bool peek_old_xi) {
   V2<T> xw = *slot;
   const T delta = p.z - gap;
   if (!(delta > T(0))) {
@@ -252,11 +252,11 @@ struct WindowFetch {
 
 // One candidate slot of particle i (partner j at position q): contact test,
 // history update in place, force and torque accumulation.
-template <class T, int MODE, class F>
+template <class T, int MODE, class F, class A>
 __device__ __forceinline__ void do_slot(const Params<T>& P, const F& fetch,
                                         V2<T>* __restrict__ hist, int i, int j, int s, size_t slot,
                                         const V4<T>& p, const V4<T>& v, const V4<T>& q, unsigned mask,
-                                        unsigned& nmask, Acc<T>& fx, Acc<T>& fy, Acc<T>& tq, T& diss, T& un,
+                                        unsigned& nmask, A& fx, A& fy, A& tq, T& diss, T& un,
                                         T& ut, int primed) {
   constexpr bool COMMIT = MODE != kPeek;
   const bool owner = i < j;
@@ -439,10 +439,10 @@ struct BondIn {
   T sj;         // partner's objective shear strain
 };
 
-template <class T, int MODE>
+template <class T, int MODE, class A>
 __device__ __forceinline__ void do_bond(const Params<T>& P, const Bufs<T>& B, int lp, int i, size_t k,
                                         long long eval, const V4<T>& p, const V4<T>& v, const BondIn<T>& in,
-                                        T si, Acc<T>& fx, Acc<T>& fy, Acc<T>& tq, ThreadLedger<T>& L,
+                                        T si, A& fx, A& fy, A& tq, ThreadLedger<T>& L,
                                         int primed) {
   constexpr bool COMMIT = MODE != kPeek;
   const unsigned w = in.w;
@@ -569,9 +569,9 @@ __device__ __forceinline__ void do_bond(const Params<T>& P, const Bufs<T>& B, in
 // Rigid circular indenter, Hertz normal + Tsuji dashpot, frictionless
 // (the reference's tool, dem.py:294-312, with the Hertz law of the contacts).
 // Distances in FP64 from the integer cell origin, only for discs near it.
-template <class T>
+template <class T, class A>
 __device__ __forceinline__ void indenter_contact(const Params<T>& P, long long eval, const V4<T>& p, const V4<T>& v,
-                                                 Acc<T>& fx, Acc<T>& fy, ThreadLedger<T>& L) {
+                                                 A& fx, A& fy, ThreadLedger<T>& L) {
   const int c = lane_to_cell(p.w);
   {
     // FP32 screen: a disc clearly out of reach never touches FP64 (the FP32
@@ -627,7 +627,7 @@ __device__ __forceinline__ void load_head_partners(const F& fetch, const uint4& 
 }
 
 // process_particle with the first three partners' positions already loaded.
-template <class T, int MODE, bool FEAT, class F>
+template <class T, int MODE, bool FEAT, class F, bool S64 = false>
 __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Bufs<T>& B, const F& fetch, int sp,
                                                    int lp, int i, const V4<T>& p, const V4<T>& v, const uint4& hd,
                                                    const V4<T>& q0, const V4<T>& q1, const V4<T>& q2, int primed,
@@ -639,7 +639,7 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
   const int cnt = (int)(hd.x & 0xFFu);
   const unsigned mask = hd.x >> 8;
   unsigned nmask = 0u;
-  Acc<T> fx, fy, tq;
+  typename AccSel<T, S64>::type fx, fy, tq;
   if (FEAT && P.BMAX > 0) {
     // the count and every slot word in one round of loads (slots past the
     // count are allocated, their words unused)
@@ -754,14 +754,14 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
   }
 }
 
-template <class T, int MODE, bool FEAT>
+template <class T, int MODE, bool FEAT, bool S64 = false>
 __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i,
                                                  const V4<T>& p, const V4<T>& v, const uint4& hd, int primed,
                                                  long long eval, ThreadLedger<T>& L) {
   V4<T> q0{}, q1{}, q2{};
   const GlobalFetch<T> fetch{B.pos[sp], B.vel[sp]};
   load_head_partners<T>(fetch, hd, q0, q1, q2);
-  process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, eval, L);
+  process_particle_q<T, MODE, FEAT, GlobalFetch<T>, S64>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, eval, L);
 }
 
 // Control fields a step kernel reads once at its start. disp and target are
@@ -773,20 +773,36 @@ struct StepCtl {
   float disp;
 };
 
-__device__ __forceinline__ StepCtl load_step_ctl(const Ctl* ctl) {
+// Buffer parities and evaluation count of a launch when the host knows them
+// (plain launches after a host read of the control block): the launch's own
+// state loads then need not wait for the control block's cold read.
+struct StepHint {
+  int valid, sp, lp;
+  long long evals;
+};
+
+__device__ __forceinline__ StepCtl load_step_ctl(const Ctl* ctl, const StepHint& hint = StepHint{0, 0, 0, 0}) {
   StepCtl c;
-  c.sp = ctl->sp;
-  c.lp = ctl->lp;
-  c.evals = ctl->evals;
-  c.target = ctl->target;
+  if (hint.valid) {
+    c.sp = hint.sp;
+    c.lp = hint.lp;
+    c.evals = hint.evals;
+  } else {
+    c.sp = ctl->sp;
+    c.lp = ctl->lp;
+    c.evals = ctl->evals;
+  }
+  c.target = ctl->target;  // read only by the last block's bookkeeping
   c.disp = ctl->disp;
   return c;
 }
 
-// Commit epilogue: per-warp ledger partials and the speed bound, then the
-// last warp of the last block does the step bookkeeping (indenter reaction,
-// rebuild trigger) and sets the graph's conditions. No block-wide barrier:
-// warps retire as soon as they are done.
+// Commit epilogue: per-warp ledger partials (fire-and-forget adds; one
+// warp owns each slot, so every slot still sums its steps in step order),
+// the block's speed bound, then the last block of the grid does the step
+// bookkeeping (indenter reaction, rebuild trigger) and sets the graph's
+// conditions. Its tail costs two round trips to L2: the grid ticket and one
+// 8-byte read of the speed bound with the status word.
 template <class T, bool FEAT>
 __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T>& B, const StepCtl& c,
                                                 const ThreadLedger<T>& L, cudaGraphConditionalHandle h_rebuild,
@@ -807,33 +823,31 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
       wb += __shfl_xor_sync(0xffffffffu, wb, off);
     }
   }
-  if (__any_sync(0xffffffffu, L.bad) && (threadIdx.x & 31) == 0) atomicOr(&ctl->status, (int)kStatusNonfinite);
-  __shared__ unsigned s_warps_done;
-  if (threadIdx.x == 0) s_warps_done = 0u;  // every block starts at zero
-  __syncthreads();
-  if ((threadIdx.x & 31) != 0) return;
-  const size_t gw = (size_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (wd != T(0)) B.diss_part[gw] += (double)wd;
-  if (FEAT && wf != T(0)) B.frac_part[gw] += (double)wf;
-  if (FEAT && wb) atomicAdd(&ctl->broken, wb);
-  if (FEAT && (wix != T(0) || wiy != T(0))) {
-    const unsigned e = atomicAdd(&ctl->load_entries, 1u);
-    B.ind_part[3 * (size_t)e] = (double)gw;
-    B.ind_part[3 * (size_t)e + 1] = (double)wix;
-    B.ind_part[3 * (size_t)e + 2] = (double)wiy;
+  __shared__ float s_vmax[32];
+  if ((threadIdx.x & 31) == 0) {
+    const size_t gw = (size_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (wd != T(0)) atomicAdd(&B.diss_part[gw], (double)wd);
+    if (FEAT && wf != T(0)) atomicAdd(&B.frac_part[gw], (double)wf);
+    if (FEAT && wb) atomicAdd(&ctl->broken, wb);
+    if (FEAT && (wix != T(0) || wiy != T(0))) {
+      const unsigned e = atomicAdd(&ctl->load_entries, 1u);
+      B.ind_part[3 * (size_t)e] = (double)gw;
+      B.ind_part[3 * (size_t)e + 1] = (double)wix;
+      B.ind_part[3 * (size_t)e + 2] = (double)wiy;
+    }
+    s_vmax[threadIdx.x >> 5] = wm;
   }
-  const unsigned bits = __float_as_uint(wm);
-  if (bits > *reinterpret_cast<volatile unsigned*>(&ctl->vmax2_bits)) atomicMax(&ctl->vmax2_bits, bits);
+  const int bad = __syncthreads_or(L.bad ? 1 : 0);
+  if (threadIdx.x != 0) return;
+  float bm = s_vmax[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bm = fmaxf(bm, s_vmax[w]);
+  if (bad) atomicOr(&ctl->status, (int)kStatusNonfinite);
+  atomicMax(&ctl->vmax2_bits, __float_as_uint(bm));
   __threadfence();
-  const unsigned mine = atomicAdd(&s_warps_done, 1u);
-  if (mine != blockDim.x / 32 - 1) return;
-  // last warp of this block
   const unsigned t = atomicAdd(&ctl->ticket, 1u);
   if (t != gridDim.x - 1) return;
-  // last block of the grid. The speed bound is read by an atomic at L2,
-  // issued only after the ticket's value was tested; the indenter partials
-  // are read with plain loads and need the fence.
-  if (FEAT) __threadfence();
+  // last block of the grid: every other block's writes are visible after this
+  __threadfence();
   if (FEAT && P.irad > T(0)) {
     // sum the indenter partials in warp order (deterministic)
     const unsigned m = *reinterpret_cast<volatile unsigned*>(&ctl->load_entries);
@@ -865,9 +879,11 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
     }
     ctl->load_entries = 0u;
   }
-  const unsigned vbits = atomicExch(&ctl->vmax2_bits, 0u);
-  const int status = *reinterpret_cast<volatile int*>(&ctl->status);
+  const unsigned long long pair = *reinterpret_cast<volatile unsigned long long*>(&ctl->vmax2_bits);
+  const unsigned vbits = (unsigned)(pair & 0xFFFFFFFFull);
+  const int status = (int)(pair >> 32);
   const float vmax = sqrtf(__uint_as_float(vbits));
+  ctl->vmax2_bits = 0u;
   ctl->ticket = 0;
   ctl->sp = sp ^ 1;
   const long long evals = c.evals + 1;
@@ -876,7 +892,8 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
   ctl->disp = disp;
   const int rebuild = (disp > P.rebuild_disp) ? 1 : 0;
   ctl->rebuild_pending = rebuild;
-  const int keep_going = (evals < c.target) && !(status & kStatusNonfinite);
+  // a non-finite state or a bounded wait that ran out ends the step loop
+  const int keep_going = (evals < c.target) && !(status & (kStatusNonfinite | kStatusTimeout));
   // use_cond bit 0: this launch sits in a graph with a rebuild IF node;
   // bit 1: it also sits in the step loop's WHILE body
   if (use_cond & 1) cudaGraphSetConditional(h_rebuild, (unsigned)rebuild);
@@ -884,12 +901,12 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
 }
 
 // One thread per particle (variant 0) and the read-back kernel.
-template <class T, int MODE, bool FEAT>
+template <class T, int MODE, bool FEAT, bool S64 = false>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel(Params<T> P, Bufs<T> B,
                                                             cudaGraphConditionalHandle h_rebuild,
                                                             cudaGraphConditionalHandle h_loop, int use_cond,
-                                                            int primed) {
-  const StepCtl c = load_step_ctl(B.ctl);
+                                                            int primed, StepHint hint) {
+  const StepCtl c = load_step_ctl(B.ctl, hint);
   const int sp = c.sp, lp = c.lp;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   ThreadLedger<T> L;
@@ -897,7 +914,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel
     const V4<T> p = B.pos[sp][i];
     const V4<T> v = B.vel[sp][i];
     const uint4 hd = B.head[lp][i];
-    process_particle<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, primed, c.evals, L);
+    process_particle<T, MODE, FEAT, S64>(P, B, sp, lp, i, p, v, hd, primed, c.evals, L);
   }
   if (MODE == kPeek) {
     const double k = block_sum_d(L.ke);
@@ -929,13 +946,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2) force_kernel
 // Persistent grid-stride variant: while a thread works on particle i it has
 // the loads of its next particle already in flight (twice the memory-level
 // parallelism of variant 0 at the cost of a dozen registers).
-template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
+template <class T, int MODE, int BLOCK, int MINB, bool FEAT, bool S64 = false>
 __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs<T> B,
                                                                cudaGraphConditionalHandle h_rebuild,
                                                                cudaGraphConditionalHandle h_loop, int use_cond,
-                                                               int primed) {
+                                                               int primed, StepHint hint) {
   static_assert(MODE != kPeek, "read-back uses force_kernel");
-  const StepCtl c = load_step_ctl(B.ctl);
+  const StepCtl c = load_step_ctl(B.ctl, hint);
   const int sp = c.sp, lp = c.lp;
   const long long eval = c.evals;
   const int stride = gridDim.x * BLOCK;
@@ -957,7 +974,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
       vn = B.vel[sp][nx];
       hn = B.head[lp][nx];
     }
-    process_particle<T, MODE, FEAT>(P, B, sp, lp, i, p, v, hd, primed, eval, L);
+    process_particle<T, MODE, FEAT, S64>(P, B, sp, lp, i, p, v, hd, primed, eval, L);
     i = nx;
     p = pn;
     v = vn;
@@ -992,14 +1009,14 @@ template <class T, int MODE, bool FEAT>
 __global__ void __launch_bounds__(kWinThreads, 1) force_kernel_win(Params<T> P, Bufs<T> B,
                                                                    cudaGraphConditionalHandle h_rebuild,
                                                                    cudaGraphConditionalHandle h_loop, int use_cond,
-                                                                   int primed) {
+                                                                   int primed, StepHint hint) {
   static_assert(MODE != kPeek && sizeof(T) == 4, "the window variant steps FP32 engines");
   extern __shared__ __align__(128) unsigned char win_smem[];
   V4<T>* spos = reinterpret_cast<V4<T>*>(win_smem);
   V4<T>* svel = spos + kWinSlots * kWinBlock;
   uint4* shead = reinterpret_cast<uint4*>(svel + kWinSlots * kWinBlock);
   uint64_t* bar = reinterpret_cast<uint64_t*>(shead + kWinHeads * kWinBlock);  // [slots] pos/vel, [heads] head
-  const StepCtl c = load_step_ctl(B.ctl);
+  const StepCtl c = load_step_ctl(B.ctl, hint);
   const int sp = c.sp, lp = c.lp;
   const int n = P.n;
   const int nblk = (n + kWinBlock - 1) / kWinBlock;
@@ -1098,13 +1115,13 @@ template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
 __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bufs<T> B,
                                                                  cudaGraphConditionalHandle h_rebuild,
                                                                  cudaGraphConditionalHandle h_loop, int use_cond,
-                                                                 int primed) {
+                                                                 int primed, StepHint hint) {
   static_assert(MODE != kPeek, "read-back uses force_kernel");
   __shared__ alignas(128) V4<T> s_pos[2][BLOCK];
   __shared__ alignas(128) V4<T> s_vel[2][BLOCK];
   __shared__ alignas(128) uint4 s_head[2][BLOCK];
   __shared__ alignas(8) uint64_t s_bar[2];
-  const StepCtl c = load_step_ctl(B.ctl);
+  const StepCtl c = load_step_ctl(B.ctl, hint);
   const int sp = c.sp, lp = c.lp;
   const long long eval = c.evals;
   const int n = P.n;

@@ -449,6 +449,19 @@ def _host_ptr(t: torch.Tensor | None):
     return None if t is None else t.data_ptr()
 
 
+# Checkpoint layout of IceDEM3D.state_dict: required keys, the per-particle
+# and per-pair tensors restored, and the ones that must equal the solver's own.
+_CHECKPOINT_KEYS = frozenset({
+    "dimension", "config", "dt", "time", "step_count", "positions", "velocities", "initial_positions", "fixed",
+    "pairs", "bonded", "alive", "failure_mode", "failure_time_s", "failure_extension_m", "failure_energy_J"})
+_CHECKPOINT_TENSORS = ("positions", "velocities", "initial_positions", "fixed", "pairs", "bonded", "alive",
+                       "failure_mode", "failure_time_s", "failure_extension_m", "failure_energy_J")
+_CHECKPOINT_FROZEN = (("initial_positions", "checkpoint reference geometry does not match this solver"),
+                      ("pairs", "checkpoint pair topology does not match this solver"),
+                      ("bonded", "checkpoint bond topology does not match this solver"),
+                      ("fixed", "checkpoint fixed-boundary mask does not match this solver"))
+
+
 class IceDEM3D:
     """3-D bonded-sphere DEM with a spherical indenter, stepped on the GPU.
 
@@ -936,47 +949,61 @@ class IceDEM3D:
             return torch.zeros(len(self.positions), dtype=self.dtype, device=self.device)
         return submerged_fraction_sphere_tensor(self.positions[:, 2], cfg.radius, cfg.water_level)
 
+    def _body_terms(self):
+        """Per-particle vertical weight and buoyancy (N) and the wet-drag
+        coefficient times the submerged fraction (N s/m), from which both
+        ``body_forces`` and ``body_force_ledger`` are formed. Buoyancy lifts
+        the submerged volume fraction of each sphere with the water's weight;
+        the drag opposes the velocity in proportion to that fraction."""
+        cfg = self.config
+        n = len(self.positions)
+        frac = self.submerged_fraction()
+        weight = torch.full((n,), -cfg.mass * cfg.gravity if cfg.gravity > 0.0 else 0.0, dtype=self.dtype,
+                            device=self.device)
+        if cfg.water_level is None:
+            return weight, torch.zeros_like(weight), torch.zeros_like(weight), frac
+        sphere = (4.0 / 3.0) * math.pi * cfg.radius ** 3
+        lift = cfg.water_density * cfg.gravity * sphere * frac
+        drag = cfg.wet_drag_coefficient * frac if cfg.wet_drag_coefficient > 0.0 else torch.zeros_like(frac)
+        return weight, lift, drag, frac
+
     @torch.no_grad()
     def body_forces(self) -> torch.Tensor:
-        cfg = self.config
-        body = torch.zeros_like(self.positions)
-        if cfg.water_level is None and cfg.gravity == 0.0:
-            return body
-        if cfg.gravity > 0.0:
-            body[:, 2] -= cfg.mass * cfg.gravity
-        if cfg.water_level is None:
-            return body
-        f_sub = self.submerged_fraction()
-        volume = (4.0 / 3.0) * math.pi * cfg.radius ** 3
-        body[:, 2] += cfg.water_density * cfg.gravity * volume * f_sub
-        if cfg.wet_drag_coefficient > 0.0:
-            body -= cfg.wet_drag_coefficient * f_sub[:, None] * self.velocities
+        """Gravity, buoyancy and wet drag on every particle, (N, 3) in N."""
+        weight, lift, drag, _ = self._body_terms()
+        body = -drag[:, None] * self.velocities
+        body[:, 2] += weight + lift
         return body
 
     @torch.no_grad()
     def body_force_ledger(self) -> dict[str, float]:
+        """Vertical totals of the body forces and the submerged volume."""
         cfg = self.config
-        n = len(self.positions)
-        f_sub = self.submerged_fraction()
-        volume = (4.0 / 3.0) * math.pi * cfg.radius ** 3
-        gravity = -cfg.mass * cfg.gravity * n
-        buoyancy = float((cfg.water_density * cfg.gravity * volume * f_sub).sum())
-        wet_drag = float(-cfg.wet_drag_coefficient * (f_sub[:, None] * self.velocities)[:, 2].sum())
-        return {"gravity_force_z_N": float(gravity), "buoyancy_force_z_N": float(buoyancy),
-                "wet_drag_force_z_N": float(wet_drag), "net_body_force_z_N": float(gravity + buoyancy + wet_drag),
-                "submerged_volume_m3": float((volume * f_sub).sum())}
+        weight, lift, drag, frac = self._body_terms()
+        g = -cfg.mass * cfg.gravity * len(self.positions)
+        b = float(lift.sum())
+        w = float(-(drag * self.velocities[:, 2]).sum())
+        sphere = (4.0 / 3.0) * math.pi * cfg.radius ** 3
+        return {"gravity_force_z_N": float(g), "buoyancy_force_z_N": b, "wet_drag_force_z_N": w,
+                "net_body_force_z_N": float(g + b + w), "submerged_volume_m3": float((sphere * frac).sum())}
 
     @torch.no_grad()
     def bond_stored_energy(self, extension: torch.Tensor | None = None) -> torch.Tensor:
+        """Elastic energy of every pair's bond springs at its current extension:
+        one spring (linear law) or the equilibrium spring plus each Maxwell
+        branch stretched by its extension minus the branch's offset."""
         if extension is None:
             i, j = self.pairs.T
             extension = torch.linalg.vector_norm(self.positions[j] - self.positions[i], dim=1) - self.rest_lengths
         if self.bond_law is None:
-            return 0.5 * self.config.bond_stiffness * extension.square()
-        energy = 0.5 * float(self.bond_law.equilibrium_stiffness) * extension.square()
-        for a, k_a in enumerate(self.bond_law.branch_stiffness):
-            s = extension - self.branch_offsets[:, a]
-            energy = energy + 0.5 * float(k_a) * s.square()
+            springs = [(float(self.config.bond_stiffness), None)]
+        else:
+            springs = [(float(self.bond_law.equilibrium_stiffness), None)]
+            springs += [(float(k), self.branch_offsets[:, a]) for a, k in enumerate(self.bond_law.branch_stiffness)]
+        energy = torch.zeros_like(extension)
+        for k, offset in springs:
+            stretch = extension if offset is None else extension - offset
+            energy = energy + 0.5 * k * stretch.square()
         return energy
 
     @torch.no_grad()
@@ -986,28 +1013,28 @@ class IceDEM3D:
         return cfg.bond_creep_force_fraction * self.unrelaxed_bond_stiffness * thr * self.rest_lengths
 
     def bond_law_report(self) -> dict[str, Any]:
+        """The bond law's parameters and state: stiffnesses, creep, strength
+        scatter and damage (the report of the reference's bonded-sphere model)."""
         cfg = self.config
-        payload: dict[str, Any] = {
-            "bond_model": cfg.bond_model,
-            "unrelaxed_stiffness_N_m": self.unrelaxed_bond_stiffness,
-            "relaxed_stiffness_N_m": (float(self.bond_law.equilibrium_stiffness) if self.bond_law is not None
-                                      else float(cfg.bond_stiffness)),
-            "creep_exponent": float(cfg.bond_creep_exponent),
-            "creep_time_s": float(cfg.bond_creep_time_s),
-            "cumulative_bond_dissipation_J": self.cumulative_bond_dissipation_J,
-            "creep_failed_bonds": int((self.failure_mode == 4).sum()),
-            "strength_weibull_modulus": float(cfg.bond_strength_weibull_modulus),
-            "strength_weibull_seed": int(cfg.bond_strength_seed),
-            "max_bond_damage": float(self.bond_damage.max()) if len(self.bond_damage) else 0.0,
-        }
-        if self.bond_breaking_strain is not None:
-            payload["bond_breaking_strain_median"] = float(self.bond_breaking_strain.median())
-            payload["bond_breaking_strain_min"] = float(self.bond_breaking_strain.min())
-            payload["bond_breaking_strain_max"] = float(self.bond_breaking_strain.max())
-        if self.bond_law is not None:
-            payload["branch_stiffness_N_m"] = [float(k) for k in self.bond_law.branch_stiffness]
-            payload["relaxation_time_s"] = [float(t) for t in self.bond_law.relaxation_time]
-        return payload
+        law = self.bond_law
+        report: dict[str, Any] = dict(
+            bond_model=cfg.bond_model,
+            unrelaxed_stiffness_N_m=self.unrelaxed_bond_stiffness,
+            relaxed_stiffness_N_m=float(cfg.bond_stiffness if law is None else law.equilibrium_stiffness),
+            creep_exponent=float(cfg.bond_creep_exponent), creep_time_s=float(cfg.bond_creep_time_s),
+            cumulative_bond_dissipation_J=self.cumulative_bond_dissipation_J,
+            creep_failed_bonds=int((self.failure_mode == 4).sum()),
+            strength_weibull_modulus=float(cfg.bond_strength_weibull_modulus),
+            strength_weibull_seed=int(cfg.bond_strength_seed),
+            max_bond_damage=float(self.bond_damage.max()) if len(self.bond_damage) else 0.0)
+        strain = self.bond_breaking_strain
+        if strain is not None:
+            for name, value in (("median", strain.median()), ("min", strain.min()), ("max", strain.max())):
+                report[f"bond_breaking_strain_{name}"] = float(value)
+        if law is not None:
+            report["branch_stiffness_N_m"] = list(map(float, law.branch_stiffness))
+            report["relaxation_time_s"] = list(map(float, law.relaxation_time))
+        return report
 
     @torch.no_grad()
     def lateral_platen_energy(self) -> float:
@@ -1054,39 +1081,32 @@ class IceDEM3D:
 
     @torch.no_grad()
     def diagnostics(self, external_forces: torch.Tensor | None = None) -> dict[str, Any]:
-        """Full diagnostic snapshot (dem3d.py:1665-1738)."""
+        """Full diagnostic record (the keys of the reference's dem3d.py:1665-1738):
+        clock and tool, reactions from a side-effect-free force probe, the
+        stored energies (the probe's contact energy from the device ledger),
+        the platen state and the body-force totals."""
         force, reaction = self.forces(external_forces, update_fracture=False, update_history=False)
-        led = self.read_ledger()
         support = -force[self.fixed].sum(dim=0)
-        kinetic = 0.5 * self.config.mass * self.velocities.square().sum()
-        bond_energy = (self.bond_stored_energy() * self.alive).sum()
-        contact_energy = float(led[_lib.L3_CONTACT_ENERGY])
-        tool_energy = self._tool_energy()
-        platen_energy = self._platen_energy()
+        parts = dict(kinetic_energy_J=float(0.5 * self.config.mass * self.velocities.square().sum()),
+                     bond_elastic_energy_J=float((self.bond_stored_energy() * self.alive).sum()),
+                     particle_contact_energy_J=float(self.read_ledger()[_lib.L3_CONTACT_ENERGY]),
+                     tool_contact_energy_J=self._tool_energy(), platen_contact_energy_J=self._platen_energy())
         lateral = self.lateral_platen_energy()
-        tp = self.tool_position
-        return {
-            "time": self.time,
-            "tool_x": float(tp[0]), "tool_y": float(tp[1]), "tool_z": float(tp[2]),
-            "reaction_x": float(reaction[0]), "reaction_y": float(reaction[1]), "reaction_z": float(reaction[2]),
-            "top_platen_reaction_z_N": float(self.last_top_platen_reaction_z),
-            "bottom_platen_reaction_z_N": float(self.last_bottom_platen_reaction_z),
-            "boundary_reaction_x": float(support[0]), "boundary_reaction_y": float(support[1]),
-            "boundary_reaction_z": float(support[2]),
-            "broken_bonds": self.broken_bonds,
-            "particle_count": len(self.positions),
-            "kinetic_energy_J": float(kinetic),
-            "bond_elastic_energy_J": float(bond_energy),
-            "particle_contact_energy_J": contact_energy,
-            "tool_contact_energy_J": tool_energy,
-            "platen_contact_energy_J": platen_energy,
-            "released_bond_energy_J": float(self.failure_energy_J.sum()),
-            "lateral_platen_reaction": [float(v) for v in self.last_lateral_platen_reaction],
-            "lateral_platen_energy_J": lateral,
-            "mechanical_energy_J": float(kinetic + bond_energy + contact_energy + tool_energy + platen_energy
-                                         + lateral),
-            **self.body_force_ledger(),
-        }
+        record: dict[str, Any] = {"time": self.time}
+        record.update(zip(("tool_x", "tool_y", "tool_z"), map(float, self.tool_position)))
+        record.update(zip(("reaction_x", "reaction_y", "reaction_z"), map(float, reaction)))
+        record["top_platen_reaction_z_N"] = float(self.last_top_platen_reaction_z)
+        record["bottom_platen_reaction_z_N"] = float(self.last_bottom_platen_reaction_z)
+        record.update(zip(("boundary_reaction_x", "boundary_reaction_y", "boundary_reaction_z"), map(float, support)))
+        record["broken_bonds"] = self.broken_bonds
+        record["particle_count"] = len(self.positions)
+        record.update(parts)
+        record["released_bond_energy_J"] = float(self.failure_energy_J.sum())
+        record["lateral_platen_reaction"] = [float(v) for v in self.last_lateral_platen_reaction]
+        record["lateral_platen_energy_J"] = lateral
+        record["mechanical_energy_J"] = sum(parts.values()) + lateral
+        record.update(self.body_force_ledger())
+        return record
 
     @torch.no_grad()
     def energy(self) -> dict[str, float]:
@@ -1128,28 +1148,43 @@ class IceDEM3D:
             },
         }
 
+    def _check_checkpoint_config(self, saved) -> None:
+        """The checkpoint's configuration, completed with the defaults of
+        fields added since, must equal this solver's (the device aside)."""
+        if not isinstance(saved, dict):
+            raise ValueError("checkpoint config must be a dictionary")
+        mine = asdict(self.config)
+        theirs = {**asdict(DEM3DConfig()), **saved}
+        mine["device"] = theirs["device"] = "cuda"  # an execution choice, not physical state
+        if {k: (tuple(v) if isinstance(v, list) else v) for k, v in theirs.items()} != mine:
+            raise ValueError("checkpoint config does not match this solver configuration")
+
+    def _checkpoint_tensor(self, name: str, value, target: torch.Tensor) -> torch.Tensor:
+        if not isinstance(value, torch.Tensor) or tuple(value.shape) != tuple(target.shape):
+            raise ValueError(f"checkpoint {name} must be a tensor with shape {tuple(target.shape)}")
+        if value.dtype != target.dtype:
+            raise ValueError(f"checkpoint {name} dtype must be {target.dtype}, got {value.dtype}")
+        value = value.to(device=self.device)
+        if value.is_floating_point() and not bool(torch.isfinite(value).all()):
+            raise ValueError(f"checkpoint {name} contains non-finite values")
+        return value
+
     @torch.no_grad()
     def load_state_dict(self, state: dict[str, Any]) -> None:
-        """Restore a ``state_dict`` snapshot after strict validation (dem3d.py:1855-1967)."""
+        """Restore a ``state_dict`` snapshot; every check runs before anything is
+        written, so a rejected checkpoint leaves the solver unchanged (the
+        restart rules of the reference's dem3d.py:1855-1967: same keys, same
+        configuration and dt, tensors of the solver's shapes and dtypes, finite,
+        the same lattice, pairs, bonds and supports, a bond-law state when the
+        law is rate dependent)."""
         if not isinstance(state, dict):
             raise TypeError("state must be a dictionary returned by state_dict()")
-        required = {"dimension", "config", "dt", "time", "step_count", "positions", "velocities",
-                    "initial_positions", "fixed", "pairs", "bonded", "alive", "failure_mode", "failure_time_s",
-                    "failure_extension_m", "failure_energy_J"}
-        missing = required.difference(state)
+        missing = _CHECKPOINT_KEYS.difference(state)
         if missing:
             raise ValueError(f"checkpoint is missing keys: {sorted(missing)}")
         if state["dimension"] != 3:
             raise ValueError("checkpoint dimension must be 3")
-        saved = state["config"]
-        if not isinstance(saved, dict):
-            raise ValueError("checkpoint config must be a dictionary")
-        mine = asdict(self.config)
-        merged = {**asdict(DEM3DConfig()), **saved}
-        # the device is an execution choice, not physical state
-        merged["device"], mine["device"] = "cuda", "cuda"
-        if {k: (tuple(v) if isinstance(v, list) else v) for k, v in merged.items()} != mine:
-            raise ValueError("checkpoint config does not match this solver configuration")
+        self._check_checkpoint_config(state["config"])
         if not math.isfinite(float(state["dt"])) or float(state["dt"]) != self.dt:
             raise ValueError("checkpoint dt does not match this solver")
         time_value = float(state["time"])
@@ -1158,49 +1193,31 @@ class IceDEM3D:
             raise ValueError("checkpoint time must be finite and nonnegative")
         if isinstance(step_value, bool) or not isinstance(step_value, int) or step_value < 0:
             raise ValueError("checkpoint step_count must be a nonnegative integer")
-        names = ("positions", "velocities", "initial_positions", "fixed", "pairs", "bonded", "alive",
-                 "failure_mode", "failure_time_s", "failure_extension_m", "failure_energy_J")
-        staged = {}
-        for name in names:
-            value, target = state[name], getattr(self, name)
-            if not isinstance(value, torch.Tensor) or tuple(value.shape) != tuple(target.shape):
-                raise ValueError(f"checkpoint {name} must be a tensor with shape {tuple(target.shape)}")
-            if value.dtype != target.dtype:
-                raise ValueError(f"checkpoint {name} dtype must be {target.dtype}, got {value.dtype}")
-            value = value.to(device=self.device)
-            if value.is_floating_point() and not bool(torch.isfinite(value).all()):
-                raise ValueError(f"checkpoint {name} contains non-finite values")
-            staged[name] = value
-        if not torch.equal(staged["initial_positions"], self.initial_positions):
-            raise ValueError("checkpoint reference geometry does not match this solver")
-        if not torch.equal(staged["pairs"], self.pairs):
-            raise ValueError("checkpoint pair topology does not match this solver")
-        if not torch.equal(staged["bonded"], self.bonded):
-            raise ValueError("checkpoint bond topology does not match this solver")
+        staged = {name: self._checkpoint_tensor(name, state[name], getattr(self, name))
+                  for name in _CHECKPOINT_TENSORS}
+        for name, message in _CHECKPOINT_FROZEN:
+            if not torch.equal(staged[name], getattr(self, name)):
+                raise ValueError(message)
         if bool((staged["alive"] & ~staged["bonded"]).any()):
             raise ValueError("checkpoint marks a non-bond pair as alive")
-        if not torch.equal(staged["fixed"], self.fixed):
-            raise ValueError("checkpoint fixed-boundary mask does not match this solver")
         bond_state = state.get("bond_law")
         if self.bond_law is not None:
             if not isinstance(bond_state, dict):
                 raise ValueError("checkpoint has no bond-law state but the solver uses a rate-dependent bond")
-            b = len(self.pairs)
-            checks = (("branch_offsets", tuple(self.branch_offsets.shape)), ("damage", (b,)),
-                      ("elongation_prev", (b,)))
-            for key, shape in checks:
+            for key, shape in (("branch_offsets", tuple(self.branch_offsets.shape)), ("damage", (len(self.pairs),)),
+                               ("elongation_prev", (len(self.pairs),))):
                 v = bond_state.get(key)
                 if not isinstance(v, torch.Tensor) or tuple(v.shape) != shape or v.dtype != self.dtype:
                     raise ValueError(f"checkpoint {key} must be a {self.dtype} tensor with shape {shape}")
                 if not bool(torch.isfinite(v).all()):
                     raise ValueError("checkpoint bond-law state is non-finite")
-        for name in names:
-            getattr(self, name).copy_(staged[name])
+        for name, value in staged.items():
+            getattr(self, name).copy_(value)
         self._fixed_u8 = self.fixed.to(torch.uint8)
         if self.bond_law is not None:
-            self.branch_offsets.copy_(bond_state["branch_offsets"].to(self.device))
-            self.bond_damage.copy_(bond_state["damage"].to(self.device))
-            self._bond_elongation_prev.copy_(bond_state["elongation_prev"].to(self.device))
+            for attr, key in (("branch_offsets", "branch_offsets"), ("bond_damage", "damage"),
+                              ("_bond_elongation_prev", "elongation_prev")):
+                getattr(self, attr).copy_(bond_state[key].to(self.device))
             self.cumulative_bond_dissipation_J = float(bond_state.get("cumulative_bond_dissipation_J", 0.0))
         self.time = time_value
         self.step_count = step_value

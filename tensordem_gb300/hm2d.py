@@ -63,6 +63,8 @@ class HM2DConfig:
     indenter_velocity: tuple[float, float] = (0.0, 0.0)
     indenter_radius: float = 0.0
     load_capacity: int = 0
+    # FP32 engines: 64 sums each particle's terms in FP64 (else float-float)
+    sum_precision: int = 32
 
     @property
     def box(self) -> tuple[float, float]:
@@ -85,6 +87,7 @@ class HM2DConfig:
         c.indenter_velocity[0], c.indenter_velocity[1] = self.indenter_velocity
         c.indenter_radius = self.indenter_radius
         c.load_capacity = self.load_capacity
+        c.sum_precision = self.sum_precision
         return c
 
 
@@ -171,6 +174,7 @@ class HM2D:
         _lib.check(rc, None, "tdem_hm_create")
         self._h = h
         self.steps = 0
+        self._anchor = torch.zeros(1, device=self.device)  # the device of the torch ops
         # TDEM_GRAPH=0 runs steps as plain launches (profilers cannot see
         # kernels inside conditional CUDA graphs); results are identical.
         if os.environ.get("TDEM_GRAPH", "1") == "0":
@@ -207,9 +211,9 @@ class HM2D:
 
     def step(self, n_steps: int = 1, *, check: bool = True) -> None:
         """Advance n velocity-Verlet steps (one graph launch)."""
+        from . import ops
         with torch.cuda.device(self.device):
-            rc = self._lib.tdem_hm_step(self._h, int(n_steps), self._stream())
-            _lib.check(rc, self._h, "tdem_hm_step")
+            ops.hm_step(self._h.value, int(n_steps), self._anchor)
             self.steps += int(n_steps)
             if check:
                 self.check()
@@ -226,11 +230,9 @@ class HM2D:
                    omega=torch.empty(n, dtype=torch.float64, device=self.device),
                    force=torch.empty((n, 2), dtype=torch.float64, device=self.device),
                    torque=torch.empty(n, dtype=torch.float64, device=self.device))
+        from . import ops
         with torch.cuda.device(self.device):
-            rc = self._lib.tdem_hm_read_state(self._h, out["pos"].data_ptr(), out["vel"].data_ptr(),
-                                              out["omega"].data_ptr(), out["force"].data_ptr(),
-                                              out["torque"].data_ptr(), 0, self._stream())
-        _lib.check(rc, self._h, "tdem_hm_read_state")
+            ops.hm_read_state(self._h.value, out["pos"], out["vel"], out["omega"], out["force"], out["torque"])
         return out
 
     def read_state_host(self, pos: np.ndarray, vel: np.ndarray, omega: np.ndarray) -> None:

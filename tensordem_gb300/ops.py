@@ -74,3 +74,36 @@ def icedem_forces(handle: int, positions: torch.Tensor, velocities: torch.Tensor
                                        out_force.data_ptr(), out_reaction.data_ptr(),
                                        _stream(positions))
     _lib.check(rc, C.c_void_p(handle), "tdem_icedem_forces")
+
+
+# ---------------------------------------------------------------------------
+# Hertz-Mindlin engine (HM2D) and the batched engine (Batch). Their state lives
+# in the native engine; ``anchor`` is a small CUDA tensor of the engine's
+# device that gives the op its device (for dispatch and the current stream).
+
+
+@torch.library.custom_op(f"{_NS}::hm_step", mutates_args=())
+def hm_step(handle: int, n_steps: int, anchor: torch.Tensor) -> None:
+    """``n_steps`` velocity-Verlet steps of a Hertz-Mindlin engine (one
+    conditional CUDA graph launch; the step of IceDEM.step, dem.py:347-382,
+    for the Hertz-Mindlin disc engine)."""
+    rc = _lib.lib().tdem_hm_step(C.c_void_p(handle), int(n_steps), _stream(anchor))
+    _lib.check(rc, C.c_void_p(handle), "tdem_hm_step")
+
+
+@torch.library.custom_op(f"{_NS}::hm_read_state", mutates_args=("pos", "vel", "omega", "force", "torque"))
+def hm_read_state(handle: int, pos: torch.Tensor, vel: torch.Tensor, omega: torch.Tensor, force: torch.Tensor,
+                  torque: torch.Tensor) -> None:
+    """Integer-time state of a Hertz-Mindlin engine in original disc order into
+    FP64 CUDA tensors: positions, velocities, spins, forces and torques."""
+    rc = _lib.lib().tdem_hm_read_state(C.c_void_p(handle), pos.data_ptr(), vel.data_ptr(), omega.data_ptr(),
+                                       force.data_ptr(), torque.data_ptr(), 0, _stream(pos))
+    _lib.check(rc, C.c_void_p(handle), "tdem_hm_read_state")
+
+
+@torch.library.custom_op(f"{_NS}::batch_step", mutates_args=())
+def batch_step(handle: int, n_steps: int, anchor: torch.Tensor) -> None:
+    """``n_steps`` steps of every live instance of a batched engine (one
+    conditional CUDA graph launch)."""
+    rc = _lib.lib().tdem_batch_step(C.c_void_p(handle), int(n_steps), _stream(anchor))
+    _lib.check(rc, C.c_void_p(handle), "tdem_batch_step")

@@ -296,3 +296,25 @@ def test_full_size_settling_case_runs(hm):
     led = e.ledger()
     assert led["evals"] == 20 and led["status"] == 0
     assert math.isfinite(led["total"])
+
+
+def test_fp64_sum_form_within_the_fp32_bound(hm):
+    """The FP64-sum form of the FP32 engine (each particle's force and torque
+    terms summed in FP64, sum_precision=64) against the FP64 oracle: the FP32
+    single-evaluation bound (2e-3 normwise), and after 100 steps the same
+    state as the default float-float form to FP32 rounding (1e-5 of the box)."""
+    from dataclasses import replace
+    cfg, st = dense_gas(24, seed=4, precision=32)
+    st["pos"][1] = st["pos"][0] + np.array([st["radius"][0] + st["radius"][1] - 3e-6, 0.0])
+    runs = {}
+    for sums in (32, 64):
+        e = _engine(hm, replace(cfg, sum_precision=sums), st)
+        s = e.state()
+        o = oracle_for(cfg, dict(st, pos=_np(s["pos"])))
+        f, _, _ = o.evaluate(o.pos, o.vel, o.omega, advance=False)
+        err = _rel(_np(s["force"]), f)
+        print(f"sum_precision {sums}: single-evaluation normwise force error {err:.2e}")
+        assert err <= 2e-3
+        e.step(100)
+        runs[sums] = _np(e.state()["pos"])
+    assert np.abs(runs[32] - runs[64]).max() <= 1e-5 * cfg.box[0]
