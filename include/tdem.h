@@ -341,6 +341,13 @@ int tdem_hm_rebuild_pending(tdem_hm* h, void* stream);
 int tdem_hm_num_variants(void);
 int tdem_hm_set_variant(tdem_hm* h, int variant);
 int tdem_hm_get_variant(const tdem_hm* h);
+/* SM clock cycles a bounded wait of the bulk-copy step kernels (variants 4-6)
+ * may take before the kernel records a timeout, drains its copies in flight
+ * and returns (default ~2e9, about a second). For tests of the failure path:
+ * a short budget makes the waits run out; the next status check then fails
+ * with TDEM_ERR_CUDA, and the engine recovers with set_state. No counterpart
+ * in the reference (it has no device waits). */
+int tdem_hm_set_wait_budget(tdem_hm* h, int64_t cycles);
 int tdem_hm_autotune(tdem_hm* h, int steps, float* ms_out, void* stream);
 
 /* Allocation-free contact forces. No counterpart in the reference: it exists
@@ -659,6 +666,12 @@ int tdem_icedem3d_step(tdem_icedem3d* h, const tdem_icedem3d_state* st, const do
  * or by size (lanes while a 16-lane group fits every particle; the default). */
 enum { TDEM_ICE3D_MAP_AUTO = 0, TDEM_ICE3D_MAP_LANES = 1, TDEM_ICE3D_MAP_PARTICLE = 2 };
 int tdem_icedem3d_set_mapping(tdem_icedem3d* h, int mapping);
+/* Naps of 64 ns a grid barrier of the cooperative step may wait before the
+ * block records a timeout and returns (default 2^24, about a second). For
+ * tests of the failure path: a short limit makes the barriers run out; the
+ * launch then fails with TDEM_ERR_CUDA ("grid barrier timed out") and the
+ * next launch starts clean. No counterpart in the reference. */
+int tdem_icedem3d_set_barrier_spins(tdem_icedem3d* h, uint64_t spins);
 
 /* Ledger of the last call (TDEM_L3_COUNT doubles). Synchronizes `stream`. */
 int tdem_icedem3d_read_ledger(tdem_icedem3d* h, double* out_host, int count, void* stream);

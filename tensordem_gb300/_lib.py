@@ -209,6 +209,8 @@ def _declare(lib: C.CDLL) -> None:
         "tdem_hm_read_history": (i32, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
         "tdem_hm_last_error": (i32, [vp, C.c_char_p, C.c_size_t]),
         "tdem_hm_contact_law": (i32, [C.POINTER(HMConfigC), C.c_int64, vp, vp, vp]),
+        "tdem_hm_set_wait_budget": (i32, [vp, C.c_int64]),
+        "tdem_icedem3d_set_barrier_spins": (i32, [vp, C.c_uint64]),
         "tdem_batch_bytes": (i32, [C.POINTER(BatchConfigC), C.POINTER(C.c_int64)]),
         "tdem_batch_create": (i32, [C.POINTER(BatchConfigC), C.POINTER(vp)]),
         "tdem_batch_destroy": (None, [vp]),

@@ -59,6 +59,7 @@ struct EngineBase {
   virtual int autotune(int steps, cudaStream_t s, float* ms_out) = 0;
   virtual int rebuild(cudaStream_t s) = 0;
   virtual int read_history(int* pairs, double* xi, long long capacity, long long* count, cudaStream_t s) = 0;
+  virtual int set_wait_budget(long long cycles) = 0;
   std::string err;
 };
 
@@ -213,8 +214,9 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 // Step-kernel variants the autotuner chooses from: 0 = one thread per
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
 // block shapes; 4..5 = bulk-copy staging of own state; 6 = neighbour window in
-// shared memory (FP32 engines; an FP64 engine runs variant 1's kernel).
-constexpr int kVariants = 7;
+// shared memory (FP32 engines; an FP64 engine runs variant 1's kernel);
+// 7..8 = two particle streams per thread at two block shapes.
+constexpr int kVariants = 9;
 constexpr int kWindowVariant = 6;
 
 template <class T>
@@ -247,6 +249,8 @@ StepFn<T> step_fn_feat(int variant, int mode) {
       case 4: return &force_kernel_bulk<T, kPrime, 256, 3, F>;
       case 5: return &force_kernel_bulk<T, kPrime, 128, 6, F>;
       case 6: return window_fn<T, kPrime, F>();
+      case 7: return &force_kernel_pf2<T, kPrime, 256, 2, F>;
+      case 8: return &force_kernel_pf2<T, kPrime, 128, 4, F>;
       default: return &force_kernel<T, kPrime, F>;
     }
   }
@@ -257,6 +261,8 @@ StepFn<T> step_fn_feat(int variant, int mode) {
     case 4: return &force_kernel_bulk<T, kStep, 256, 3, F>;
     case 5: return &force_kernel_bulk<T, kStep, 128, 6, F>;
     case 6: return window_fn<T, kStep, F>();
+    case 7: return &force_kernel_pf2<T, kStep, 256, 2, F>;
+    case 8: return &force_kernel_pf2<T, kStep, 128, 4, F>;
     default: return &force_kernel<T, kStep, F>;
   }
 }
@@ -272,7 +278,7 @@ StepFn<T> step_fn(int variant, int mode, bool feat, bool sum64 = false) {
 template <class T>
 inline int variant_block(int variant) {
   if (variant == kWindowVariant) return sizeof(T) == 4 ? kWinThreads : 256;
-  return (variant == 2 || variant == 5) ? 128 : 256;
+  return (variant == 2 || variant == 5 || variant == 8) ? 128 : 256;
 }
 
 // Dynamic shared memory of a variant's step kernel.
@@ -898,6 +904,13 @@ struct Engine final : EngineBase {
 
   int get_variant() const override { return variant; }
 
+  int set_wait_budget(long long cycles) override {
+    if (cycles < 0) return tdem::fail(&err, TDEM_ERR_BADARG, "wait budget must be >= 0");
+    P.wait_budget = cycles;
+    destroy_graphs();  // the step graph holds the parameters by value
+    return TDEM_OK;
+  }
+
   // Time `steps` steps with every variant (advancing the simulation) and keep
   // the fastest. Per-particle arithmetic is identical in all variants.
   int autotune(int steps, cudaStream_t s, float* ms_out) override {
@@ -1126,6 +1139,11 @@ int tdem_hm_set_variant(tdem_hm* h, int variant) {
 }
 
 int tdem_hm_get_variant(const tdem_hm* h) { return h ? h->e->get_variant() : -1; }
+
+int tdem_hm_set_wait_budget(tdem_hm* h, int64_t cycles) {
+  if (!h) return TDEM_ERR_BADARG;
+  return h->e->set_wait_budget((long long)cycles);
+}
 
 int tdem_hm_autotune(tdem_hm* h, int steps, float* ms_out, void* stream) {
   if (!h || steps < 1) return TDEM_ERR_BADARG;

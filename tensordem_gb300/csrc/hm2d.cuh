@@ -99,6 +99,9 @@ struct Params {
   float eps_t_lo, eps_t_hi, eps_s_lo, eps_s_hi;
   // indenter centre at evaluation 0 and its displacement per evaluation
   float ind_x0f, ind_y0f, ind_dxf, ind_dyf;
+  // SM clock cycles a bounded wait of the bulk-copy kernels may take (about
+  // a second by default; tests of the failure path shorten it)
+  long long wait_budget;
 };
 
 constexpr unsigned kBondIdx = (1u << 29) - 1u;

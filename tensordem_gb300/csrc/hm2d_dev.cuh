@@ -983,6 +983,69 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
   commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
+// Two-stream variant: each thread walks two interleaved particle streams
+// (particles i and i + stride of a 2 x stride grid window per iteration),
+// with both streams' next particles prefetched and both particles' partner
+// gathers issued together before either is computed, so two dependent
+// gather chains are in flight per thread instead of one.
+template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
+__global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf2(Params<T> P, Bufs<T> B,
+                                                                cudaGraphConditionalHandle h_rebuild,
+                                                                cudaGraphConditionalHandle h_loop, int use_cond,
+                                                                int primed, StepHint hint) {
+  static_assert(MODE != kPeek, "read-back uses force_kernel");
+  const StepCtl c = load_step_ctl(B.ctl, hint);
+  const int sp = c.sp, lp = c.lp;
+  const long long eval = c.evals;
+  const int n = P.n;
+  const int stride = gridDim.x * BLOCK;
+  const GlobalFetch<T> fetch{B.pos[sp], B.vel[sp]};
+  ThreadLedger<T> L;
+  int i = blockIdx.x * BLOCK + threadIdx.x;
+  V4<T> pa{}, va{}, pb{}, vb{};
+  uint4 ha = make_uint4(0u, 0u, 0u, 0u), hb = ha;
+  if (i < n) {
+    pa = B.pos[sp][i];
+    va = B.vel[sp][i];
+    ha = B.head[lp][i];
+  }
+  if (i + stride < n) {
+    pb = B.pos[sp][i + stride];
+    vb = B.vel[sp][i + stride];
+    hb = B.head[lp][i + stride];
+  }
+  while (i < n) {
+    const int nx = i + 2 * stride;
+    V4<T> pan{}, van{}, pbn{}, vbn{};
+    uint4 han = make_uint4(0u, 0u, 0u, 0u), hbn = han;
+    if (nx < n) {
+      pan = B.pos[sp][nx];
+      van = B.vel[sp][nx];
+      han = B.head[lp][nx];
+    }
+    if (nx + stride < n) {
+      pbn = B.pos[sp][nx + stride];
+      vbn = B.vel[sp][nx + stride];
+      hbn = B.head[lp][nx + stride];
+    }
+    V4<T> qa0{}, qa1{}, qa2{}, qb0{}, qb1{}, qb2{};
+    load_head_partners<T>(fetch, ha, qa0, qa1, qa2);
+    load_head_partners<T>(fetch, hb, qb0, qb1, qb2);
+    process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, pa, va, ha, qa0, qa1, qa2, primed, eval, L);
+    if (i + stride < n)
+      process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i + stride, pb, vb, hb, qb0, qb1, qb2, primed, eval,
+                                        L);
+    i = nx;
+    pa = pan;
+    va = van;
+    ha = han;
+    pb = pbn;
+    vb = vbn;
+    hb = hbn;
+  }
+  commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
+}
+
 // Neighbour-window variant (FP32). Each CTA (one per SM) owns a contiguous
 // range of sorted particles and walks it two ring blocks (2 x 256 particles)
 // per iteration. Positions and velocities of a sliding window of sorted
@@ -1055,21 +1118,25 @@ __global__ void __launch_bounds__(kWinThreads, 1) force_kernel_win(Params<T> P, 
   if (tid == 0 && b0 < b1) issue_upto(b0);
   int waited_pv = first - 1;  // highest ring block this thread has seen complete
   int waited_hd = b0 - 1;     // highest head block this thread has seen complete
-  bool ok = true;
+  bool ok = true, failed = false;
   for (int k = b0; k < b1; k += 2) {
     // the window's new blocks and this iteration's heads
     const int need = min(last, k + 1 + kWinHalo);
     while (ok && waited_pv < need) {
       const int r = waited_pv + 1 - first;
-      ok = bulk::mbar_wait_bounded(&bar[r & (kWinSlots - 1)], (uint32_t)((r >> 4) & 1), kWaitBudget);
+      ok = bulk::mbar_wait_bounded(&bar[r & (kWinSlots - 1)], (uint32_t)((r >> 4) & 1), P.wait_budget);
       if (ok) ++waited_pv;
     }
     while (ok && waited_hd < min(k + 1, b1 - 1)) {
       const int r = waited_hd + 1 - b0;
-      ok = bulk::mbar_wait_bounded(&bar[kWinSlots + (r & (kWinHeads - 1))], (uint32_t)((r >> 3) & 1), kWaitBudget);
+      ok = bulk::mbar_wait_bounded(&bar[kWinSlots + (r & (kWinHeads - 1))], (uint32_t)((r >> 3) & 1),
+                                   P.wait_budget);
       if (ok) ++waited_hd;
     }
-    if (__syncthreads_or(!ok)) break;
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
     const int blk = k + (tid >= kWinBlock ? 1 : 0);
     const int i = blk * kWinBlock + (tid & (kWinBlock - 1));
     if (blk < b1 && i < n) {
@@ -1088,7 +1155,7 @@ __global__ void __launch_bounds__(kWinThreads, 1) force_kernel_win(Params<T> P, 
     __syncthreads();  // every thread is done with the slots the next copies overwrite
     if (tid == 0) issue_upto(k + 2);
   }
-  if (!ok) {
+  if (failed) {
     if (tid == 0) {
       atomicOr(&B.ctl->status, (int)kStatusTimeout);
       // drain the copies in flight before the CTA's shared memory is released
@@ -1150,9 +1217,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_bulk(Params<T> P, Bu
     const int next = tile + gridDim.x;
     // buf ^ 1 was released by the barrier that ended the previous iteration
     if (threadIdx.x == 0 && next < ntiles) issue(next, buf ^ 1);
-    const bool ok = bulk::mbar_wait_bounded(&s_bar[buf], (uint32_t)((k >> 1) & 1), kWaitBudget);
+    const bool ok = bulk::mbar_wait_bounded(&s_bar[buf], (uint32_t)((k >> 1) & 1), P.wait_budget);
     if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicOr(&B.ctl->status, (int)kStatusTimeout);
+      if (threadIdx.x == 0) {
+        atomicOr(&B.ctl->status, (int)kStatusTimeout);
+        // let the copies in flight land before the block's shared memory goes
+        bulk::mbar_wait_bounded(&s_bar[buf], (uint32_t)((k >> 1) & 1), kWaitBudget);
+        if (next < ntiles) bulk::mbar_wait_bounded(&s_bar[buf ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kWaitBudget);
+      }
+      __syncthreads();
       break;
     }
     const int i = tile * BLOCK + threadIdx.x;
@@ -1708,6 +1781,7 @@ inline void make_params(const tdem_hm_config& c, int slots, Params<T>& P) {
   P.ind_y0f = (float)c.indenter_center[1];
   P.ind_dxf = (float)((double)P.dt * c.indenter_velocity[0]);
   P.ind_dyf = (float)((double)P.dt * c.indenter_velocity[1]);
+  P.wait_budget = kWaitBudget;
 }
 
 }  // namespace hm

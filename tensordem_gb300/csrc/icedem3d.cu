@@ -113,6 +113,7 @@ struct Dev {
   double* part;    // [grid, kPartials] per-block ledger partials
   double* pmin;    // [grid, 2] per-block min break margin, max history size
   double* pdiss;   // [grid] per-block dashpot dissipation of the launch
+  unsigned long long barrier_spins;  // naps a grid barrier may wait (kBarrierSpins; tests shorten it)
 };
 
 // Grid-wide barrier of a cooperative launch. The wait is bounded: when it
@@ -132,7 +133,7 @@ __device__ __noinline__ bool grid_sync(const Dev& D) {
     } else {
       unsigned long long spins = 0;
       while (*gen == g) {
-        if (++spins > kBarrierSpins) {
+        if (++spins > D.barrier_spins) {
           ok = 0;
           atomicOr(D.status, kStatusBarrier);
           break;
@@ -1720,6 +1721,7 @@ int tdem_icedem3d_create(const tdem_icedem3d_config* cfg, const tdem_icedem3d_to
   Dev& D = h->dev;
   unsigned H = 64;
   while (H < 2u * (unsigned)n) H <<= 1;
+  D.barrier_spins = kBarrierSpins;
   D.hmask = H - 1;
   int rc = 0;
   auto fail_out = [&](int code) {
@@ -1805,6 +1807,12 @@ int tdem_icedem3d_step(tdem_icedem3d* h, const tdem_icedem3d_state* st, const do
   if (n_steps < 1) return tdem::fail(&h->err, TDEM_ERR_BADARG, "n_steps must be >= 1");
   Out o{nullptr, 0, 1, 1, (long long)n_steps, time, h->mapping};
   return launch(h, st, loads, o, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int tdem_icedem3d_set_barrier_spins(tdem_icedem3d* h, uint64_t spins) {
+  if (!h) return TDEM_ERR_BADARG;
+  h->dev.barrier_spins = (unsigned long long)spins;
+  return TDEM_OK;
 }
 
 int tdem_icedem3d_set_mapping(tdem_icedem3d* h, int mapping) {
