@@ -344,7 +344,8 @@ int tdem_hm_get_variant(const tdem_hm* h);
 /* SM clock cycles a bounded wait of the bulk-copy step kernels (variants 4-6)
  * may take before the kernel records a timeout, drains its copies in flight
  * and returns (default ~2e9, about a second). For tests of the failure path:
- * a short budget makes the waits run out; the next status check then fails
+ * a budget of 0 makes each wait a single non-blocking probe of the copy it
+ * waits for, so the waits run out; the next status check then fails
  * with TDEM_ERR_CUDA, and the engine recovers with set_state. No counterpart
  * in the reference (it has no device waits). */
 int tdem_hm_set_wait_budget(tdem_hm* h, int64_t cycles);

@@ -53,8 +53,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0u;
 }
 
-// Wait for phase `parity` of `bar` for at most `budget` SM clock cycles.
+// Non-blocking probe of phase `parity` of `bar`.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0u;
+}
+
+// Wait for phase `parity` of `bar` for at most `budget` SM clock cycles. A
+// budget of 0 makes the wait one non-blocking probe (try_wait itself may
+// suspend until the phase completes), which tests of the failure path use.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long budget) {
+  if (budget <= 0) return mbar_test_wait(bar, parity);
   const long long start = clock64();
   while (!mbar_try_wait(bar, parity)) {
     if (clock64() - start > budget) return false;

@@ -214,9 +214,8 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 // Step-kernel variants the autotuner chooses from: 0 = one thread per
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
 // block shapes; 4..5 = bulk-copy staging of own state; 6 = neighbour window in
-// shared memory (FP32 engines; an FP64 engine runs variant 1's kernel);
-// 7..8 = two particle streams per thread at two block shapes.
-constexpr int kVariants = 9;
+// shared memory (FP32 engines; an FP64 engine runs variant 1's kernel).
+constexpr int kVariants = 7;
 constexpr int kWindowVariant = 6;
 
 template <class T>
@@ -249,8 +248,6 @@ StepFn<T> step_fn_feat(int variant, int mode) {
       case 4: return &force_kernel_bulk<T, kPrime, 256, 3, F>;
       case 5: return &force_kernel_bulk<T, kPrime, 128, 6, F>;
       case 6: return window_fn<T, kPrime, F>();
-      case 7: return &force_kernel_pf2<T, kPrime, 256, 2, F>;
-      case 8: return &force_kernel_pf2<T, kPrime, 128, 4, F>;
       default: return &force_kernel<T, kPrime, F>;
     }
   }
@@ -261,8 +258,6 @@ StepFn<T> step_fn_feat(int variant, int mode) {
     case 4: return &force_kernel_bulk<T, kStep, 256, 3, F>;
     case 5: return &force_kernel_bulk<T, kStep, 128, 6, F>;
     case 6: return window_fn<T, kStep, F>();
-    case 7: return &force_kernel_pf2<T, kStep, 256, 2, F>;
-    case 8: return &force_kernel_pf2<T, kStep, 128, 4, F>;
     default: return &force_kernel<T, kStep, F>;
   }
 }
@@ -278,7 +273,7 @@ StepFn<T> step_fn(int variant, int mode, bool feat, bool sum64 = false) {
 template <class T>
 inline int variant_block(int variant) {
   if (variant == kWindowVariant) return sizeof(T) == 4 ? kWinThreads : 256;
-  return (variant == 2 || variant == 5 || variant == 8) ? 128 : 256;
+  return (variant == 2 || variant == 5) ? 128 : 256;
 }
 
 // Dynamic shared memory of a variant's step kernel.

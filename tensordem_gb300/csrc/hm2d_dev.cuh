@@ -983,69 +983,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
   commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
-// Two-stream variant: each thread walks two interleaved particle streams
-// (particles i and i + stride of a 2 x stride grid window per iteration),
-// with both streams' next particles prefetched and both particles' partner
-// gathers issued together before either is computed, so two dependent
-// gather chains are in flight per thread instead of one.
-template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
-__global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf2(Params<T> P, Bufs<T> B,
-                                                                cudaGraphConditionalHandle h_rebuild,
-                                                                cudaGraphConditionalHandle h_loop, int use_cond,
-                                                                int primed, StepHint hint) {
-  static_assert(MODE != kPeek, "read-back uses force_kernel");
-  const StepCtl c = load_step_ctl(B.ctl, hint);
-  const int sp = c.sp, lp = c.lp;
-  const long long eval = c.evals;
-  const int n = P.n;
-  const int stride = gridDim.x * BLOCK;
-  const GlobalFetch<T> fetch{B.pos[sp], B.vel[sp]};
-  ThreadLedger<T> L;
-  int i = blockIdx.x * BLOCK + threadIdx.x;
-  V4<T> pa{}, va{}, pb{}, vb{};
-  uint4 ha = make_uint4(0u, 0u, 0u, 0u), hb = ha;
-  if (i < n) {
-    pa = B.pos[sp][i];
-    va = B.vel[sp][i];
-    ha = B.head[lp][i];
-  }
-  if (i + stride < n) {
-    pb = B.pos[sp][i + stride];
-    vb = B.vel[sp][i + stride];
-    hb = B.head[lp][i + stride];
-  }
-  while (i < n) {
-    const int nx = i + 2 * stride;
-    V4<T> pan{}, van{}, pbn{}, vbn{};
-    uint4 han = make_uint4(0u, 0u, 0u, 0u), hbn = han;
-    if (nx < n) {
-      pan = B.pos[sp][nx];
-      van = B.vel[sp][nx];
-      han = B.head[lp][nx];
-    }
-    if (nx + stride < n) {
-      pbn = B.pos[sp][nx + stride];
-      vbn = B.vel[sp][nx + stride];
-      hbn = B.head[lp][nx + stride];
-    }
-    V4<T> qa0{}, qa1{}, qa2{}, qb0{}, qb1{}, qb2{};
-    load_head_partners<T>(fetch, ha, qa0, qa1, qa2);
-    load_head_partners<T>(fetch, hb, qb0, qb1, qb2);
-    process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, pa, va, ha, qa0, qa1, qa2, primed, eval, L);
-    if (i + stride < n)
-      process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i + stride, pb, vb, hb, qb0, qb1, qb2, primed, eval,
-                                        L);
-    i = nx;
-    pa = pan;
-    va = van;
-    ha = han;
-    pb = pbn;
-    vb = vbn;
-    hb = hbn;
-  }
-  commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
-}
-
 // Neighbour-window variant (FP32). Each CTA (one per SM) owns a contiguous
 // range of sorted particles and walks it two ring blocks (2 x 256 particles)
 // per iteration. Positions and velocities of a sliding window of sorted
