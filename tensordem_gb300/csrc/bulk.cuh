@@ -78,5 +78,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return true;
 }
 
+// Per-thread asynchronous copies (cp.async, 16 bytes, L2 only) into shared
+// memory, in commit groups that complete in order. A thread waits only for
+// its own groups, so a thread that reads back only what it copied needs no
+// block barrier. The copies are plain loads that always complete.
+__device__ __forceinline__ void cp16(void* dst_smem, const void* src_gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst_smem)), "l"(src_gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// Wait until at most N of this thread's most recent groups are pending.
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 }  // namespace bulk
 }  // namespace tdem

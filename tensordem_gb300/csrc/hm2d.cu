@@ -214,9 +214,12 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 // Step-kernel variants the autotuner chooses from: 0 = one thread per
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
 // block shapes; 4..5 = bulk-copy staging of own state; 6 = neighbour window in
-// shared memory (FP32 engines; an FP64 engine runs variant 1's kernel).
-constexpr int kVariants = 7;
+// shared memory; 7..8 = per-thread cp.async pipeline, three discs deep, at 3
+// and 4 blocks per SM. Variants 6..8 are FP32 kernels; an FP64 engine runs
+// variant 1's kernel for them.
+constexpr int kVariants = 9;
 constexpr int kWindowVariant = 6;
+constexpr int kAsyncVariant = 7;
 
 template <class T>
 using StepFn = void (*)(Params<T>, Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int,
@@ -227,6 +230,15 @@ template <class T, int MODE, bool F>
 StepFn<T> window_fn() {
   if constexpr (sizeof(T) == 4)
     return &force_kernel_win<T, MODE, F>;
+  else
+    return &force_kernel_pf<T, MODE, 256, 3, F>;
+}
+
+// The cp.async pipeline for FP32 engines; variant 1's kernel for FP64.
+template <class T, int MODE, int MINB, bool F>
+StepFn<T> async_fn() {
+  if constexpr (sizeof(T) == 4)
+    return &force_kernel_async<T, MODE, 256, MINB, F>;
   else
     return &force_kernel_pf<T, MODE, 256, 3, F>;
 }
@@ -248,6 +260,8 @@ StepFn<T> step_fn_feat(int variant, int mode) {
       case 4: return &force_kernel_bulk<T, kPrime, 256, 3, F>;
       case 5: return &force_kernel_bulk<T, kPrime, 128, 6, F>;
       case 6: return window_fn<T, kPrime, F>();
+      case 7: return async_fn<T, kPrime, 3, F>();
+      case 8: return async_fn<T, kPrime, 4, F>();
       default: return &force_kernel<T, kPrime, F>;
     }
   }
@@ -258,6 +272,8 @@ StepFn<T> step_fn_feat(int variant, int mode) {
     case 4: return &force_kernel_bulk<T, kStep, 256, 3, F>;
     case 5: return &force_kernel_bulk<T, kStep, 128, 6, F>;
     case 6: return window_fn<T, kStep, F>();
+    case 7: return async_fn<T, kStep, 3, F>();
+    case 8: return async_fn<T, kStep, 4, F>();
     default: return &force_kernel<T, kStep, F>;
   }
 }
@@ -279,7 +295,10 @@ inline int variant_block(int variant) {
 // Dynamic shared memory of a variant's step kernel.
 template <class T>
 inline size_t variant_smem(int variant) {
-  return (variant == kWindowVariant && sizeof(T) == 4) ? kWinSmem : 0;
+  if (sizeof(T) != 4) return 0;
+  if (variant == kWindowVariant) return kWinSmem;
+  if (variant >= kAsyncVariant) return async_smem(256);
+  return 0;
 }
 
 template <class T>

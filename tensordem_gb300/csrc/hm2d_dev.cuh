@@ -983,6 +983,102 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
   commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
+// Shared memory of the pipelined kernel per thread: three list heads, two
+// own-state pairs and two sets of three partner positions, 16 bytes each.
+constexpr int kAsyncRecords = 3 + 2 * 2 + 2 * 3;
+constexpr size_t async_smem(int block) { return (size_t)kAsyncRecords * block * 16; }
+
+// Software-pipelined grid-stride variant (FP32). A disc's step is two
+// dependent gathers deep: its list head, then its partners' positions. Each
+// thread keeps three of its discs in flight through shared memory with
+// per-thread cp.async copies, so neither gather waits in the iteration that
+// needs it: while disc k is computed, the first three partner positions of
+// disc k+1, the own state of disc k+1 and the list head of disc k+2 land.
+// The copies live in shared memory, not registers, so the depth costs no
+// occupancy; each thread reads back only its own copies (no block barrier).
+// Layout, 16-byte records indexed [slot][thread]: heads [3], positions [2],
+// velocities [2], partner positions [2][3].
+template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
+__global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, Bufs<T> B,
+                                                                  cudaGraphConditionalHandle h_rebuild,
+                                                                  cudaGraphConditionalHandle h_loop, int use_cond,
+                                                                  int primed, StepHint hint) {
+  static_assert(MODE != kPeek, "read-back uses force_kernel");
+  static_assert(sizeof(V4<T>) == 16, "one 16-byte copy per record");
+  using bulk::cp16;
+  using bulk::cp_commit;
+  using bulk::cp_wait;
+  extern __shared__ uint4 async_smem_base[];
+  const StepCtl c = load_step_ctl(B.ctl, hint);
+  const int sp = c.sp, lp = c.lp;
+  const int t = threadIdx.x;
+  const int end = P.n;
+  const int stride = gridDim.x * BLOCK;
+  uint4* sh = async_smem_base;                                           // [3][BLOCK]
+  V4<T>* spos = reinterpret_cast<V4<T>*>(async_smem_base + 3 * BLOCK);  // [2][BLOCK]
+  V4<T>* svel = spos + 2 * BLOCK;                                        // [2][BLOCK]
+  V4<T>* sq = svel + 2 * BLOCK;                                          // [2][3][BLOCK]
+  const V4<T>* __restrict__ pos = B.pos[sp];
+  const V4<T>* __restrict__ vel = B.vel[sp];
+  const uint4* __restrict__ head = B.head[lp];
+  const GlobalFetch<T> fetch{pos, vel};
+  ThreadLedger<T> L;
+  // partner positions of the disc whose head sits in head slot h, into set s
+  auto gather = [&](int h, int s) {
+    const uint4 hd = sh[h * BLOCK + t];
+    const int cnt = (int)(hd.x & 0xFFu);
+    V4<T>* q = sq + (size_t)s * 3 * BLOCK + t;
+    if (cnt > 0) cp16(q, pos + hd.y);
+    if (cnt > 1) cp16(q + BLOCK, pos + hd.z);
+    if (cnt > 2) cp16(q + 2 * BLOCK, pos + hd.w);
+  };
+  int i = blockIdx.x * BLOCK + t;
+  // prologue: heads of the first two discs and the first disc's own state,
+  // then the first disc's partners
+  if (i < end) {
+    cp16(sh + t, head + i);
+    cp16(spos + t, pos + i);
+    cp16(svel + t, vel + i);
+  }
+  if (i + stride < end) cp16(sh + BLOCK + t, head + i + stride);
+  cp_commit();
+  cp_wait<0>();
+  if (i < end) gather(0, 0);
+  cp_commit();
+  int h0 = 0;  // head slot of disc k; disc k+1 uses h0+1, disc k+2 h0+2 (mod 3)
+  int s = 0;   // own-state and partner set of disc k; disc k+1 uses s^1
+  for (; i < end; i += stride) {
+    const int h1 = h0 == 2 ? 0 : h0 + 1, h2 = h1 == 2 ? 0 : h1 + 1;
+    const int i1 = i + stride, i2 = i1 + stride;
+    // group X_k: head of disc k+2, own state of disc k+1
+    if (i2 < end) cp16(sh + h2 * BLOCK + t, head + i2);
+    if (i1 < end) {
+      cp16(spos + (s ^ 1) * BLOCK + t, pos + i1);
+      cp16(svel + (s ^ 1) * BLOCK + t, vel + i1);
+    }
+    cp_commit();
+    cp_wait<2>();  // X_{k-1} landed: the head of disc k+1
+    // group Y_k: partners of disc k+1
+    if (i1 < end) gather(h1, s ^ 1);
+    cp_commit();
+    cp_wait<2>();  // Y_{k-1} landed: the partners of disc k
+    const uint4 hd = sh[h0 * BLOCK + t];
+    const V4<T> p = spos[s * BLOCK + t];
+    const V4<T> v = svel[s * BLOCK + t];
+    const V4<T>* q = sq + (size_t)s * 3 * BLOCK + t;
+    const int cnt = (int)(hd.x & 0xFFu);
+    V4<T> q0{}, q1{}, q2{};
+    if (cnt > 0) q0 = q[0];
+    if (cnt > 1) q1 = q[BLOCK];
+    if (cnt > 2) q2 = q[2 * BLOCK];
+    process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, c.evals, L);
+    h0 = h1;
+    s ^= 1;
+  }
+  cp_wait<0>();
+  commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
+}
+
 // Neighbour-window variant (FP32). Each CTA (one per SM) owns a contiguous
 // range of sorted particles and walks it two ring blocks (2 x 256 particles)
 // per iteration. Positions and velocities of a sliding window of sorted
