@@ -215,9 +215,10 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 // particle; 1..3 = persistent grid-stride with next-particle prefetch at three
 // block shapes; 4..5 = bulk-copy staging of own state; 6 = neighbour window in
 // shared memory; 7..8 = per-thread cp.async pipeline, three discs deep, at 3
-// and 4 blocks per SM. Variants 6..8 are FP32 kernels; an FP64 engine runs
-// variant 1's kernel for them.
-constexpr int kVariants = 9;
+// and 4 blocks per SM; 9..10 = the same pipeline with one 1024-thread CTA
+// per SM, CTA-major and warp-major chunk order. Variants 6..10 are FP32
+// kernels; an FP64 engine runs variant 1's kernel for them.
+constexpr int kVariants = 11;
 constexpr int kWindowVariant = 6;
 constexpr int kAsyncVariant = 7;
 
@@ -235,10 +236,10 @@ StepFn<T> window_fn() {
 }
 
 // The cp.async pipeline for FP32 engines; variant 1's kernel for FP64.
-template <class T, int MODE, int MINB, bool F>
+template <class T, int MODE, int MINB, bool F, int BLOCK = 256, bool WMAJ = false>
 StepFn<T> async_fn() {
   if constexpr (sizeof(T) == 4)
-    return &force_kernel_async<T, MODE, 256, MINB, F>;
+    return &force_kernel_async<T, MODE, BLOCK, MINB, F, WMAJ>;
   else
     return &force_kernel_pf<T, MODE, 256, 3, F>;
 }
@@ -262,6 +263,8 @@ StepFn<T> step_fn_feat(int variant, int mode) {
       case 6: return window_fn<T, kPrime, F>();
       case 7: return async_fn<T, kPrime, 3, F>();
       case 8: return async_fn<T, kPrime, 4, F>();
+      case 9: return async_fn<T, kPrime, 1, F, 1024>();
+      case 10: return async_fn<T, kPrime, 1, F, 1024, true>();
       default: return &force_kernel<T, kPrime, F>;
     }
   }
@@ -274,6 +277,8 @@ StepFn<T> step_fn_feat(int variant, int mode) {
     case 6: return window_fn<T, kStep, F>();
     case 7: return async_fn<T, kStep, 3, F>();
     case 8: return async_fn<T, kStep, 4, F>();
+    case 9: return async_fn<T, kStep, 1, F, 1024>();
+    case 10: return async_fn<T, kStep, 1, F, 1024, true>();
     default: return &force_kernel<T, kStep, F>;
   }
 }
@@ -289,6 +294,7 @@ StepFn<T> step_fn(int variant, int mode, bool feat, bool sum64 = false) {
 template <class T>
 inline int variant_block(int variant) {
   if (variant == kWindowVariant) return sizeof(T) == 4 ? kWinThreads : 256;
+  if (variant == 9 || variant == 10) return sizeof(T) == 4 ? 1024 : 256;
   return (variant == 2 || variant == 5) ? 128 : 256;
 }
 
@@ -297,6 +303,7 @@ template <class T>
 inline size_t variant_smem(int variant) {
   if (sizeof(T) != 4) return 0;
   if (variant == kWindowVariant) return kWinSmem;
+  if (variant == 9 || variant == 10) return async_smem(1024);
   if (variant >= kAsyncVariant) return async_smem(256);
   return 0;
 }

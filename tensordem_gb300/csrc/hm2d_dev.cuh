@@ -838,16 +838,20 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
     s_vmax[threadIdx.x >> 5] = wm;
   }
   const int bad = __syncthreads_or(L.bad ? 1 : 0);
+  if (threadIdx.x >= 32) return;
+  // the block's speed bound: warp 0 reduces the warps' bounds (>= 0)
+  float bm = threadIdx.x < (blockDim.x >> 5) ? s_vmax[threadIdx.x] : 0.0f;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, off));
   if (threadIdx.x != 0) return;
-  float bm = s_vmax[0];
-  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bm = fmaxf(bm, s_vmax[w]);
   if (bad) atomicOr(&ctl->status, (int)kStatusNonfinite);
   atomicMax(&ctl->vmax2_bits, __float_as_uint(bm));
-  __threadfence();
-  const unsigned t = atomicAdd(&ctl->ticket, 1u);
+  // the grid ticket with release-acquire order: this block's writes (its
+  // threads' through the barrier above) are visible before its ticket, and
+  // the last block sees every other block's writes after its own
+  unsigned t;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(t) : "l"(&ctl->ticket) : "memory");
   if (t != gridDim.x - 1) return;
-  // last block of the grid: every other block's writes are visible after this
-  __threadfence();
   if (FEAT && P.irad > T(0)) {
     // sum the indenter partials in warp order (deterministic)
     const unsigned m = *reinterpret_cast<volatile unsigned*>(&ctl->load_entries);
@@ -998,7 +1002,12 @@ constexpr size_t async_smem(int block) { return (size_t)kAsyncRecords * block * 
 // occupancy; each thread reads back only its own copies (no block barrier).
 // Layout, 16-byte records indexed [slot][thread]: heads [3], positions [2],
 // velocities [2], partner positions [2][3].
-template <class T, int MODE, int BLOCK, int MINB, bool FEAT>
+//
+// WMAJ: the grid's warps take 32-disc chunks warp-major (warp w of CTA b is
+// grid warp w * G + b), so that when the chunk count is not a multiple of
+// the grid's warps, the warps with one chunk fewer are spread over all CTAs
+// instead of filling the last CTAs (which then idle their SMs early).
+template <class T, int MODE, int BLOCK, int MINB, bool FEAT, bool WMAJ = false>
 __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, Bufs<T> B,
                                                                   cudaGraphConditionalHandle h_rebuild,
                                                                   cudaGraphConditionalHandle h_loop, int use_cond,
@@ -1032,7 +1041,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
     if (cnt > 1) cp16(q + BLOCK, pos + hd.z);
     if (cnt > 2) cp16(q + 2 * BLOCK, pos + hd.w);
   };
-  int i = blockIdx.x * BLOCK + t;
+  int i = WMAJ ? (int)(((t >> 5) * gridDim.x + blockIdx.x) * 32 + (t & 31)) : (int)(blockIdx.x * BLOCK + t);
   // prologue: heads of the first two discs and the first disc's own state,
   // then the first disc's partners
   if (i < end) {
