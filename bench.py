@@ -227,11 +227,13 @@ def profiled_traffic() -> float | None:
         return None
 
 
-def algorithmic_bytes(n: int, head_bytes: int, contact_sides: int) -> int:
+def algorithmic_bytes(n: int, head_bytes: int, contact_sides: int, remainder: bool = False) -> int:
     """Bytes one step must move in this layout: state read + write (pos, vel:
-    2 x 2 x 16 B per disc), the list head (16 B per disc) and the tangential
-    history of every touching contact side (8 B read + 8 B write)."""
-    return n * (64 + head_bytes) + 16 * contact_sides
+    2 x 2 x 16 B per disc), the list head (16 B per disc), the position
+    remainder when the engine keeps one (8 B read + 8 B write per disc) and
+    the tangential history of every touching contact side (8 B read + 8 B
+    write)."""
+    return n * (64 + head_bytes + (16 if remainder else 0)) + 16 * contact_sides
 
 
 def survey_bytes(n: int, k: int, c: int, b: int, r: float) -> float:
@@ -294,14 +296,16 @@ def flushed_trial(eng, flush_l2, stream, dev, steps: int = 20) -> dict:
     return means
 
 
-def form_rate(seed, steps, warmup, flush_l2, stream, dev, *, precision=64, sum_precision=32) -> dict:
+def form_rate(seed, steps, warmup, flush_l2, stream, dev, *, precision=64, sum_precision=32,
+              position_remainder=1) -> dict:
     """Another numeric form of the same kernels on the same workload and loop:
-    the plain FP64 build, or the FP32 build with FP64 per-particle sums."""
+    the plain FP64 build, the FP32 build with FP64 per-particle sums, or the
+    FP32 build without position remainders."""
     from dataclasses import replace
 
     from tensordem_gb300.hm2d import HM2D, granular_gas_case
     cfg, st = granular_gas_case(N_SIDE, seed=seed, precision=precision)
-    cfg = replace(cfg, sum_precision=sum_precision)
+    cfg = replace(cfg, sum_precision=sum_precision, position_remainder=position_remainder)
     eng = HM2D(cfg, device=dev)
     eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
     eng.step(2)
@@ -311,7 +315,8 @@ def form_rate(seed, steps, warmup, flush_l2, stream, dev, *, precision=64, sum_p
     return {"value": cfg.n * steps / (total / 1e3), "unit": UNIT, "steps": steps, "variant": eng.variant,
             "step_kernel_us_mean": 1e3 * sum(step_ms) / len(step_ms), "rebuilds": len(rebuild_ms),
             "note": ("precision=64 build of the same kernels (FP64 contacts, sums and ledger)" if precision == 64
-                     else "FP32 contacts with FP64 per-particle force/torque sums") +
+                     else "FP32 contacts with FP64 per-particle force/torque sums" if sum_precision == 64
+                     else "FP32 contacts, plain FP32 position offsets (no remainder pair)") +
                     ", same seeded 1,048,576-disc state and the same flushed per-step loop"}
 
 
@@ -367,6 +372,8 @@ def batched_leg(seed: int = 0, *, serve_seconds: float = 20.0, calibrate_seconds
         "particles": rep["particles"], "instances_with_status": rep["instances_with_status"],
         "peak_load_rel_err_max": agree["peak_load_rel_err_max"],
         "ledger_total_rel_diff_max": agree["ledger_total_rel_diff_max"],
+        "ledger_rel_diff_max_by_kind": agree["ledger_rel_diff_max_by_kind"],
+        "ledger_normalisation": agree["ledger_normalisation"],
         "served": {"capacity_particle_steps_per_s": capacity, "requests": srv["requests"],
                    "completed": srv["completed"], "latency_s": srv["latency_s"],
                    "queue_wait_s": srv["queue_wait_s"], "particle_steps_per_s": srv["particle_steps_per_s"],
@@ -423,7 +430,7 @@ def run_ours(a) -> None:
     k_pairs = len(eng.pairs())
     c_contacts = len(hist)
     r_interval = led1["evals"] / max(1, led1["rebuilds"])
-    alg = algorithmic_bytes(n, 16, 2 * c_contacts)
+    alg = algorithmic_bytes(n, 16, 2 * c_contacts, remainder=cfg.precision == 32 and cfg.position_remainder == 1)
     peak, peak_kind = measured_peak()
     achieved = alg / (kernel_ms / 1e3) / 1e9
     traffic = profiled_traffic()
@@ -467,6 +474,8 @@ def run_ours(a) -> None:
 
     fp64 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=64)
     sums64 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=32, sum_precision=64)
+    plain32 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=32,
+                        position_remainder=0)
     batched = None
     if rank == 0 and world == 1 and not a.no_batched:
         del eng
@@ -488,7 +497,8 @@ def run_ours(a) -> None:
                           "step_kernel_us_median": 1e3 * statistics.median(step_ms),
                           "wall_s_timed_loop": wall,
                           "max_neighbors_seen": led1["max_neighbors"],
-                          "touching_contacts_end": c_contacts, "fp64": fp64, "fp32_fp64_sums": sums64}}
+                          "touching_contacts_end": c_contacts, "fp64": fp64, "fp32_fp64_sums": sums64,
+                          "fp32_no_position_remainder": plain32}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

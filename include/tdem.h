@@ -224,6 +224,13 @@ typedef struct {
   int32_t sum_precision;  /* FP32 engines: 64 sums each particle's force and
                              torque terms in FP64; 0 or 32: compensated FP32
                              (float-float) sums. FP64 engines sum in FP64. */
+  int32_t position_remainder; /* FP32 engines: 1 keeps each position's FP32
+                             rounding remainder (one FP32 pair per disc, 16 more
+                             bytes per disc and step), so that positions
+                             integrate to about 48 bits and the energy ledger
+                             closes as in FP64 before any break; 0: plain FP32
+                             offsets. Ignored by FP64 engines and by the
+                             allocation-free entry point. */
 } tdem_hm_config;
 
 /* Ledger slots of tdem_hm_read_ledger (J unless noted). */
@@ -436,6 +443,7 @@ typedef struct {
   int64_t particle_capacity; /* particles resident at once (live + retired awaiting compaction) */
   int64_t key_capacity;      /* cell keys over all instances (an instance takes ncx * ncy) */
   int32_t rebuild_every;     /* 0: rebuild on the displacement bound only; k > 0: also every k steps */
+  int32_t position_remainder; /* FP32: 1 keeps each position's rounding remainder (see tdem_hm_config) */
 } tdem_batch_config;
 
 /* Ledger slots of tdem_batch_read: TDEM_HM_L_* (per instance; EVALS counts

@@ -76,7 +76,7 @@ class HMConfigC(C.Structure):
         ("bond_damping", C.c_double), ("breaking_strain", C.c_double),
         ("shear_breaking_strain", C.c_double), ("indenter_center", C.c_double * 2),
         ("indenter_velocity", C.c_double * 2), ("indenter_radius", C.c_double),
-        ("load_capacity", C.c_int32), ("sum_precision", C.c_int32),
+        ("load_capacity", C.c_int32), ("sum_precision", C.c_int32), ("position_remainder", C.c_int32),
     ]
 
 
@@ -84,7 +84,7 @@ class BatchConfigC(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("max_neighbors", C.c_int32), ("max_bonds", C.c_int32),
         ("max_instances", C.c_int32), ("particle_capacity", C.c_int64), ("key_capacity", C.c_int64),
-        ("rebuild_every", C.c_int32),
+        ("rebuild_every", C.c_int32), ("position_remainder", C.c_int32),
     ]
 
 

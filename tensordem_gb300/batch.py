@@ -44,6 +44,8 @@ class BatchConfig:
     max_bonds: int = 6
     precision: int = 32
     rebuild_every: int = 0
+    # FP32: 1 keeps each position's FP32 rounding remainder (see HM2DConfig)
+    position_remainder: int = 1
 
     def to_c(self) -> _lib.BatchConfigC:
         c = _lib.BatchConfigC()
@@ -51,6 +53,7 @@ class BatchConfig:
         c.max_instances, c.particle_capacity, c.key_capacity = (self.max_instances, self.particle_capacity,
                                                                  self.key_capacity)
         c.rebuild_every = self.rebuild_every
+        c.position_remainder = self.position_remainder
         return c
 
     def bytes(self) -> int:

@@ -414,7 +414,10 @@ __global__ void batch_append_kernel(Params<T> Q, Bufs<T> B, int slot, int m, con
     const int cy = (int)fmin(fmax(fy, 0.0), (double)(Q.ncy - 1));
     const double r = radius[j], ms = mass[j];
     const bool clamped = isinf(ms) && ms > 0.0;  // infinite mass: a clamped disc
-    B.pos[sp][i] = V4<T>{(T)(x - cx * c), (T)(y - cy * c), (T)r, cell_to_lane(cx | (cy << 16), T(0))};
+    const double ox = x - cx * c, oy = y - cy * c;
+    B.pos[sp][i] = V4<T>{(T)ox, (T)oy, (T)r, cell_to_lane(cx | (cy << 16), T(0))};
+    if (sizeof(T) == 4 && Q.prem)
+      B.prem[lp][i] = make_float2((float)(ox - (double)(T)ox), (float)(oy - (double)(T)oy));
     B.vel[sp][i] = clamped ? V4<T>{T(0), T(0), T(0), T(0)}
                            : V4<T>{(T)vel[2 * j], (T)vel[2 * j + 1], (T)omega[j], (T)(1.0 / ms)};
     if (B.bcnt[lp]) B.bcnt[lp][i] = 0;
@@ -506,8 +509,9 @@ __global__ void batch_unpack_kernel(Params<T> Q, Bufs<T> B, int slot, int m, dou
     if (o < 0 || o >= m) continue;
     const V4<T> q = B.pos[sp][p];
     const int c = lane_to_cell(q.w);
-    pos[2 * o] = (double)(c & 0xFFFF) * cl + (double)q.x;
-    pos[2 * o + 1] = (double)(c >> 16) * cl + (double)q.y;
+    const float2 rm = (sizeof(T) == 4 && Q.prem) ? B.prem[lp][p] : make_float2(0.0f, 0.0f);
+    pos[2 * o] = (double)(c & 0xFFFF) * cl + (double)q.x + (double)rm.x;
+    pos[2 * o + 1] = (double)(c >> 16) * cl + (double)q.y + (double)rm.y;
     const V4<T> v = B.peek_vel[p];
     vel[2 * o] = (double)v.x;
     vel[2 * o + 1] = (double)v.y;
@@ -718,6 +722,7 @@ struct Batch final : BatchBase {
       B.orig[b] = a.take<int>(N);
       B.inst[b] = a.take<int>(N);
       B.whist[b] = a.take<V2<T>>(4 * N);
+      B.prem[b] = (sizeof(T) == 4 && cfg.position_remainder) ? a.take<float2>(N) : nullptr;
       if (BM > 0) {
         B.bpart[b] = a.take<unsigned>(BM * N);
         B.bref[b] = a.take<V2<T>>(BM * N);
@@ -765,6 +770,8 @@ struct Batch final : BatchBase {
     if (c.key_capacity < 2 || c.key_capacity > (1ll << 31) - 1)
       return tdem::fail(&e, TDEM_ERR_BADARG, "key_capacity must be in 2..2^31-1");
     if (c.rebuild_every < 0) return tdem::fail(&e, TDEM_ERR_BADARG, "rebuild_every must be >= 0");
+    if (c.position_remainder != 0 && c.position_remainder != 1)
+      return tdem::fail(&e, TDEM_ERR_BADARG, "position_remainder must be 0 or 1");
     return TDEM_OK;
   }
 
@@ -774,6 +781,7 @@ struct Batch final : BatchBase {
     G.n = (int)c.particle_capacity;
     G.W = c.max_neighbors;
     G.BMAX = c.max_bonds;
+    G.prem = (sizeof(T) == 4 && c.position_remainder) ? 1 : 0;
     int dev = 0;
     TDEM_CUDA_TRY(&err, cudaGetDevice(&dev));
     TDEM_CUDA_TRY(&err, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1070,6 +1078,7 @@ struct Batch final : BatchBase {
     I.par.eval0 = evals;
     I.par.stop = LLONG_MAX;
     I.par.feat = (nb > 0 || c.indenter_radius > 0.0) ? 1 : 0;
+    I.par.prem = G.prem;  // the batch's arrays decide, not the instance's config
     // stage and append
     double* h = stage_host;
     std::memcpy(h, pos, 2 * (size_t)m * sizeof(double));

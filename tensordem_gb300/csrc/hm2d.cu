@@ -300,11 +300,11 @@ inline int variant_block(int variant) {
 
 // Dynamic shared memory of a variant's step kernel.
 template <class T>
-inline size_t variant_smem(int variant) {
+inline size_t variant_smem(int variant, bool prem) {
   if (sizeof(T) != 4) return 0;
   if (variant == kWindowVariant) return kWinSmem;
-  if (variant == 9 || variant == 10) return async_smem(1024);
-  if (variant >= kAsyncVariant) return async_smem(256);
+  if (variant == 9 || variant == 10) return async_smem(1024, prem);
+  if (variant >= kAsyncVariant) return async_smem(256, prem);
   return 0;
 }
 
@@ -388,6 +388,7 @@ struct Engine final : EngineBase {
   int init(const tdem_hm_config& c) {
     make_params<T>(c, c.max_neighbors, P);
     sum64 = sizeof(T) == 4 && c.sum_precision == 64;
+    P.prem = (sizeof(T) == 4 && c.position_remainder) ? 1 : 0;
     const size_t n = (size_t)c.n, W = (size_t)c.max_neighbors;
     nblocks = (int)((n + kThreads - 1) / kThreads);
     scan_blocks = (P.nkeys + kScanChunk - 1) / kScanChunk;
@@ -418,6 +419,7 @@ struct Engine final : EngineBase {
           (rc = alloc(&B.nbr[b], (W > 3 ? W - 3 : 1) * n)) ||
           (rc = alloc(&B.hist[b], W * n)))
         return rc;
+      if (P.prem && (rc = alloc(&B.prem[b], n))) return rc;
     }
     if ((rc = alloc(&B.cell_count, (size_t)P.nkeys)) || (rc = alloc(&B.cell_start, (size_t)P.nkeys)) ||
         (rc = alloc(&B.cell_fill, (size_t)P.nkeys)) || (rc = alloc(&B.perm, n)) ||
@@ -451,7 +453,7 @@ struct Engine final : EngineBase {
   bool feat() const { return P.BMAX > 0 || P.irad > T(0); }
   // launch shape of a variant's step kernel (the FP64-sum form has one shape)
   int block_of(int v) const { return sum64 ? 256 : variant_block<T>(v); }
-  size_t smem_of(int v) const { return sum64 ? 0 : variant_smem<T>(v); }
+  size_t smem_of(int v) const { return sum64 ? 0 : variant_smem<T>(v, P.prem != 0); }
   dim3 grid_n() const { return dim3((unsigned)nblocks); }
   dim3 grid_keys() const { return dim3((unsigned)((P.nkeys + kThreads - 1) / kThreads)); }
 
@@ -1023,6 +1025,7 @@ const char* hm_config_error(const tdem_hm_config* c) {
   if (c->precision != 32 && c->precision != 64) return "precision must be 32 or 64";
   if (c->sum_precision != 0 && c->sum_precision != 32 && c->sum_precision != 64)
     return "sum_precision must be 0, 32 or 64";
+  if (c->position_remainder != 0 && c->position_remainder != 1) return "position_remainder must be 0 or 1";
   return nullptr;
 }
 

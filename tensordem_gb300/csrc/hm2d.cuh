@@ -94,6 +94,7 @@ struct Params {
   long long eval0;   // batch evaluation index of the instance's first step
   long long stop;    // the instance's own step limit: frozen once it has taken `stop` steps
   int feat;          // 1: the instance has bonds or an indenter (stepped by the bonded kernel build)
+  int prem;          // FP32: positions carry their rounding remainder (Bufs::prem)
   // FP32 screens that keep FP64 off the common path (decisions unchanged):
   // float brackets of the break strains (largest float <= eps, smallest >= eps)
   float eps_t_lo, eps_t_hi, eps_s_lo, eps_s_hi;
@@ -197,6 +198,11 @@ struct Bufs {
   double* iled;        // [slots * kInstLedger] per-instance ledger
   int* tmp_key;        // rebuild: cell key of each old particle
   int* ifirst;         // [2 * slots]: first tile of each slot, plain instances then the others
+  // FP32 position remainders (Params::prem): the exact position of a disc is
+  // its cell origin + FP32 offset + this FP32 pair. Indexed by the list
+  // parity lp: a step updates its own disc's pair in place, a rebuild
+  // gathers them into the other array in the new order.
+  float2* prem[2];
 };
 
 // The cell id rides in the last lane of the position vector: bit-cast for

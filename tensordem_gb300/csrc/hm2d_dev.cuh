@@ -613,6 +613,30 @@ __device__ __forceinline__ void indenter_contact(const Params<T>& P, long long e
   L.un += (T)(0.4 * fel * delta);
 }
 
+// Compensated FP32 coordinates (Params::prem): a coordinate is the pair
+// (x, r) with x the FP32 offset and r the FP32 remainder of its rounding.
+// a + b == s + e exactly (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (x, r) += a * b, renormalised so that |r| stays within half an ulp of the
+// returned offset: the product's rounding error (from an FMA) and the sum's
+// (TwoSum) go to the remainder instead of being lost.
+__device__ __forceinline__ float add_prod_comp(float x, float& r, float a, float b) {
+  const float d = __fmul_rn(a, b);
+  const float de = __fmaf_rn(a, b, -d);
+  float s, e;
+  two_sum(x, d, s, e);
+  const float t = __fadd_rn(__fadd_rn(r, e), de);
+  float s2, r2;
+  two_sum(s, t, s2, r2);
+  r = r2;
+  return s2;
+}
+
 // Everything one particle does in one evaluation: its candidate slots, the
 // walls, and (committing modes) the velocity-Verlet update into the other
 // buffers. p, v, hd are the particle's own loads (already issued).
@@ -627,16 +651,24 @@ __device__ __forceinline__ void load_head_partners(const F& fetch, const uint4& 
 }
 
 // process_particle with the first three partners' positions already loaded.
+// rem_pre: the disc's position remainder when the caller has it already
+// (null: loaded here).
 template <class T, int MODE, bool FEAT, class F, bool S64 = false>
 __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Bufs<T>& B, const F& fetch, int sp,
                                                    int lp, int i, const V4<T>& p, const V4<T>& v, const uint4& hd,
                                                    const V4<T>& q0, const V4<T>& q1, const V4<T>& q2, int primed,
-                                                   long long eval, ThreadLedger<T>& L) {
+                                                   long long eval, ThreadLedger<T>& L,
+                                                   const float2* rem_pre = nullptr) {
   constexpr bool COMMIT = MODE != kPeek;
   const int n = P.n;
   const unsigned* __restrict__ tail = B.nbr[lp];
   V2<T>* __restrict__ hist = B.hist[lp];
   const int cnt = (int)(hd.x & 0xFFu);
+  // the position remainder, loaded now and used after the contact loop
+  float2 rem = make_float2(0.0f, 0.0f);
+  if constexpr (sizeof(T) == 4) {
+    if (P.prem) rem = rem_pre ? *rem_pre : B.prem[lp][i];
+  }
   const unsigned mask = hd.x >> 8;
   unsigned nmask = 0u;
   typename AccSel<T, S64>::type fx, fy, tq;
@@ -730,10 +762,15 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
       const double m = 1.0 / (double)inv_m;
       const double r = (double)p.z;
       L.ke += 0.5 * m * ((double)vx * vx + (double)vy * vy) + 0.5 * (m * r * r / (double)P.kinv) * (double)om * om;
-      const double x = (double)(c & 0xFFFF) * (double)P.cell + (double)p.x;
-      const double y = (double)(c >> 16) * (double)P.cell + (double)p.y;
+      const double x = (double)(c & 0xFFFF) * (double)P.cell + (double)p.x + (double)rem.x;
+      const double y = (double)(c >> 16) * (double)P.cell + (double)p.y + (double)rem.y;
       L.pe += -m * ((double)P.gx * x + (double)P.gy * y);
     }
+    // The contact, bond and indenter energies above are those of the FP32
+    // offsets; the remainder moves the disc by r, which changes them to first
+    // order by -F . r (F: the disc's force without gravity). Counted with
+    // the potential energy.
+    if (sizeof(T) == 4 && P.prem) L.pe -= (double)Fx * (double)rem.x + (double)Fy * (double)rem.y;
   } else {
     T vx, vy, om;
     if (MODE == kPrime || (MODE == kBatch && !primed)) {
@@ -745,8 +782,16 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
       vy = (v.y + P.half_dt * ay) + P.half_dt * ay;
       om = (v.z + P.half_dt * al) + P.half_dt * al;
     }
-    const T ox = p.x + P.dt * vx;
-    const T oy = p.y + P.dt * vy;
+    T ox, oy;
+    if (sizeof(T) == 4 && P.prem) {
+      float2 r = rem;
+      ox = (T)add_prod_comp((float)p.x, r.x, (float)P.dt, (float)vx);
+      oy = (T)add_prod_comp((float)p.y, r.y, (float)P.dt, (float)vy);
+      B.prem[lp][i] = r;
+    } else {
+      ox = p.x + P.dt * vx;
+      oy = p.y + P.dt * vy;
+    }
     B.pos[sp ^ 1][i] = V4<T>{ox, oy, p.z, p.w};
     B.vel[sp ^ 1][i] = V4<T>{vx, vy, om, v.w};
     L.vmax2 = fmaxf(L.vmax2, (float)(vx * vx + vy * vy));
@@ -757,11 +802,13 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
 template <class T, int MODE, bool FEAT, bool S64 = false>
 __device__ __forceinline__ void process_particle(const Params<T>& P, const Bufs<T>& B, int sp, int lp, int i,
                                                  const V4<T>& p, const V4<T>& v, const uint4& hd, int primed,
-                                                 long long eval, ThreadLedger<T>& L) {
+                                                 long long eval, ThreadLedger<T>& L,
+                                                 const float2* rem_pre = nullptr) {
   V4<T> q0{}, q1{}, q2{};
   const GlobalFetch<T> fetch{B.pos[sp], B.vel[sp]};
   load_head_partners<T>(fetch, hd, q0, q1, q2);
-  process_particle_q<T, MODE, FEAT, GlobalFetch<T>, S64>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, eval, L);
+  process_particle_q<T, MODE, FEAT, GlobalFetch<T>, S64>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, eval, L,
+                                                         rem_pre);
 }
 
 // Control fields a step kernel reads once at its start. disp and target are
@@ -964,33 +1011,43 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_pf(Params<T> P, Bufs
   ThreadLedger<T> L;
   V4<T> p{}, v{};
   uint4 hd = make_uint4(0u, 0u, 0u, 0u);
+  // the position remainder travels with the own state (FP32 engines)
+  const bool pr = sizeof(T) == 4 && P.prem;
+  float2 r{0.0f, 0.0f};
   if (i < P.n) {
     p = B.pos[sp][i];
     v = B.vel[sp][i];
     hd = B.head[lp][i];
+    if (pr) r = B.prem[lp][i];
   }
   while (i < P.n) {
     const int nx = i + stride;
     V4<T> pn{}, vn{};
     uint4 hn = make_uint4(0u, 0u, 0u, 0u);
+    float2 rn{0.0f, 0.0f};
     if (nx < P.n) {
       pn = B.pos[sp][nx];
       vn = B.vel[sp][nx];
       hn = B.head[lp][nx];
+      if (pr) rn = B.prem[lp][nx];
     }
-    process_particle<T, MODE, FEAT, S64>(P, B, sp, lp, i, p, v, hd, primed, eval, L);
+    process_particle<T, MODE, FEAT, S64>(P, B, sp, lp, i, p, v, hd, primed, eval, L, &r);
     i = nx;
     p = pn;
     v = vn;
     hd = hn;
+    r = rn;
   }
   commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
 
 // Shared memory of the pipelined kernel per thread: three list heads, two
-// own-state pairs and two sets of three partner positions, 16 bytes each.
+// own-state pairs and two sets of three partner positions, 16 bytes each,
+// then (engines with position remainders) two 8-byte remainders.
 constexpr int kAsyncRecords = 3 + 2 * 2 + 2 * 3;
-constexpr size_t async_smem(int block) { return (size_t)kAsyncRecords * block * 16; }
+constexpr size_t async_smem(int block, bool prem) {
+  return (size_t)kAsyncRecords * block * 16 + (prem ? (size_t)2 * block * 8 : 0);
+}
 
 // Software-pipelined grid-stride variant (FP32). A disc's step is two
 // dependent gathers deep: its list head, then its partners' positions. Each
@@ -1015,6 +1072,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
   static_assert(MODE != kPeek, "read-back uses force_kernel");
   static_assert(sizeof(V4<T>) == 16, "one 16-byte copy per record");
   using bulk::cp16;
+  using bulk::cp8;
   using bulk::cp_commit;
   using bulk::cp_wait;
   extern __shared__ uint4 async_smem_base[];
@@ -1027,6 +1085,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
   V4<T>* spos = reinterpret_cast<V4<T>*>(async_smem_base + 3 * BLOCK);  // [2][BLOCK]
   V4<T>* svel = spos + 2 * BLOCK;                                        // [2][BLOCK]
   V4<T>* sq = svel + 2 * BLOCK;                                          // [2][3][BLOCK]
+  float2* srem = reinterpret_cast<float2*>(sq + 6 * BLOCK);              // [2][BLOCK]
+  const bool pr = P.prem != 0;
+  const float2* __restrict__ prem = B.prem[lp];
   const V4<T>* __restrict__ pos = B.pos[sp];
   const V4<T>* __restrict__ vel = B.vel[sp];
   const uint4* __restrict__ head = B.head[lp];
@@ -1048,6 +1109,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
     cp16(sh + t, head + i);
     cp16(spos + t, pos + i);
     cp16(svel + t, vel + i);
+    if (pr) cp8(srem + t, prem + i);
   }
   if (i + stride < end) cp16(sh + BLOCK + t, head + i + stride);
   cp_commit();
@@ -1064,6 +1126,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
     if (i1 < end) {
       cp16(spos + (s ^ 1) * BLOCK + t, pos + i1);
       cp16(svel + (s ^ 1) * BLOCK + t, vel + i1);
+      if (pr) cp8(srem + (s ^ 1) * BLOCK + t, prem + i1);
     }
     cp_commit();
     cp_wait<2>();  // X_{k-1} landed: the head of disc k+1
@@ -1080,7 +1143,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
     if (cnt > 0) q0 = q[0];
     if (cnt > 1) q1 = q[BLOCK];
     if (cnt > 2) q2 = q[2 * BLOCK];
-    process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, c.evals, L);
+    const float2 rm = pr ? srem[s * BLOCK + t] : make_float2(0.0f, 0.0f);
+    process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, c.evals, L, &rm);
     h0 = h1;
     s ^= 1;
   }
@@ -1481,7 +1545,17 @@ __global__ void gather_kernel(Params<T> P, Bufs<T> B) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nn; p += gridDim.x * blockDim.x) {
     const int i = B.perm[p];
     const V4<T> q = B.pos[sp][i];
-    const V2<T> off = B.tmp_off[i];
+    V2<T> off = B.tmp_off[i];
+    if (sizeof(T) == 4 && P.prem) {
+      // the offset relative to the new cell, with its remainder carried over:
+      // (x, r) + (old cell - new cell) * cell
+      const int co = lane_to_cell(q.w), cn = B.tmp_cell[i];
+      const float cl = (float)(MULTI ? B.iparams[B.inst[lp][i]].cell : P.cell);
+      float2 r = B.prem[lp][i];
+      off.x = (T)add_prod_comp((float)q.x, r.x, (float)((co & 0xFFFF) - (cn & 0xFFFF)), cl);
+      off.y = (T)add_prod_comp((float)q.y, r.y, (float)((co >> 16) - (cn >> 16)), cl);
+      B.prem[lp ^ 1][p] = r;
+    }
     B.pos[sp ^ 1][p] = V4<T>{off.x, off.y, q.z, cell_to_lane(B.tmp_cell[i], T(0))};
     B.vel[sp ^ 1][p] = B.vel[sp][i];
     B.orig[lp ^ 1][p] = B.orig[lp][i];
@@ -1663,7 +1737,10 @@ __global__ void pack_kernel(Params<T> P, Bufs<T> B, const double* pos, const dou
   const int cy = (int)fmin(fmax(fy, 0.0), (double)(P.ncy - 1));
   const double r = radius[i], m = mass[i];
   const bool clamped = isinf(m) && m > 0.0;  // infinite mass: a clamped disc
-  B.pos[sp][i] = V4<T>{(T)(x - cx * c), (T)(y - cy * c), (T)r, cell_to_lane(cx | (cy << 16), T(0))};
+  const double ox = x - cx * c, oy = y - cy * c;
+  B.pos[sp][i] = V4<T>{(T)ox, (T)oy, (T)r, cell_to_lane(cx | (cy << 16), T(0))};
+  if (sizeof(T) == 4 && P.prem)
+    B.prem[lp][i] = make_float2((float)(ox - (double)(T)ox), (float)(oy - (double)(T)oy));
   B.vel[sp][i] = clamped ? V4<T>{T(0), T(0), T(0), T(0)}
                          : V4<T>{(T)vel[2 * i], (T)vel[2 * i + 1], (T)omega[i], (T)(1.0 / m)};
   if (B.bcnt[lp]) B.bcnt[lp][i] = 0;
@@ -1687,8 +1764,9 @@ __global__ void unpack_kernel(Params<T> P, Bufs<T> B, double* pos, double* vel, 
   const int c = lane_to_cell(q.w);
   const double cl = (double)P.cell;
   if (pos) {
-    pos[2 * o] = (double)(c & 0xFFFF) * cl + (double)q.x;
-    pos[2 * o + 1] = (double)(c >> 16) * cl + (double)q.y;
+    const float2 r = (sizeof(T) == 4 && P.prem) ? B.prem[lp][p] : make_float2(0.0f, 0.0f);
+    pos[2 * o] = (double)(c & 0xFFFF) * cl + (double)q.x + (double)r.x;
+    pos[2 * o + 1] = (double)(c >> 16) * cl + (double)q.y + (double)r.y;
   }
   const V4<T> v = B.peek_vel[p];
   if (vel) {

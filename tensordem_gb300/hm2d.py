@@ -65,6 +65,9 @@ class HM2DConfig:
     load_capacity: int = 0
     # FP32 engines: 64 sums each particle's terms in FP64 (else float-float)
     sum_precision: int = 32
+    # FP32 engines: 1 keeps each position's FP32 rounding remainder (positions
+    # integrate to ~48 bits; the energy ledger closes as in FP64 before breaks)
+    position_remainder: int = 1
 
     @property
     def box(self) -> tuple[float, float]:
@@ -88,6 +91,7 @@ class HM2DConfig:
         c.indenter_radius = self.indenter_radius
         c.load_capacity = self.load_capacity
         c.sum_precision = self.sum_precision
+        c.position_remainder = self.position_remainder
         return c
 
 
