@@ -81,7 +81,7 @@ def workload_config(seed: int = 0) -> dict:
     return {"workload": "2-D polydisperse Hertz-Mindlin disc settling, 1,048,576 discs "
                         "(1024x1024 jittered grid, area fraction 0.55, 4 walls, gravity), "
                         "radii U[0.8,1.2] mm, E 70 GPa, nu 0.25, mu 0.5, e 0.8, dt 0.2 Rayleigh",
-            "discs": N_SIDE * N_SIDE, "seed": seed, "precision": "fp32 contacts, compensated sums, fp64 ledger",
+            "discs": N_SIDE * N_SIDE, "seed": seed, "precision": "fp32 contacts on fp32 cell offsets with fp32 rounding remainders, compensated sums, fp64 ledger",
             "l2": "flushed before every timed step (256 MiB written, another 256 MiB read)",
             "parallelism": "replicas"}
 

@@ -193,6 +193,16 @@ class HM2D:
     def _stream(self) -> int:
         return torch.cuda.current_stream(self.device).cuda_stream
 
+    @property
+    def handle(self) -> int:
+        """The engine's C-ABI handle (tdem_hm*), as the torch ops take it."""
+        return int(self._h.value)
+
+    @property
+    def anchor(self) -> torch.Tensor:
+        """A one-element tensor on the engine's device: the torch ops' device argument."""
+        return self._anchor
+
     def use_graph(self, on: bool) -> None:
         self._lib.tdem_hm_use_graph(self._h, 1 if on else 0)
 
