@@ -272,7 +272,10 @@ int tdem_hm_set_state(tdem_hm* h, const double* pos, const double* vel, const do
 
 /* Advance n velocity-Verlet steps (FloeBed.step, kernel.py:410-419), list
  * rebuilds and history remap included (kernel.py:230-274). Asynchronous:
- * check tdem_hm_status afterwards. */
+ * check tdem_hm_status afterwards. n_steps == 0 steps nothing and builds the
+ * step graph for the current variant if it is not built yet (the first
+ * stepping call after creation or a variant change otherwise pays that,
+ * about half a second). */
 int tdem_hm_step(tdem_hm* h, int64_t n_steps, void* stream);
 
 /* Integer-time state in original order: positions, velocities, omega, total

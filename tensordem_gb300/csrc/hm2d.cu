@@ -412,6 +412,7 @@ struct Engine final : EngineBase {
       vgrid[v] = std::max(1, std::min(need, per_sm * sms));
       nwarp_slots = std::max(nwarp_slots, vgrid[v] * (bs / 32));
     }
+    P.ind_slots = nwarp_slots;
     int rc = TDEM_OK;
     for (int b = 0; b < 2 && !rc; ++b) {
       if ((rc = alloc(&B.pos[b], n)) || (rc = alloc(&B.vel[b], n)) || (rc = alloc(&B.head[b], n)) ||
@@ -427,7 +428,7 @@ struct Engine final : EngineBase {
         (rc = alloc(&B.tmp_off, n)) || (rc = alloc(&B.diss_part, (size_t)nwarp_slots)) ||
         (rc = alloc(&B.peek_part, (size_t)nblocks * 12)) || (rc = alloc(&B.peek_vel, n)) ||
         (rc = alloc(&B.peek_force, n)) || (rc = alloc(&B.ctl, 1)) || (rc = alloc(&B.invperm, n)) ||
-        (rc = alloc(&B.frac_part, (size_t)nwarp_slots)) || (rc = alloc(&B.ind_part, 3 * (size_t)nwarp_slots)) ||
+        (rc = alloc(&B.frac_part, (size_t)nwarp_slots)) || (rc = alloc(&B.ind_part, 6 * (size_t)nwarp_slots)) ||
         (rc = alloc(&B.load, 2 * (size_t)std::max(P.load_cap, 1))))
       return rc;
     if (P.BMAX > 0) {
@@ -605,7 +606,17 @@ struct Engine final : EngineBase {
 
   int step(long long n, cudaStream_t s) override {
     if (!has_state) return tdem::fail(&err, TDEM_ERR_STATE, "step before set_state");
-    if (n <= 0) return TDEM_OK;
+    if (n <= 0) {
+      // no step: build the step graph for the current variant now, so that
+      // the next call does not (instantiating it takes ~0.5 s)
+      if (graph_on && !graph_failed && !exec && build_graph() != TDEM_OK) {
+        graph_error = err;
+        graph_failed = true;
+        destroy_graphs();
+        cudaGetLastError();
+      }
+      return TDEM_OK;
+    }
     mirror_ok = false;  // rebuild decisions inside the step graph are the device's
     if (!primed) {
       int rc = prime(s);

@@ -88,6 +88,7 @@ struct Params {
   double ind_x0, ind_y0, ind_vx, ind_vy;
   T irad;
   int load_cap;   // capacity of the per-evaluation indenter load record
+  int ind_slots;  // indenter partials: entries of the first half of Bufs::ind_part (the second half: sorted)
   // batched engine: one Params per instance (n = the particle capacity, the
   // stride of every slot-major array)
   int key_off;       // first cell key of the instance (key = key_off + cy * ncx + cx)
@@ -185,7 +186,7 @@ struct Bufs {
   double* frac_part;   // per step-kernel warp: fracture energy released (J)
   double* peek_bond;   // per block: bond elastic energy (read-back)
   // indenter: per-evaluation partial reactions (warp id, fx, fy) and the load record
-  double* ind_part;    // [3 * nwarp_slots]
+  double* ind_part;    // [6 * nwarp_slots]: entries (warp id, fx, fy), then the same in warp order
   double* load;        // [2 * load_cap]: reaction (x, y) per evaluation
   // batched engine (null for a single solve)
   int* inst[2];        // instance slot of each particle, swapped at a rebuild

@@ -885,41 +885,66 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
     s_vmax[threadIdx.x >> 5] = wm;
   }
   const int bad = __syncthreads_or(L.bad ? 1 : 0);
-  if (threadIdx.x >= 32) return;
-  // the block's speed bound: warp 0 reduces the warps' bounds (>= 0)
-  float bm = threadIdx.x < (blockDim.x >> 5) ? s_vmax[threadIdx.x] : 0.0f;
+  // with an indenter the whole last block puts the reaction partials in order
+  const bool ind = FEAT && P.irad > T(0);
+  if (!ind && threadIdx.x >= 32) return;
+  __shared__ unsigned s_last;
+  bool last = false;
+  if (threadIdx.x < 32) {
+    // the block's speed bound: warp 0 reduces the warps' bounds (>= 0)
+    float bm = threadIdx.x < (blockDim.x >> 5) ? s_vmax[threadIdx.x] : 0.0f;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, off));
-  if (threadIdx.x != 0) return;
-  if (bad) atomicOr(&ctl->status, (int)kStatusNonfinite);
-  atomicMax(&ctl->vmax2_bits, __float_as_uint(bm));
-  // the grid ticket with release-acquire order: this block's writes (its
-  // threads' through the barrier above) are visible before its ticket, and
-  // the last block sees every other block's writes after its own
-  unsigned t;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(t) : "l"(&ctl->ticket) : "memory");
-  if (t != gridDim.x - 1) return;
-  if (FEAT && P.irad > T(0)) {
-    // sum the indenter partials in warp order (deterministic)
-    const unsigned m = *reinterpret_cast<volatile unsigned*>(&ctl->load_entries);
-    double* e = B.ind_part;
-    for (unsigned a = 1; a < m; ++a) {
-      const double k0 = e[3 * a], k1 = e[3 * a + 1], k2 = e[3 * a + 2];
-      unsigned b = a;
-      while (b > 0 && e[3 * (b - 1)] > k0) {
-        e[3 * b] = e[3 * (b - 1)];
-        e[3 * b + 1] = e[3 * (b - 1) + 1];
-        e[3 * b + 2] = e[3 * (b - 1) + 2];
-        --b;
-      }
-      e[3 * b] = k0;
-      e[3 * b + 1] = k1;
-      e[3 * b + 2] = k2;
+    for (int off = 16; off > 0; off >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, off));
+    if (threadIdx.x == 0) {
+      if (bad) atomicOr(&ctl->status, (int)kStatusNonfinite);
+      atomicMax(&ctl->vmax2_bits, __float_as_uint(bm));
+      // the grid ticket with release-acquire order: this block's writes (its
+      // threads' through the barrier above) are visible before its ticket,
+      // and the last block sees every other block's writes after its own
+      unsigned t;
+      asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(t) : "l"(&ctl->ticket) : "memory");
+      last = t == gridDim.x - 1;
+      s_last = last ? 1u : 0u;
     }
+  }
+  if (ind) {
+    __syncthreads();
+    if (!s_last) return;
+    // the indenter partials (warp id, fx, fy), one per warp that touched the
+    // indenter, put in warp order by rank (the keys are distinct) into the
+    // second half of ind_part, by every thread of the last block
+    const unsigned m = *reinterpret_cast<volatile unsigned*>(&ctl->load_entries);
+    const double* e = B.ind_part;
+    double* o = B.ind_part + 3 * (size_t)P.ind_slots;
+    for (unsigned a = threadIdx.x; a < m; a += blockDim.x) {
+      const double k0 = e[3 * a];
+      unsigned r = 0;
+      for (unsigned u = 0; u < m; ++u) r += (e[3 * u] < k0) ? 1u : 0u;
+      o[3 * r] = k0;
+      o[3 * r + 1] = e[3 * a + 1];
+      o[3 * r + 2] = e[3 * a + 2];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    // summed in warp order, eight loads in flight at a time
     double sx = 0.0, sy = 0.0;
-    for (unsigned a = 0; a < m; ++a) {
-      sx += e[3 * a + 1];
-      sy += e[3 * a + 2];
+    unsigned a = 0;
+    for (; a + 8 <= m; a += 8) {
+      double x[8], y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        x[u] = o[3 * (a + u) + 1];
+        y[u] = o[3 * (a + u) + 2];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        sx += x[u];
+        sy += y[u];
+      }
+    }
+    for (; a < m; ++a) {
+      sx += o[3 * a + 1];
+      sy += o[3 * a + 2];
     }
     ctl->reaction_x = -sx;
     ctl->reaction_y = -sy;
@@ -929,6 +954,8 @@ __device__ __forceinline__ void commit_epilogue(const Params<T>& P, const Bufs<T
       B.load[2 * c.evals + 1] = -sy;
     }
     ctl->load_entries = 0u;
+  } else if (!last) {
+    return;
   }
   const unsigned long long pair = *reinterpret_cast<volatile unsigned long long*>(&ctl->vmax2_bits);
   const unsigned vbits = (unsigned)(pair & 0xFFFFFFFFull);

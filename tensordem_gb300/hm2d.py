@@ -224,7 +224,9 @@ class HM2D:
         self.steps = 0
 
     def step(self, n_steps: int = 1, *, check: bool = True) -> None:
-        """Advance n velocity-Verlet steps (one graph launch)."""
+        """Advance n velocity-Verlet steps (one graph launch). ``step(0)``
+        only builds the step graph for the current variant (about half a
+        second), which the first stepping call would otherwise pay."""
         from . import ops
         with torch.cuda.device(self.device):
             ops.hm_step(self._h.value, int(n_steps), self._anchor)
