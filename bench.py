@@ -320,6 +320,49 @@ def form_rate(seed, steps, warmup, flush_l2, stream, dev, *, precision=64, sum_p
                     ", same seeded 1,048,576-disc state and the same flushed per-step loop"}
 
 
+ICE_STEPS = 2000
+
+
+def ice_leg(seed: int, dev, peak: float) -> dict:
+    """The bonded 1M-disc ice sheet (2048 x 512 hex lattice, 3.1M bonds,
+    indenter): every disc carries its six bond forces every step, so this
+    is the contact-dense counterpart of the settling gas. 2,000 steps in the
+    conditional step graph (strain kernel, step kernel, rebuild IF), the
+    variant autotuned and the graph built before the clock starts; the
+    state and bond arrays (~350 MB) exceed L2, so no flush is needed."""
+    import torch
+
+    from tensordem_gb300.hm2d import HM2D, ice_sheet_case
+    cfg, st, bonds, strength = ice_sheet_case(2048, 512, seed=seed, steps=ICE_STEPS)
+    eng = HM2D(cfg, device=dev)
+    eng.set_state(st["pos"], st["vel"], st["omega"], st["radius"], st["mass"], st["inertia"])
+    eng.set_bonds(bonds, strength)
+    eng.autotune(steps=10)
+    eng.step(0)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    eng.step(ICE_STEPS, check=False)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    eng.check()
+    ms = e0.elapsed_time(e1)
+    led = eng.ledger()
+    n, nb = cfg.n, len(bonds)
+    # bytes a step must move: the gas step's 96 B per disc, two slot copies
+    # per bond (partner word 4 B, reference vector 8 B, strength 4 B, history
+    # 8 B read and 8 B written) and the strain (4 B written, 4 B read)
+    alg = n * (96 + 8) + 2 * nb * 32
+    us = 1e3 * ms / ICE_STEPS
+    return {"workload": "bonded ice sheet, 2048 x 512 hex lattice (1,048,576 discs, 3,140,609 bonds), indenter "
+                        "R = 2 m at 0.5 m/s, FP32 contacts and bonds, FP64 ledger; 2,000 graph-launched steps",
+            "value": n * ICE_STEPS / (ms / 1e3), "unit": UNIT, "us_per_step": us, "variant": eng.variant,
+            "bytes_per_step_model": alg, "achieved_gbs": alg / (us / 1e6) / 1e9,
+            "frac": alg / (us / 1e6) / 1e9 / peak, "bonds": nb, "broken": led["broken"],
+            "tool_work_J": led["tool_work"], "ledger_total_rel_work": led["total"] / max(led["tool_work"], 1e-300)}
+
+
 BATCH_INSTANCES = 512
 BATCH_STEPS = 1000
 BATCH_SAMPLE = 64
@@ -476,6 +519,7 @@ def run_ours(a) -> None:
     sums64 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=32, sum_precision=64)
     plain32 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=32,
                         position_remainder=0)
+    ice = ice_leg(rank, dev, peak) if not a.no_batched else None
     batched = None
     if rank == 0 and world == 1 and not a.no_batched:
         del eng
@@ -498,7 +542,7 @@ def run_ours(a) -> None:
                           "wall_s_timed_loop": wall,
                           "max_neighbors_seen": led1["max_neighbors"],
                           "touching_contacts_end": c_contacts, "fp64": fp64, "fp32_fp64_sums": sums64,
-                          "fp32_no_position_remainder": plain32}}
+                          "fp32_no_position_remainder": plain32, "bonded_sheet_1M": ice}}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
