@@ -220,7 +220,9 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 // kernels; an FP64 engine runs variant 1's kernel for them.
 constexpr int kVariants = 11;
 constexpr int kWindowVariant = 6;
-constexpr int kAsyncVariant = 7;
+constexpr int kAsyncVariant = 7;       // 7, 8: 256-thread CTAs
+constexpr int kAsyncWideVariant = 9;   // 9, 10: one 1024-thread CTA per SM
+constexpr int kWideBlock = 1024;
 
 template <class T>
 using StepFn = void (*)(Params<T>, Bufs<T>, cudaGraphConditionalHandle, cudaGraphConditionalHandle, int, int,
@@ -251,36 +253,26 @@ StepFn<T> step_fn_sum64(int mode) {
   return mode == kPrime ? &force_kernel_pf<T, kPrime, 256, 3, F, true> : &force_kernel_pf<T, kStep, 256, 3, F, true>;
 }
 
+template <class T, int MODE, bool F>
+StepFn<T> step_fn_mode(int variant) {
+  switch (variant) {
+    case 1: return &force_kernel_pf<T, MODE, 256, 3, F>;
+    case 2: return &force_kernel_pf<T, MODE, 128, 6, F>;
+    case 3: return &force_kernel_pf<T, MODE, 256, 2, F>;
+    case 4: return &force_kernel_bulk<T, MODE, 256, 3, F>;
+    case 5: return &force_kernel_bulk<T, MODE, 128, 6, F>;
+    case kWindowVariant: return window_fn<T, MODE, F>();
+    case kAsyncVariant: return async_fn<T, MODE, 3, F>();
+    case kAsyncVariant + 1: return async_fn<T, MODE, 4, F>();
+    case kAsyncWideVariant: return async_fn<T, MODE, 1, F, kWideBlock>();
+    case kAsyncWideVariant + 1: return async_fn<T, MODE, 1, F, kWideBlock, true>();
+    default: return &force_kernel<T, MODE, F>;
+  }
+}
+
 template <class T, bool F>
 StepFn<T> step_fn_feat(int variant, int mode) {
-  if (mode == kPrime) {
-    switch (variant) {
-      case 1: return &force_kernel_pf<T, kPrime, 256, 3, F>;
-      case 2: return &force_kernel_pf<T, kPrime, 128, 6, F>;
-      case 3: return &force_kernel_pf<T, kPrime, 256, 2, F>;
-      case 4: return &force_kernel_bulk<T, kPrime, 256, 3, F>;
-      case 5: return &force_kernel_bulk<T, kPrime, 128, 6, F>;
-      case 6: return window_fn<T, kPrime, F>();
-      case 7: return async_fn<T, kPrime, 3, F>();
-      case 8: return async_fn<T, kPrime, 4, F>();
-      case 9: return async_fn<T, kPrime, 1, F, 1024>();
-      case 10: return async_fn<T, kPrime, 1, F, 1024, true>();
-      default: return &force_kernel<T, kPrime, F>;
-    }
-  }
-  switch (variant) {
-    case 1: return &force_kernel_pf<T, kStep, 256, 3, F>;
-    case 2: return &force_kernel_pf<T, kStep, 128, 6, F>;
-    case 3: return &force_kernel_pf<T, kStep, 256, 2, F>;
-    case 4: return &force_kernel_bulk<T, kStep, 256, 3, F>;
-    case 5: return &force_kernel_bulk<T, kStep, 128, 6, F>;
-    case 6: return window_fn<T, kStep, F>();
-    case 7: return async_fn<T, kStep, 3, F>();
-    case 8: return async_fn<T, kStep, 4, F>();
-    case 9: return async_fn<T, kStep, 1, F, 1024>();
-    case 10: return async_fn<T, kStep, 1, F, 1024, true>();
-    default: return &force_kernel<T, kStep, F>;
-  }
+  return mode == kPrime ? step_fn_mode<T, kPrime, F>(variant) : step_fn_mode<T, kStep, F>(variant);
 }
 
 // FEAT kernels carry the bonded-particle model and the indenter; the plain
@@ -294,7 +286,7 @@ StepFn<T> step_fn(int variant, int mode, bool feat, bool sum64 = false) {
 template <class T>
 inline int variant_block(int variant) {
   if (variant == kWindowVariant) return sizeof(T) == 4 ? kWinThreads : 256;
-  if (variant == 9 || variant == 10) return sizeof(T) == 4 ? 1024 : 256;
+  if (variant >= kAsyncWideVariant) return sizeof(T) == 4 ? kWideBlock : 256;
   return (variant == 2 || variant == 5) ? 128 : 256;
 }
 
@@ -303,7 +295,7 @@ template <class T>
 inline size_t variant_smem(int variant, bool prem) {
   if (sizeof(T) != 4) return 0;
   if (variant == kWindowVariant) return kWinSmem;
-  if (variant == 9 || variant == 10) return async_smem(1024, prem);
+  if (variant >= kAsyncWideVariant) return async_smem(kWideBlock, prem);
   if (variant >= kAsyncVariant) return async_smem(256, prem);
   return 0;
 }
