@@ -519,7 +519,7 @@ def run_ours(a) -> None:
     sums64 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=32, sum_precision=64)
     plain32 = form_rate(rank, min(a.steps, 200), a.warmup, flush_l2, stream, dev, precision=32,
                         position_remainder=0)
-    ice = ice_leg(rank, dev, peak) if not a.no_batched else None
+    ice = ice_leg(rank, dev, peak) if (rank == 0 and world == 1 and not a.no_batched) else None
     batched = None
     if rank == 0 and world == 1 and not a.no_batched:
         del eng
