@@ -489,7 +489,9 @@ int tdem_batch_admit(tdem_batch* h, const tdem_hm_config* inst, const double* po
                      void* stream);
 
 /* Advance every live instance by n_steps (one graph launch). Asynchronous.
- * n_steps == 0 only sorts in admitted instances and compacts retired ones. */
+ * n_steps == 0 only sorts in admitted instances, compacts retired ones and
+ * builds the step graph for the current variant if it is not built yet
+ * (otherwise the first stepping call pays that, about half a second). */
 int tdem_batch_step(tdem_batch* h, int64_t n_steps, void* stream);
 
 /* Integer-time state of one instance in its local order (host FP64 outputs,

@@ -149,7 +149,8 @@ class Batch:
         return int(out.value)
 
     def step(self, n: int) -> None:
-        """Advance every live instance by n steps (asynchronous)."""
+        """Advance every live instance by n steps (asynchronous). ``step(0)``
+        sorts in admissions, compacts retirements and builds the step graph."""
         from . import ops
         if not hasattr(self, "_anchor"):
             self._anchor = torch.zeros(1, device=self.device)  # the device of the torch op

@@ -192,12 +192,16 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   int4 d = make_int4(0, 0, 0, 0);
   V4<T> p{}, v{};
   uint4 hd = make_uint4(0u, 0u, 0u, 0u);
+  // the position remainders travel with the own state (FP32 batches that keep them)
+  const float2* __restrict__ prem = B.prem[lp];
+  float2 r{0.0f, 0.0f};
   if (t < tend) {
     d = B.tiles[t];
     if (lane < d.z) {
       p = pos[d.y + lane];
       v = vel[d.y + lane];
       hd = head[d.y + lane];
+      if (prem) r = prem[d.y + lane];
     }
   }
   bool frozen = false;  // the open segment's instance has taken all its steps
@@ -266,12 +270,14 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     int4 dn = make_int4(0, 0, 0, 0);
     V4<T> pn{}, vn{};
     uint4 hn = make_uint4(0u, 0u, 0u, 0u);
+    float2 rn{0.0f, 0.0f};
     if (tn < tnend) {
       dn = B.tiles[tn];
       if (lane < dn.z) {
         pn = pos[dn.y + lane];
         vn = vel[dn.y + lane];
         hn = head[dn.y + lane];
+        if (prem) rn = prem[dn.y + lane];
       }
     }
     const int k = d.x;
@@ -303,7 +309,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
       }
     } else if (run) {
       ThreadLedger<T> L;
-      if (lane < d.z) process_particle<T, MODE, FEAT>(Q, B, sp, lp, d.y + lane, p, v, hd, primed, le, L);
+      if (lane < d.z) process_particle<T, MODE, FEAT>(Q, B, sp, lp, d.y + lane, p, v, hd, primed, le, L, &r);
       double* row = B.tpart + (size_t)t * kTileVals;
       if (MODE == kBatch) {
         const float f = (float)Q.dt / Q.rebuild_disp;
@@ -353,6 +359,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     p = pn;
     v = vn;
     hd = hn;
+    r = rn;
     if (next_chunk && t < tend) nb = grab();
   }
   flush();
@@ -1132,8 +1139,8 @@ struct Batch final : BatchBase {
   }
 
   int step(long long n, cudaStream_t s) override {
-    int rc = settle(s);  // n == 0 only settles admissions and retirements
-    if (rc || n <= 0) return rc;
+    int rc = settle(s);  // n == 0 settles admissions and retirements and builds the step graph
+    if (rc || n < 0) return rc;
     if (graph_on && !graph_failed && !exec) {
       if (build_graph() != TDEM_OK) {
         graph_failed = true;  // plain launches: the same kernels and results
@@ -1141,6 +1148,7 @@ struct Batch final : BatchBase {
         cudaGetLastError();
       }
     }
+    if (n == 0) return TDEM_OK;
     if (graph_on && exec) {
       rc = set_graph_target(n);
       if (rc) return rc;
