@@ -216,9 +216,12 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 // block shapes; 4..5 = bulk-copy staging of own state; 6 = neighbour window in
 // shared memory; 7..8 = per-thread cp.async pipeline, three discs deep, at 3
 // and 4 blocks per SM; 9..10 = the same pipeline with one 1024-thread CTA
-// per SM, CTA-major and warp-major chunk order. Variants 6..10 are FP32
-// kernels; an FP64 engine runs variant 1's kernel for them.
-constexpr int kVariants = 11;
+// per SM, CTA-major and warp-major chunk order; 11 = the pipeline with one
+// 512-thread CTA per SM (128 registers: the bonded build without spills).
+// Variants 6..11 are FP32 kernels; an FP64 engine runs variant 1's kernel
+// for them.
+constexpr int kVariants = 12;
+constexpr int kAsyncHalfVariant = 11;
 constexpr int kWindowVariant = 6;
 constexpr int kAsyncVariant = 7;       // 7, 8: 256-thread CTAs
 constexpr int kAsyncWideVariant = 9;   // 9, 10: one 1024-thread CTA per SM
@@ -266,6 +269,7 @@ StepFn<T> step_fn_mode(int variant) {
     case kAsyncVariant + 1: return async_fn<T, MODE, 4, F>();
     case kAsyncWideVariant: return async_fn<T, MODE, 1, F, kWideBlock>();
     case kAsyncWideVariant + 1: return async_fn<T, MODE, 1, F, kWideBlock, true>();
+    case kAsyncHalfVariant: return async_fn<T, MODE, 1, F, kWideBlock / 2, true>();
     default: return &force_kernel<T, MODE, F>;
   }
 }
@@ -286,6 +290,7 @@ StepFn<T> step_fn(int variant, int mode, bool feat, bool sum64 = false) {
 template <class T>
 inline int variant_block(int variant) {
   if (variant == kWindowVariant) return sizeof(T) == 4 ? kWinThreads : 256;
+  if (variant == kAsyncHalfVariant) return sizeof(T) == 4 ? kWideBlock / 2 : 256;
   if (variant >= kAsyncWideVariant) return sizeof(T) == 4 ? kWideBlock : 256;
   return (variant == 2 || variant == 5) ? 128 : 256;
 }
@@ -295,6 +300,7 @@ template <class T>
 inline size_t variant_smem(int variant, bool prem) {
   if (sizeof(T) != 4) return 0;
   if (variant == kWindowVariant) return kWinSmem;
+  if (variant == kAsyncHalfVariant) return async_smem(kWideBlock / 2, prem);
   if (variant >= kAsyncWideVariant) return async_smem(kWideBlock, prem);
   if (variant >= kAsyncVariant) return async_smem(256, prem);
   return 0;

@@ -330,6 +330,20 @@ __device__ __forceinline__ V2<T> cell_delta(const Params<T>& P, const V4<T>& a, 
                fma((T)((cb >> 16) - (ca >> 16)), P.cell, b.y - a.y)};
 }
 
+// The shear invariant sqrt((E00 - E11)^2 + 4 E01^2) of the Green-Lagrange
+// strain E = (G + G^T + G^T G) / 2, G = F - I, from the bond sums g and the
+// pseudo-inverse pi of the reference-vector covariance.
+template <class T>
+__device__ __forceinline__ T shear_invariant(T g00, T g01, T g10, T g11, const V4<T>& pi) {
+  const T f00 = g00 * pi.x + g01 * pi.z, f01 = g00 * pi.y + g01 * pi.w;
+  const T f10 = g10 * pi.x + g11 * pi.z, f11 = g10 * pi.y + g11 * pi.w;
+  const T e00 = T(0.5) * (T(2) * f00 + f00 * f00 + f10 * f10);
+  const T e11 = T(0.5) * (T(2) * f11 + f01 * f01 + f11 * f11);
+  const T e01 = T(0.5) * ((f01 + f10) + f00 * f01 + f10 * f11);
+  const T dd = e00 - e11;
+  return dev_sqrt(dd * dd + T(4) * (e01 * e01));
+}
+
 // Per-disc objective shear invariant over the disc's initial bonds (broken or
 // not), the reference's local Green-Lagrange measure (dem.py:182-208) written
 // with G = F - I: E = (G + G^T + G^T G) / 2.
@@ -337,6 +351,49 @@ template <class T, bool MULTI = false>
 __global__ void strain_kernel(Params<T> P, Bufs<T> B) {
   const int sp = B.ctl->sp, lp = B.ctl->lp;
   const int n = MULTI ? B.ctl->n_live : P.n;
+  if constexpr (!MULTI) {
+    // One engine with bonds: the count, the own position, the pseudo-inverse
+    // and every slot's word and reference vector in one round of loads (their
+    // addresses are known up front), then all partner positions in a second
+    // round, then the sums in slot order.
+    const V4<T>* __restrict__ pos = B.pos[sp];
+    const unsigned* __restrict__ bpart = B.bpart[lp];
+    const V2<T>* __restrict__ bref = B.bref[lp];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const int bc = B.bcnt[lp][i];
+      const V4<T> p = pos[i];
+      const V4<T> pi = B.bpinv[lp][i];
+      unsigned w[kMaxBondSlots];
+      V2<T> r[kMaxBondSlots];
+#pragma unroll
+      for (int u = 0; u < kMaxBondSlots; ++u) {
+        if (u < P.BMAX) {
+          w[u] = bpart[(size_t)u * n + i];
+          r[u] = bref[(size_t)u * n + i];
+        }
+      }
+      V4<T> q[kMaxBondSlots];
+#pragma unroll
+      for (int u = 0; u < kMaxBondSlots; ++u)
+        if (u < bc) q[u] = pos[(int)(w[u] & kBondIdx)];
+      T g00 = 0, g01 = 0, g10 = 0, g11 = 0;
+#pragma unroll
+      for (int u = 0; u < kMaxBondSlots; ++u) {
+        if (u < bc) {
+          const V2<T> cur = cell_delta<T>(P, p, q[u]);
+          const T ux = cur.x - r[u].x, uy = cur.y - r[u].y;
+          g00 += ux * r[u].x;
+          g01 += ux * r[u].y;
+          g10 += uy * r[u].x;
+          g11 += uy * r[u].y;
+        }
+      }
+      T sv = T(0);
+      if (bc > 0) sv = shear_invariant<T>(g00, g01, g10, g11, pi);
+      B.strain[i] = sv;
+    }
+    return;
+  }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int bc = B.bcnt[lp][i];
     T sv = T(0);
@@ -374,14 +431,7 @@ __global__ void strain_kernel(Params<T> P, Bufs<T> B) {
           }
         }
       }
-      const V4<T> pi = B.bpinv[lp][i];
-      const T f00 = g00 * pi.x + g01 * pi.z, f01 = g00 * pi.y + g01 * pi.w;
-      const T f10 = g10 * pi.x + g11 * pi.z, f11 = g10 * pi.y + g11 * pi.w;
-      const T e00 = T(0.5) * (T(2) * f00 + f00 * f00 + f10 * f10);
-      const T e11 = T(0.5) * (T(2) * f11 + f01 * f01 + f11 * f11);
-      const T e01 = T(0.5) * ((f01 + f10) + f00 * f01 + f10 * f11);
-      const T dd = e00 - e11;
-      sv = dev_sqrt(dd * dd + T(4) * (e01 * e01));
+      sv = shear_invariant<T>(g00, g01, g10, g11, B.bpinv[lp][i]);
     }
     B.strain[i] = sv;
   }

@@ -45,9 +45,9 @@ def test_version_and_capacity(library):
 
 
 def test_variant_counts(library):
-    """Host-only queries: eleven single-engine step-kernel variants and six
+    """Host-only queries: twelve single-engine step-kernel variants and six
     batched shapes (block size, CTAs per SM, tiles per work grab)."""
-    assert library.tdem_hm_num_variants() == 11
+    assert library.tdem_hm_num_variants() == 12
     assert library.tdem_batch_num_variants() == 6
 
 
