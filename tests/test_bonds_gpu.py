@@ -168,6 +168,33 @@ def test_bonded_variants_bit_identical(hm):
     assert all(o == outs[0] for o in outs[1:])
 
 
+def test_variants_match_on_a_multi_cta_sheet_through_breaks(hm):
+    """The pipelined 512-thread variant (11), the grid-stride variant (3) and
+    one thread per disc (0) on a sheet of 7,680 discs (15 warps of 512-thread
+    CTAs) through ~150 breaks: positions, velocities, spins and the break
+    table bit for bit; the ledger, whose per-thread float partials group the
+    terms differently in each launch shape, to 1e-7 of the work input."""
+    outs, ledgers = [], []
+    for v in (11, 3, 0):
+        cfg, st, bonds, strength = small_sheet(160, 48, precision=32, steps=300, speed=20.0)
+        e = _engine(hm, cfg, st, bonds, strength)
+        e.variant = v
+        assert e.variant == v
+        e.step(300)
+        s = e.state()
+        b = e.bonds()
+        outs.append(tuple(s[k].cpu().numpy().tobytes() for k in ("pos", "vel", "omega"))
+                    + (b["mode"].tobytes(), b["fail_eval"].tobytes()))
+        ledgers.append(e.ledger())
+        broken = int((b["mode"] != 0).sum())
+    assert broken > 0
+    assert outs[1] == outs[0] and outs[2] == outs[0]
+    work = max(abs(ledgers[0]["tool_work"]), 1e-300)
+    for led in ledgers[1:]:
+        for key in ("total", "bond_elastic", "dissipated", "fracture_released"):
+            assert abs(led[key] - ledgers[0][key]) <= 1e-7 * work, key
+
+
 def test_full_size_ice_sheet_builds_and_steps(hm):
     cfg, st, bonds, strength = hm.ice_sheet_case(2048, 512, steps=50)
     e = _engine(hm, cfg, st, bonds, strength)
