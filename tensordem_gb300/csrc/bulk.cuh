@@ -91,6 +91,11 @@ __device__ __forceinline__ void cp8(void* dst_smem, const void* src_gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst_smem)), "l"(src_gmem) : "memory");
 }
 
+// 4-byte variant.
+__device__ __forceinline__ void cp4(void* dst_smem, const void* src_gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst_smem)), "l"(src_gmem) : "memory");
+}
+
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
 // Wait until at most N of this thread's most recent groups are pending.

@@ -316,6 +316,7 @@ struct Engine final : EngineBase {
   int variant = 0;
   int vgrid[kVariants] = {};
   int nwarp_slots = 0;
+  int sgrid = 1;  // grid of the pipelined strain kernel (FP32 engines with bonds)
   bool primed = false;
   bool has_state = false;
   bool graph_on = true;
@@ -411,6 +412,16 @@ struct Engine final : EngineBase {
       nwarp_slots = std::max(nwarp_slots, vgrid[v] * (bs / 32));
     }
     P.ind_slots = nwarp_slots;
+    if (sizeof(T) == 4 && P.BMAX > 0) {
+      // the pipelined strain kernel: resident blocks per SM x SMs
+      int per_sm = 0;
+      TDEM_CUDA_TRY(&err, cudaFuncSetAttribute(reinterpret_cast<const void*>(&strain_kernel_async<float>),
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainSmem));
+      TDEM_CUDA_TRY(&err, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                              &per_sm, reinterpret_cast<const void*>(&strain_kernel_async<float>), kStrainBlock,
+                              kStrainSmem));
+      sgrid = std::max(1, std::min((int)((n + kStrainBlock - 1) / kStrainBlock), per_sm * sms));
+    }
     int rc = TDEM_OK;
     for (int b = 0; b < 2 && !rc; ++b) {
       if ((rc = alloc(&B.pos[b], n)) || (rc = alloc(&B.vel[b], n)) || (rc = alloc(&B.head[b], n)) ||
@@ -513,9 +524,16 @@ struct Engine final : EngineBase {
     if (P.BMAX > 0) {
       void* sargs[] = {&P, &B};
       cudaKernelNodeParams sk = {};
-      sk.func = reinterpret_cast<void*>(&strain_kernel<T>);
-      sk.gridDim = grid_n();
-      sk.blockDim = dim3(kThreads);
+      if constexpr (sizeof(T) == 4) {
+        sk.func = reinterpret_cast<void*>(&strain_kernel_async<T>);
+        sk.gridDim = dim3((unsigned)sgrid);
+        sk.blockDim = dim3(kStrainBlock);
+        sk.sharedMemBytes = (unsigned)kStrainSmem;
+      } else {
+        sk.func = reinterpret_cast<void*>(&strain_kernel<T>);
+        sk.gridDim = grid_n();
+        sk.blockDim = dim3(kThreads);
+      }
       sk.kernelParams = sargs;
       TDEM_CUDA_TRY(&err, cudaGraphAddKernelNode(&snode, g, dep, ndep, &sk));
       dep = &snode;
@@ -589,7 +607,11 @@ struct Engine final : EngineBase {
   }
 
   void launch_strain(cudaStream_t s) {
-    if (P.BMAX > 0) strain_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
+    if (P.BMAX <= 0) return;
+    if constexpr (sizeof(T) == 4)
+      strain_kernel_async<T><<<sgrid, kStrainBlock, kStrainSmem, s>>>(P, B);
+    else
+      strain_kernel<T><<<grid_n(), kThreads, 0, s>>>(P, B);
   }
 
   int prime(cudaStream_t s) {

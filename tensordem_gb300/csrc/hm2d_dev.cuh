@@ -392,49 +392,126 @@ __global__ void strain_kernel(Params<T> P, Bufs<T> B) {
       if (bc > 0) sv = shear_invariant<T>(g00, g01, g10, g11, pi);
       B.strain[i] = sv;
     }
-    return;
-  }
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int bc = B.bcnt[lp][i];
-    T sv = T(0);
-    if (bc > 0) {
-      const Params<T>& Q = MULTI ? B.iparams[B.inst[lp][i]] : P;
-      const V4<T>* pos = B.pos[sp];
-      const V4<T> p = pos[i];
-      T g00 = 0, g01 = 0, g10 = 0, g11 = 0;
-      // four slots at a time: their slot words, then their partner positions,
-      // then the sums (in slot order)
-      constexpr int KS = 4;
-      for (int s0 = 0; s0 < bc; s0 += KS) {
-        unsigned w[KS];
+  } else {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const int bc = B.bcnt[lp][i];
+      T sv = T(0);
+      if (bc > 0) {
+        const Params<T>& Q = MULTI ? B.iparams[B.inst[lp][i]] : P;
+        const V4<T>* pos = B.pos[sp];
+        const V4<T> p = pos[i];
+        T g00 = 0, g01 = 0, g10 = 0, g11 = 0;
+        // four slots at a time: their slot words, then their partner positions,
+        // then the sums (in slot order)
+        constexpr int KS = 4;
+        for (int s0 = 0; s0 < bc; s0 += KS) {
+          unsigned w[KS];
 #pragma unroll
-        for (int u = 0; u < KS; ++u)
-          if (s0 + u < bc) w[u] = B.bpart[lp][(size_t)(s0 + u) * P.n + i];
-        V4<T> q[KS];
-        V2<T> r[KS];
+          for (int u = 0; u < KS; ++u)
+            if (s0 + u < bc) w[u] = B.bpart[lp][(size_t)(s0 + u) * P.n + i];
+          V4<T> q[KS];
+          V2<T> r[KS];
 #pragma unroll
-        for (int u = 0; u < KS; ++u) {
-          if (s0 + u < bc) {
-            q[u] = pos[(int)(w[u] & kBondIdx)];
-            r[u] = B.bref[lp][(size_t)(s0 + u) * P.n + i];
+          for (int u = 0; u < KS; ++u) {
+            if (s0 + u < bc) {
+              q[u] = pos[(int)(w[u] & kBondIdx)];
+              r[u] = B.bref[lp][(size_t)(s0 + u) * P.n + i];
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < KS; ++u) {
+            if (s0 + u < bc) {
+              const V2<T> cur = cell_delta<T>(Q, p, q[u]);
+              const T ux = cur.x - r[u].x, uy = cur.y - r[u].y;
+              g00 += ux * r[u].x;
+              g01 += ux * r[u].y;
+              g10 += uy * r[u].x;
+              g11 += uy * r[u].y;
+            }
           }
         }
-#pragma unroll
-        for (int u = 0; u < KS; ++u) {
-          if (s0 + u < bc) {
-            const V2<T> cur = cell_delta<T>(Q, p, q[u]);
-            const T ux = cur.x - r[u].x, uy = cur.y - r[u].y;
-            g00 += ux * r[u].x;
-            g01 += ux * r[u].y;
-            g10 += uy * r[u].x;
-            g11 += uy * r[u].y;
-          }
-        }
+        sv = shear_invariant<T>(g00, g01, g10, g11, B.bpinv[lp][i]);
       }
-      sv = shear_invariant<T>(g00, g01, g10, g11, B.bpinv[lp][i]);
+      B.strain[i] = sv;
     }
+  }
+}
+
+// Pipelined strain for FP32 engines: a persistent grid in which each thread
+// stages its next disc's first round (count, own position, pseudo-inverse,
+// slot words, reference vectors) into shared memory with cp.async while it
+// gathers the current disc's partners and sums its bonds. The same sums in
+// the same order as strain_kernel. Layout [stage][slot][thread].
+constexpr int kStrainBlock = 256;
+constexpr size_t kStrainSmem = (size_t)2 * kStrainBlock * (kMaxBondSlots * (4 + 8) + 16 + 16 + 4);
+
+template <class T>
+__global__ void __launch_bounds__(kStrainBlock) strain_kernel_async(Params<T> P, Bufs<T> B) {
+  static_assert(sizeof(T) == 4, "the pipelined strain serves FP32 engines");
+  using bulk::cp16;
+  using bulk::cp4;
+  using bulk::cp8;
+  using bulk::cp_commit;
+  using bulk::cp_wait;
+  constexpr int BL = kStrainBlock, S = kMaxBondSlots;
+  extern __shared__ uint4 strain_smem[];
+  V4<T>* spos = reinterpret_cast<V4<T>*>(strain_smem);              // [2][BL]
+  V4<T>* spi = spos + 2 * BL;                                        // [2][BL]
+  V2<T>* sref = reinterpret_cast<V2<T>*>(spi + 2 * BL);              // [2][S][BL]
+  unsigned* sw = reinterpret_cast<unsigned*>(sref + 2 * S * BL);     // [2][S][BL]
+  int* sbc = reinterpret_cast<int*>(sw + 2 * S * BL);                // [2][BL]
+  const int sp = B.ctl->sp, lp = B.ctl->lp;
+  const int n = P.n, BM = P.BMAX;
+  const int t = threadIdx.x;
+  const int stride = gridDim.x * BL;
+  const V4<T>* __restrict__ pos = B.pos[sp];
+  const unsigned* __restrict__ bpart = B.bpart[lp];
+  const V2<T>* __restrict__ bref = B.bref[lp];
+  auto stage = [&](int i, int st) {
+    cp4(sbc + st * BL + t, B.bcnt[lp] + i);
+    cp16(spos + st * BL + t, pos + i);
+    cp16(spi + st * BL + t, B.bpinv[lp] + i);
+#pragma unroll
+    for (int u = 0; u < S; ++u) {
+      if (u < BM) {
+        const size_t k = (size_t)u * n + i;
+        cp4(sw + (st * S + u) * BL + t, bpart + k);
+        cp8(sref + (st * S + u) * BL + t, bref + k);
+      }
+    }
+  };
+  int i = blockIdx.x * BL + t;
+  if (i < n) stage(i, 0);
+  cp_commit();
+  for (int st = 0; i < n; i += stride, st ^= 1) {
+    const int i1 = i + stride;
+    if (i1 < n) stage(i1, st ^ 1);
+    cp_commit();
+    cp_wait<1>();  // this disc's staged loads have landed
+    const int bc = sbc[st * BL + t];
+    const V4<T> p = spos[st * BL + t];
+    V4<T> q[S];
+#pragma unroll
+    for (int u = 0; u < S; ++u)
+      if (u < bc) q[u] = pos[(int)(sw[(st * S + u) * BL + t] & kBondIdx)];
+    T g00 = 0, g01 = 0, g10 = 0, g11 = 0;
+#pragma unroll
+    for (int u = 0; u < S; ++u) {
+      if (u < bc) {
+        const V2<T> r = sref[(st * S + u) * BL + t];
+        const V2<T> cur = cell_delta<T>(P, p, q[u]);
+        const T ux = cur.x - r.x, uy = cur.y - r.y;
+        g00 += ux * r.x;
+        g01 += ux * r.y;
+        g10 += uy * r.x;
+        g11 += uy * r.y;
+      }
+    }
+    T sv = T(0);
+    if (bc > 0) sv = shear_invariant<T>(g00, g01, g10, g11, spi[st * BL + t]);
     B.strain[i] = sv;
   }
+  cp_wait<0>();
 }
 
 // Per-thread ledger terms of the particles a thread processed.
