@@ -236,7 +236,7 @@ def algorithmic_bytes(n: int, head_bytes: int, contact_sides: int, remainder: bo
     return n * (64 + head_bytes + (16 if remainder else 0)) + 16 * contact_sides
 
 
-def survey_bytes(n: int, k: int, c: int, b: int, r: float) -> float:
+def cell_list_bytes(n: int, k: int, c: int, b: int, r: float) -> float:
     """The hot-path byte model N*64 + K*4 + C*16 + B*20 + 96*N/R: particle
     state read and written, one 4-byte candidate index per candidate pair, 16 B
     of history per active contact, 20 B per bond, and the rebuild's sort
@@ -477,11 +477,11 @@ def run_ours(a) -> None:
     peak, peak_kind = measured_peak()
     achieved = alg / (kernel_ms / 1e3) / 1e9
     traffic = profiled_traffic()
-    sb = survey_bytes(n, k_pairs, c_contacts, 0, r_interval)
+    sb = cell_list_bytes(n, k_pairs, c_contacts, 0, r_interval)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_step": alg,
-                "survey_model": {"bytes_per_step": sb, "achieved": sb / (kernel_ms / 1e3) / 1e9,
+                "cell_list_model": {"bytes_per_step": sb, "achieved": sb / (kernel_ms / 1e3) / 1e9,
                                  "frac": sb / (kernel_ms / 1e3) / 1e9 / peak,
                                  "N": n, "K": k_pairs, "C": c_contacts, "B": 0, "R": r_interval},
                 "dram": None if traffic is None else {
