@@ -217,7 +217,8 @@ void launch_rebuild_seq(const Params<T>& P, const Bufs<T>& B, cudaStream_t s) {
 // shared memory; 7..8 = per-thread cp.async pipeline, three discs deep, at 3
 // and 4 blocks per SM; 9..10 = the same pipeline with one 1024-thread CTA
 // per SM, CTA-major and warp-major chunk order; 11 = the pipeline with one
-// 512-thread CTA per SM (128 registers: the bonded build without spills).
+// 512-thread CTA per SM (128 registers: the bonded build without spills; it
+// also stages each disc's bond slot words one disc ahead).
 // Variants 6..11 are FP32 kernels; an FP64 engine runs variant 1's kernel
 // for them.
 constexpr int kVariants = 12;
@@ -241,10 +242,10 @@ StepFn<T> window_fn() {
 }
 
 // The cp.async pipeline for FP32 engines; variant 1's kernel for FP64.
-template <class T, int MODE, int MINB, bool F, int BLOCK = 256, bool WMAJ = false>
+template <class T, int MODE, int MINB, bool F, int BLOCK = 256, bool WMAJ = false, bool PW = false>
 StepFn<T> async_fn() {
   if constexpr (sizeof(T) == 4)
-    return &force_kernel_async<T, MODE, BLOCK, MINB, F, WMAJ>;
+    return &force_kernel_async<T, MODE, BLOCK, MINB, F, WMAJ, PW>;
   else
     return &force_kernel_pf<T, MODE, 256, 3, F>;
 }
@@ -269,7 +270,7 @@ StepFn<T> step_fn_mode(int variant) {
     case kAsyncVariant + 1: return async_fn<T, MODE, 4, F>();
     case kAsyncWideVariant: return async_fn<T, MODE, 1, F, kWideBlock>();
     case kAsyncWideVariant + 1: return async_fn<T, MODE, 1, F, kWideBlock, true>();
-    case kAsyncHalfVariant: return async_fn<T, MODE, 1, F, kWideBlock / 2, true>();
+    case kAsyncHalfVariant: return async_fn<T, MODE, 1, F, kWideBlock / 2, true, F>();
     default: return &force_kernel<T, MODE, F>;
   }
 }
@@ -463,7 +464,13 @@ struct Engine final : EngineBase {
   bool feat() const { return P.BMAX > 0 || P.irad > T(0); }
   // launch shape of a variant's step kernel (the FP64-sum form has one shape)
   int block_of(int v) const { return sum64 ? 256 : variant_block<T>(v); }
-  size_t smem_of(int v) const { return sum64 ? 0 : variant_smem<T>(v, P.prem != 0); }
+  size_t smem_of(int v) const {
+    if (sum64) return 0;
+    // variant 11's bonded build stages the bond slot words too
+    const size_t bond = (v == kAsyncHalfVariant && sizeof(T) == 4 && feat()) ? async_bond_smem(kWideBlock / 2, P.BMAX)
+                                                                              : 0;
+    return variant_smem<T>(v, P.prem != 0) + bond;
+  }
   dim3 grid_n() const { return dim3((unsigned)nblocks); }
   dim3 grid_keys() const { return dim3((unsigned)((P.nkeys + kThreads - 1) / kThreads)); }
 

@@ -779,13 +779,15 @@ __device__ __forceinline__ void load_head_partners(const F& fetch, const uint4& 
 
 // process_particle with the first three partners' positions already loaded.
 // rem_pre: the disc's position remainder when the caller has it already
-// (null: loaded here).
-template <class T, int MODE, bool FEAT, class F, bool S64 = false>
+// (null: loaded here). PREW: the caller has staged the disc's bond slot
+// words (pw[u * pw_stride]), bond count and strain.
+template <class T, int MODE, bool FEAT, class F, bool S64 = false, bool PREW = false>
 __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Bufs<T>& B, const F& fetch, int sp,
                                                    int lp, int i, const V4<T>& p, const V4<T>& v, const uint4& hd,
                                                    const V4<T>& q0, const V4<T>& q1, const V4<T>& q2, int primed,
                                                    long long eval, ThreadLedger<T>& L,
-                                                   const float2* rem_pre = nullptr) {
+                                                   const float2* rem_pre = nullptr, const unsigned* pw = nullptr,
+                                                   int pw_stride = 0, int pbc = 0, T psi = T(0)) {
   constexpr bool COMMIT = MODE != kPeek;
   const int n = P.n;
   const unsigned* __restrict__ tail = B.nbr[lp];
@@ -805,10 +807,10 @@ __device__ __forceinline__ void process_particle_q(const Params<T>& P, const Buf
     unsigned wds[kMaxBondSlots];
 #pragma unroll
     for (int u = 0; u < kMaxBondSlots; ++u)
-      if (u < P.BMAX) wds[u] = B.bpart[lp][(size_t)u * n + i];
-    const int bc = B.bcnt[lp][i];
+      if (u < P.BMAX) wds[u] = PREW ? pw[u * pw_stride] : B.bpart[lp][(size_t)u * n + i];
+    const int bc = PREW ? pbc : B.bcnt[lp][i];
     if (bc > 0) {
-      const T si = B.strain[i];
+      const T si = PREW ? psi : B.strain[i];
       constexpr int KB = 2;  // bond slots whose partner loads are in flight together
 #pragma unroll
       for (int s0 = 0; s0 < kMaxBondSlots; s0 += KB) {
@@ -1218,7 +1220,11 @@ constexpr size_t async_smem(int block, bool prem) {
 // grid warp w * G + b), so that when the chunk count is not a multiple of
 // the grid's warps, the warps with one chunk fewer are spread over all CTAs
 // instead of filling the last CTAs (which then idle their SMs early).
-template <class T, int MODE, int BLOCK, int MINB, bool FEAT, bool WMAJ = false>
+// PW (engines with bonds): each disc's bond slot words, bond count and strain
+// are staged with its own state, one disc ahead, into [2][BMAX][BLOCK] words,
+// [2][BLOCK] counts and [2][BLOCK] strains after the records above, so the
+// bond partners' gathers start without a dependent load.
+template <class T, int MODE, int BLOCK, int MINB, bool FEAT, bool WMAJ = false, bool PW = false>
 __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, Bufs<T> B,
                                                                   cudaGraphConditionalHandle h_rebuild,
                                                                   cudaGraphConditionalHandle h_loop, int use_cond,
@@ -1247,6 +1253,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
   const uint4* __restrict__ head = B.head[lp];
   const GlobalFetch<T> fetch{pos, vel};
   ThreadLedger<T> L;
+  // bond staging (PW): slot words, counts and strains of the disc in flight
+  const int BM = (PW && FEAT) ? P.BMAX : 0;
+  unsigned* sbw = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned char*>(async_smem_base) +
+                                              (size_t)kAsyncRecords * BLOCK * 16 + (pr ? (size_t)2 * BLOCK * 8 : 0));
+  int* sbc = reinterpret_cast<int*>(sbw + 2 * BM * BLOCK);
+  T* ssi = reinterpret_cast<T*>(sbc + 2 * BLOCK);
+  auto stage_bonds = [&](int d, int s) {
+    if (BM > 0) {
+      for (int u = 0; u < BM; ++u) bulk::cp4(sbw + (s * BM + u) * BLOCK + t, B.bpart[lp] + (size_t)u * end + d);
+      bulk::cp4(sbc + s * BLOCK + t, B.bcnt[lp] + d);
+      bulk::cp4(ssi + s * BLOCK + t, B.strain + d);
+    }
+  };
   // partner positions of the disc whose head sits in head slot h, into set s
   auto gather = [&](int h, int s) {
     const uint4 hd = sh[h * BLOCK + t];
@@ -1264,6 +1283,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
     cp16(spos + t, pos + i);
     cp16(svel + t, vel + i);
     if (pr) cp8(srem + t, prem + i);
+    stage_bonds(i, 0);
   }
   if (i + stride < end) cp16(sh + BLOCK + t, head + i + stride);
   cp_commit();
@@ -1281,6 +1301,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
       cp16(spos + (s ^ 1) * BLOCK + t, pos + i1);
       cp16(svel + (s ^ 1) * BLOCK + t, vel + i1);
       if (pr) cp8(srem + (s ^ 1) * BLOCK + t, prem + i1);
+      stage_bonds(i1, s ^ 1);
     }
     cp_commit();
     cp_wait<2>();  // X_{k-1} landed: the head of disc k+1
@@ -1298,13 +1319,22 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
     if (cnt > 1) q1 = q[BLOCK];
     if (cnt > 2) q2 = q[2 * BLOCK];
     const float2 rm = pr ? srem[s * BLOCK + t] : make_float2(0.0f, 0.0f);
-    process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, c.evals, L, &rm);
+    if constexpr (PW && FEAT) {
+      process_particle_q<T, MODE, FEAT, GlobalFetch<T>, false, true>(
+          P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, c.evals, L, &rm, sbw + s * BM * BLOCK + t, BLOCK,
+          BM > 0 ? sbc[s * BLOCK + t] : 0, BM > 0 ? ssi[s * BLOCK + t] : T(0));
+    } else {
+      process_particle_q<T, MODE, FEAT>(P, B, fetch, sp, lp, i, p, v, hd, q0, q1, q2, primed, c.evals, L, &rm);
+    }
     h0 = h1;
     s ^= 1;
   }
   cp_wait<0>();
   commit_epilogue<T, FEAT>(P, B, c, L, h_rebuild, h_loop, use_cond);
 }
+
+// Shared memory of the bond staging of a PW pipelined kernel.
+inline size_t async_bond_smem(int block, int bmax) { return (size_t)2 * block * ((size_t)bmax * 4 + 4 + 4); }
 
 // Neighbour-window variant (FP32). Each CTA (one per SM) owns a contiguous
 // range of sorted particles and walks it two ring blocks (2 x 256 particles)
