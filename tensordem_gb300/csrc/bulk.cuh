@@ -96,6 +96,12 @@ __device__ __forceinline__ void cp4(void* dst_smem, const void* src_gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst_smem)), "l"(src_gmem) : "memory");
 }
 
+// Bulk prefetch of [src, src + bytes) into L2 (16-byte aligned, bytes a
+// multiple of 16, inside the array).
+__device__ __forceinline__ void prefetch_l2(const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
 // Wait until at most N of this thread's most recent groups are pending.

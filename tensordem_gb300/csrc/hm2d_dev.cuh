@@ -1264,6 +1264,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) force_kernel_async(Params<T> P, B
       for (int u = 0; u < BM; ++u) bulk::cp4(sbw + (s * BM + u) * BLOCK + t, B.bpart[lp] + (size_t)u * end + d);
       bulk::cp4(sbc + s * BLOCK + t, B.bcnt[lp] + d);
       bulk::cp4(ssi + s * BLOCK + t, B.strain + d);
+      // the warp's 32 discs' reference vectors, histories and strengths
+      // towards L2 (one row segment of one slot array per lane; whole warps
+      // only, each range rounded inwards to 16-byte bounds)
+      const int lane = t & 31, base = d - lane;
+      if (WMAJ && base + 32 <= end && lane < 3 * BM) {
+        const int u = lane / 3, a = lane - 3 * u;
+        const size_t k = (size_t)u * end + base;
+        const char* lo = a == 0   ? reinterpret_cast<const char*>(B.bref[lp] + k)
+                         : a == 1 ? reinterpret_cast<const char*>(B.bus[lp] + k)
+                                  : reinterpret_cast<const char*>(B.bstr[lp] + k);
+        const char* hi = lo + 32 * (a == 2 ? sizeof(T) : sizeof(V2<T>));
+        const uintptr_t l16 = ((uintptr_t)lo + 15) & ~(uintptr_t)15, h16 = (uintptr_t)hi & ~(uintptr_t)15;
+        if (h16 > l16) bulk::prefetch_l2(reinterpret_cast<const void*>(l16), (unsigned)(h16 - l16));
+      }
     }
   };
   // partner positions of the disc whose head sits in head slot h, into set s
