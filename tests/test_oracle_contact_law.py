@@ -159,3 +159,39 @@ def test_restitution_map_is_zero_at_one_monotonic_and_invertible():
 def test_invalid_restitution_is_rejected(e):
     with pytest.raises(ValueError):
         tsuji_beta(e)
+
+
+def test_normal_dashpot_adds_the_viscous_term_while_approaching_and_clamps_at_zero():
+    """The reference's dashpot convention (tests/test_contact_mindlin_history.py:148-156):
+    F_n = max(F_el + gamma sqrt(S_n m*) v_n, 0) with v_n > 0 while approaching."""
+    delta = 1e-4
+    p = _params(restitution=0.5)
+    s_n, _ = _stiffness(delta)
+    meff = 0.5
+    approach = _one(p, delta, vel_a=(0.2, 0.0))
+    expect = approach["f_el"][0] + p.damp * math.sqrt(s_n * meff) * 0.2
+    assert approach["f_n"][0] == pytest.approx(expect, rel=1e-12)
+    assert approach["dashpot_loss"] > 0.0
+    fast_out = _one(p, delta, vel_a=(-1e3, 0.0))  # separating fast: the dashpot would pull
+    assert fast_out["f_n"][0] == 0.0
+
+
+def test_separated_pairs_forget_their_history():
+    """A contact that opens drops its tangential history; when the two discs
+    touch again the history starts from zero (the reference's
+    tests/test_contact_mindlin_history.py:133-146, inactive contacts forget)."""
+    from oracle.hm2d import HM2DOracle
+    r = np.full(2, R)
+    m = np.ones(2)
+    inertia = 0.5 * m * r * r
+    p = _params(mu=10.0, dt=1e-3)  # sticks: 320 N of spring against a 518 N cap
+    o = HM2DOracle(np.array([[0.0, 0.0], [2 * R - 1e-4, 0.0]]), np.zeros((2, 2)), np.zeros(2), r, m, inertia, p)
+    touching = o.pos.copy()
+    moving = np.array([[0.0, 0.5], [0.0, 0.0]])  # tangential sliding of disc 0
+    o.evaluate(touching, moving, np.zeros(2), advance=True)
+    assert len(o.state.keys) == 1 and abs(o.state.xi[0, 1]) > 0.0
+    apart = np.array([[0.0, 0.0], [2 * R + 1e-4, 0.0]])
+    o.evaluate(apart, np.zeros((2, 2)), np.zeros(2), advance=True)
+    assert len(o.state.keys) == 0
+    force, torque, _ = o.evaluate(touching, np.zeros((2, 2)), np.zeros(2), advance=False)
+    assert force[0, 1] == 0.0 and force[1, 1] == 0.0 and np.all(torque == 0.0)
