@@ -195,3 +195,31 @@ def test_separated_pairs_forget_their_history():
     assert len(o.state.keys) == 0
     force, torque, _ = o.evaluate(touching, np.zeros((2, 2)), np.zeros(2), advance=False)
     assert force[0, 1] == 0.0 and force[1, 1] == 0.0 and np.all(torque == 0.0)
+
+
+def test_disc_launched_on_a_frictional_floor_leaves_rolling_at_two_thirds():
+    """The reference's analytic sliding-disc anchor
+    (tests/test_granular2d_column_collapse.py:55-79): a uniform disc launched
+    at v0 on a floor with friction spins up and leaves rolling without slip
+    at 2 v0 / 3; the friction work is m v0^2 / 6, and the ledger closes on
+    it. Here with the oracle's Hertz floor and Mindlin spring (no dashpot),
+    the disc starting at its static overlap."""
+    from oracle.hm2d import HM2DOracle, rayleigh_dt
+    r, rho, young, nu, g, mu, v0 = 0.01, 1000.0, 1e7, 0.3, 9.81, 0.3, 0.5
+    m = rho * math.pi * r * r
+    inertia = 0.5 * m * r * r
+    overlap = (3.0 * m * g / (4.0 * effective_modulus(young, nu) * math.sqrt(r))) ** (2.0 / 3.0)
+    dt = 0.05 * rayleigh_dt(r, rho, young, nu)
+    p = HMParams(young=young, poisson=nu, restitution=1.0, mu=0.0, mu_wall=mu, dt=dt, gravity=(0.0, -g),
+                 box=(1.0, 0.2), walls=(True, False, True, False), skin=0.1 * r)
+    o = HM2DOracle(np.array([[0.1, r - overlap]]), np.array([[v0, 0.0]]), np.zeros(1), np.array([r]),
+                   np.array([m]), np.array([inertia]), p)
+    e0 = o.energies()
+    o.step(int(1.3 * v0 / (3.0 * mu * g) / dt))  # 30% past the analytic end of slip
+    e1 = o.energies()
+    analytic = m * v0 * v0 / 6.0
+    assert o.vel[0, 0] == pytest.approx(2.0 * v0 / 3.0, rel=0.01)
+    assert abs(o.vel[0, 0] + o.omega[0] * r) < 0.01 * v0  # rolling, up to the spring's micro-slip
+    assert o.dissipated == pytest.approx(analytic, rel=0.01)
+    stored = lambda e: e["kinetic"] + e["potential"] + e["elastic_normal"] + e["elastic_tangential"]
+    assert abs(stored(e0) - stored(e1) - o.dissipated) < 1e-3 * analytic
