@@ -64,7 +64,7 @@ def test_cpu_baseline_runs_the_oracle_on_every_requested_core():
 
 
 def test_reference_arm_prints_the_contract_line():
-    """`bench.py --impl reference` (the driver's reference arm) prints one
+    """`bench.py --impl reference` (the bench's reference arm) prints one
     JSON line with the GPU arm's metric and unit, a cpu_baseline object
     describing its own run and an e2e object with no host-device copies."""
     import json
