@@ -7,7 +7,8 @@ Anchors restated from the reference's own tests: Hertz normal law
 (tests/test_scale_ceiling_dem.py:130-144), elastic energy conservation and
 free flight (:147-172), Coulomb cycle area
 (src/tensordem/contact_tangential.py:215-256), brute-force pair sets (:41-50),
-and the Hertz contact duration of tests/test_dem3d_hertz_impact_time.py.
+the Hertz contact duration of tests/test_dem3d_hertz_impact_time.py and the
+second-order convergence of tests/test_dem3d_integration_order.py.
 """
 
 import math
@@ -176,3 +177,28 @@ def test_hertz_contact_duration_matches_the_johnson_closed_form():
         assert rebound == pytest.approx(1.0, abs=1e-7)
     slope = np.polyfit(np.log(speeds), np.log([t for t, _, _ in runs]), 1)[0]
     assert slope == pytest.approx(-0.2, abs=1e-6)
+
+
+def test_velocity_verlet_is_second_order_through_a_hertz_contact():
+    """The integration-order check of the reference's 3-D suite
+    (tests/test_dem3d_integration_order.py) on the oracle's 2-D step: halving
+    dt quarters the position and velocity errors at a fixed time inside a
+    head-on Hertz contact (reference: 64,000 steps per contact time)."""
+    r, v0 = 1e-3, 1.0
+    st0 = two_disc_state(delta=2e-6, r=r)
+    mstar, rstar = 0.5 * st0["mass"][0], 0.5 * r
+    k_h = (4.0 / 3.0) * effective_modulus(E, NU) * math.sqrt(rstar)
+    t_c = 2.9432751843247047 * (5.0 * mstar / (4.0 * k_h)) ** 0.4 * v0 ** -0.2
+
+    def state_at(per_contact):
+        st = dict(st0, vel=np.array([[0.5 * v0, 0.0], [-0.5 * v0, 0.0]]))
+        o = HM2DOracle(**st, params=_params(dt=t_c / per_contact))
+        o.step(int(round(0.3 * per_contact)))  # the same end time 0.3 t_c for every dt
+        return o.pos[1, 0] - o.pos[0, 0], o.vel[0, 0]
+
+    ref = state_at(64000)
+    runs = [state_at(n) for n in (500, 1000, 2000, 4000)]
+    for k in (0, 1):
+        err = [abs(s[k] - ref[k]) for s in runs]
+        ratios = [err[i] / err[i + 1] for i in range(3)]
+        assert all(3.9 < q < 4.1 for q in ratios), (k, ratios)
